@@ -1,0 +1,217 @@
+/*
+ * lattice_gpu.h — C ABI of the GB300 lattice-evolution library (liblattice_gpu.so).
+ *
+ * The reference (sjcott/Axions) has no library boundary: its hot path is the
+ * body of the time-step loop inside main() of four programs.  Each entry point
+ * below names the loop-body fragment it replaces (reference file:line).  The
+ * C++ drop-in programs (in axions_gb300/host/) and the Python mirror
+ * (axions_gb300/lattice.py) call only these functions.
+ *
+ * Conventions
+ *   - Every function returns int status: LAT_OK (0) or a negative LAT_ERR_*.
+ *     lat_last_error() returns a message for the calling thread's last error.
+ *     No C++ exception crosses this boundary and no device code traps.
+ *   - Device memory is owned by the handle.  Host buffers are owned by the
+ *     caller and copied synchronously (the call returns when the copy is done).
+ *   - Field layout on the host is the reference's: one contiguous array per
+ *     component, sites in linear order (i*ny + j)*nz + k (z fastest), i.e. the
+ *     `pos` of calcInd() in mpi_evolution.cpp:62 and Array(..,i,j,k) in
+ *     array.cpp:66-94.  Component order:
+ *        Abelian-Higgs: phi_re, phi_im, theta_x, theta_y, theta_z   (5)
+ *        Moore:         phi1_re, phi1_im, phi2_re, phi2_im,
+ *                       theta_x, theta_y, theta_z                    (7)
+ *     theta_mu is the link phase g*d_mu*A_mu (ic.txt columns,
+ *     initialConditions.cpp:539).
+ *   - Time levels follow the reference's two-slot scheme: at time step n the
+ *     "now" level is slot (n+1)%2 and the "past" level slot n%2
+ *     (mpi_evolution.cpp:370-371); a step writes the new level into the past
+ *     slot in place (mpi_evolution.cpp:432,499-501).
+ *   - One host thread per handle.  Handles are independent of one another.
+ */
+#ifndef AXIONS_LATTICE_GPU_H
+#define AXIONS_LATTICE_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LAT_ABI_VERSION 1
+
+/* status codes */
+#define LAT_OK             0
+#define LAT_ERR_INVALID   -1  /* bad argument or parameter combination      */
+#define LAT_ERR_NOMEM     -2  /* device or host allocation failed            */
+#define LAT_ERR_CUDA      -3  /* CUDA runtime error                          */
+#define LAT_ERR_TIMEOUT   -4  /* a bounded device wait gave up               */
+#define LAT_ERR_CAPACITY  -5  /* caller buffer too small (count still valid) */
+#define LAT_ERR_STATE     -6  /* call not valid in the handle's state        */
+#define LAT_ERR_NODEVICE  -7  /* no CUDA device / kernel image not loadable  */
+
+/* models */
+#define LAT_MODEL_AH     0   /* Abelian-Higgs: evolution.cpp, mpi_evolution.cpp       */
+#define LAT_MODEL_MOORE  1   /* two scalars: mooreEvol.cpp, moore_mpi_evolution.cpp  */
+
+/* precision of the stored fields and of the step arithmetic */
+#define LAT_F64 0            /* the reference's arithmetic                          */
+#define LAT_F32 1            /* FP32 fields and step; energy/Gauss sums stay FP64   */
+
+/* boundary handling */
+#define LAT_BC_PERIODIC 0    /* periodic in x, y, z (mpi_evolution.cpp:385-405)             */
+#define LAT_BC_FIXED    1    /* only interior sites evolve; the outer layer of sites is
+                                held fixed (evolution.cpp:166-186 with xyBC/zBC "fixed";
+                                mooreEvol.cpp:187-189,672-692)                               */
+
+/* energy density variants (diagnostics) */
+#define LAT_ENERGY_EVOLUTION 0  /* evolution.cpp:322-334,398-427 and mooreEvol.cpp:341-391:
+                                   gauge kinetic term (dtheta/(g*dt*dmu))^2/2, zero if g==0  */
+#define LAT_ENERGY_MPI       1  /* mpi_evolution.cpp:509-532, moore_mpi_evolution.cpp:558-588:
+                                   gauge kinetic term (dtheta/dt)^2/2, always included      */
+
+/* gauge current of the Moore model */
+#define LAT_MOORE_CURRENT_PLAIN  0  /* j1 + j2 without charges (moore_mpi_evolution.cpp:498-515) */
+#define LAT_MOORE_CURRENT_CHARGE 1  /* q1*j1 + q2*j2 (mooreEvol.cpp:295-312)                     */
+
+/* which scalar a detection call looks at */
+#define LAT_FIELD_PHI1 0     /* phi (AH) or phi1 (Moore) */
+#define LAT_FIELD_PHI2 1     /* phi2 (Moore only)        */
+
+/*
+ * Parameters.  Names and meaning follow the reference's compile-time
+ * constants (mpi_evolution.cpp:15-60, moore_mpi_evolution.cpp:15-65,
+ * evolution.cpp:23-58, mooreEvol.cpp:19-42).  lat_params_init() fills the
+ * defaults of mpi_evolution.cpp (AH) or moore_mpi_evolution.cpp (Moore).
+ */
+typedef struct lat_params {
+    int32_t abi_version;   /* must be LAT_ABI_VERSION                                   */
+    int32_t model;         /* LAT_MODEL_*                                                */
+    int32_t precision;     /* LAT_F64 / LAT_F32                                          */
+    int32_t bc;            /* LAT_BC_*                                                   */
+    int64_t nx, ny, nz;    /* lattice sides; nx*ny*nz < 2^31                             */
+    double dx, dy, dz, dt;
+    double lambda;         /* AH lambda; Moore lambda1                                   */
+    double eta;            /* AH eta;    Moore eta1                                      */
+    double lambda2;        /* Moore only                                                 */
+    double eta2;           /* Moore only                                                 */
+    double lambda12;       /* Moore only: cross coupling                                 */
+    double g;              /* gauge coupling                                             */
+    double q1, q2;         /* Moore charges (reference: const int)                       */
+    int32_t damped_nt;     /* damping applies while TimeStep < damped_nt                 */
+    int32_t moore_current; /* LAT_MOORE_CURRENT_*                                        */
+    double dampFac;        /* damping coefficient while damped                           */
+    double alpha;          /* PRS friction factor on the scalars                         */
+    double scaling;        /* scale-factor power; friction = alpha*scaling/tau           */
+    double tau0;           /* conformal time at step 0: tau = tau0 + TimeStep*dt (=1)    */
+    int32_t energy_form;   /* LAT_ENERGY_*                                               */
+    int32_t reserved0;
+    double reserved[4];
+} lat_params;
+
+typedef struct lat_handle lat_handle;
+
+/* Result of one diagnostic step: energy of the level before the update and the
+ * Gauss-law deviation summed over the evolved sites (the reference's
+ * deviationParameter before its normalisation, evolution.cpp:419,1404-1408). */
+typedef struct lat_diag {
+    double energy;         /* sum over evolved sites of rho*dx*dy*dz                     */
+    double gauss_abs_sum;  /* sum over evolved sites of |G|  (0 when g == 0)             */
+    int64_t sites;         /* number of evolved sites summed over                        */
+    int64_t time_step;     /* TimeStep the values belong to                              */
+} lat_diag;
+
+/* ---- library ---------------------------------------------------------------- */
+const char* lat_version(void);
+const char* lat_last_error(void);
+
+/* Fill reference defaults for a model.  Replaces the const blocks
+ * mpi_evolution.cpp:15-60 / moore_mpi_evolution.cpp:15-65. */
+int lat_params_init(lat_params* p, int32_t model);
+
+/* Host-side seeded random-phase initial condition, both levels equal, theta=0.
+ * Replaces mpi_evolution.cpp:287-312 (AH) and moore_mpi_evolution.cpp:293-323
+ * (Moore): mt19937(seed), uniform_real_distribution<double>(0, 2*pi), one draw
+ * per site in linear order, phi = eta*(cos, sin).  For Moore, independent != 0
+ * draws phi1's phase then phi2's phase per site from the same stream (an
+ * extension; the reference gives both scalars the same phase,
+ * moore_mpi_evolution.cpp:309-313).  `fields` is [ncomp][nx*ny*nz]. */
+int lat_random_phase_ic(const lat_params* p, uint32_t seed, int32_t independent,
+                        double* fields);
+
+/* ---- lattice handle ----------------------------------------------------------- */
+/* Allocate the two-level state of one lattice on the current CUDA device.
+ * Replaces the field vectors of mpi_evolution.cpp:94 (no halo: the whole
+ * lattice is resident and the periodic wrap is done in-kernel). */
+int lat_create(const lat_params* p, lat_handle** out);
+int lat_destroy(lat_handle* h);
+
+/* Launch all work of this handle on `stream` (a cudaStream_t); NULL restores
+ * the handle's own stream. */
+int lat_set_stream(lat_handle* h, void* stream);
+
+int lat_get_params(const lat_handle* h, lat_params* out);
+int lat_num_components(const lat_handle* h);
+int64_t lat_time_step(const lat_handle* h);
+/* bytes of device memory the handle holds */
+int64_t lat_device_bytes(const lat_handle* h);
+
+/* Upload the state: `now` is the level at TimeStep `time_step`, `past` the one
+ * before (for a stationary start pass the same array twice, as
+ * mpi_evolution.cpp:155-162 does).  Each is [ncomp][nx*ny*nz] doubles; FP32
+ * handles convert on the device.  Replaces the IC load mpi_evolution.cpp:143-285. */
+int lat_set_state(lat_handle* h, const double* now, const double* past, int64_t time_step);
+/* Download the state; either pointer may be NULL. */
+int lat_get_state(lat_handle* h, double* now, double* past);
+
+/* Advance `nsteps` leapfrog steps without diagnostics.  Replaces the per-site
+ * EoM + in-place update of mpi_evolution.cpp:381-501 (AH) and
+ * moore_mpi_evolution.cpp:405-550 (Moore), and the halo exchange
+ * mpi_evolution.cpp:925-943, which is not needed on one resident lattice. */
+int lat_step(lat_handle* h, int32_t nsteps);
+
+/* One step that also returns the energy and Gauss deviation of the level it
+ * starts from.  Replaces evolution.cpp:273-431 + 1384-1408 and
+ * mooreEvol.cpp:187-395 + 672-692 (one step of the loop with its valsPerLoop
+ * values). */
+int lat_step_diag(lat_handle* h, lat_diag* out);
+
+/* Run `nsteps` steps; at every step n with n % diag_every == 0 (diag_every > 0)
+ * record a lat_diag into `out` (capacity `cap` entries, `*count` = entries
+ * written).  Diagnostics stay on the device until the end of the call. */
+int lat_advance(lat_handle* h, int32_t nsteps, int32_t diag_every,
+                lat_diag* out, int64_t cap, int64_t* count);
+
+/* Diagnostics of the current level without stepping (read-only). */
+int lat_diagnostics(lat_handle* h, lat_diag* out);
+
+/* Bilinear string-crossing detection on the current ("now") level of one
+ * scalar.  Replaces mpi_evolution.cpp:536-789 (+ the gather :795-888) and
+ * evolution.cpp:723-1016.  Writes `*count` crossings as xyz triples
+ * (x0,y0,z0,x1,...) in the reference's order: sites in linear order, and per
+ * site the z-directed face, the y-directed face, the x-directed face, each with
+ * its "+sqrt" root before its "-sqrt" root.  Coordinates are (i - x0)*dx with
+ * x0 = int((nx-1)/2) (mpi_evolution.cpp:131-133,547-549).  If cap is too small
+ * the first `cap` triples are written, *count holds the full count and the call
+ * returns LAT_ERR_CAPACITY.  xyz may be NULL with cap 0 to query the count. */
+int lat_detect_crossings(lat_handle* h, int32_t field, double* xyz, int64_t cap,
+                         int64_t* count);
+
+/* Integer winding of the scalar's phase around every plaquette of the current
+ * level (no counterpart in the reference, which has only the bilinear
+ * detection above; followString.cpp:1-262 is an unfinished fragment).
+ * out (may be NULL) is int8 [3][nx*ny*nz]: out[d*N + s] is the winding (-1, 0
+ * or +1) of the face with normal d (0=x, 1=y, 2=z) whose lowest corner is site
+ * s, traversed counter-clockwise about +d:
+ *   d=x: s, s+y, s+y+z, s+z    d=y: s, s+z, s+z+x, s+x    d=z: s, s+x, s+x+y, s+y
+ * Each edge a->b contributes the signed crossing of the ray Re>0, Im=0 decided
+ * by the sign of Re(a)Im(b) - Im(a)Re(b) (products rounded separately, no FMA),
+ * so results are bit-exact between host and device.  *abs_sum (may be NULL)
+ * is the sum of |winding| over all faces.  With LAT_BC_FIXED faces that leave
+ * the lattice are 0. */
+int lat_winding(lat_handle* h, int32_t field, int8_t* out, int64_t* abs_sum);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AXIONS_LATTICE_GPU_H */

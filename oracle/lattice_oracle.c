@@ -1,0 +1,704 @@
+/*
+ * lattice_oracle.c — CPU restatement of the reference's lattice hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker for the CUDA library; see the header).
+ *
+ * Every expression keeps the reference's operation order, so that with
+ * -ffp-contract=off and the same libm this file reproduces the reference's
+ * doubles bit for bit (checked against fixtures made by running the reference;
+ * tests/test_oracle_golden.py).  pow(x,2) is written x*x, which is what g++ -O3
+ * emits for the reference's pow(x,2).
+ */
+#include "lattice_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------------- */
+/* RNG: mt19937 (Matsumoto & Nishimura 1998) and libstdc++'s                  */
+/* generate_canonical<double,53> / uniform_real_distribution                  */
+/* ------------------------------------------------------------------------- */
+
+void orc_mt_seed(orc_mt19937* g, uint32_t seed)
+{
+    g->mt[0] = seed;
+    for (int i = 1; i < 624; ++i)
+        g->mt[i] = 1812433253u * (g->mt[i - 1] ^ (g->mt[i - 1] >> 30)) + (uint32_t)i;
+    g->idx = 624;
+}
+
+static void orc_mt_twist(orc_mt19937* g)
+{
+    for (int i = 0; i < 624; ++i) {
+        uint32_t y = (g->mt[i] & 0x80000000u) | (g->mt[(i + 1) % 624] & 0x7fffffffu);
+        uint32_t v = g->mt[(i + 397) % 624] ^ (y >> 1);
+        if (y & 1u) v ^= 0x9908b0dfu;
+        g->mt[i] = v;
+    }
+    g->idx = 0;
+}
+
+uint32_t orc_mt_next(orc_mt19937* g)
+{
+    if (g->idx >= 624) orc_mt_twist(g);
+    uint32_t y = g->mt[g->idx++];
+    y ^= (y >> 11);
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= (y >> 18);
+    return y;
+}
+
+/* uniform_real_distribution<double>(0, 2*pi) with pi = 4*atan(1)
+ * (mpi_evolution.cpp:12,291): u = (g1 + g2*2^32) / 2^64, clamped below 1,
+ * value = u*(b - a) + a. */
+double orc_uniform_0_2pi(orc_mt19937* g)
+{
+    double sum = 0.0;
+    double tmp = 1.0;
+    sum += (double)orc_mt_next(g) * tmp;
+    tmp *= 4294967296.0;
+    sum += (double)orc_mt_next(g) * tmp;
+    tmp *= 4294967296.0;
+    double u = sum / tmp;
+    if (u >= 1.0) u = nextafter(1.0, 0.0);
+    const double pi = 4.0 * atan(1.0);
+    const double b = 2 * pi, a = 0.0;
+    return u * (b - a) + a;
+}
+
+static int ncomp_of(const lat_params* p) { return p->model == LAT_MODEL_MOORE ? 7 : 5; }
+
+int orc_random_phase_ic(const lat_params* p, uint32_t seed, int independent, double* st)
+{
+    const int64_t N = p->nx * p->ny * p->nz;
+    const int nc = ncomp_of(p);
+    memset(st, 0, sizeof(double) * (size_t)nc * 2 * (size_t)N);
+    orc_mt19937 g;
+    orc_mt_seed(&g, seed);
+    for (int64_t s = 0; s < N; ++s) {
+        double phase = orc_uniform_0_2pi(&g);
+        double ph2 = phase;
+        if (p->model == LAT_MODEL_MOORE && independent) ph2 = orc_uniform_0_2pi(&g);
+        double v[4];
+        v[0] = p->eta * cos(phase);
+        v[1] = p->eta * sin(phase);
+        int ns = 2;
+        if (p->model == LAT_MODEL_MOORE) {
+            v[2] = p->eta2 * cos(ph2);
+            v[3] = p->eta2 * sin(ph2);
+            ns = 4;
+        }
+        for (int c = 0; c < ns; ++c) {
+            st[((int64_t)c * 2 + 0) * N + s] = v[c];
+            st[((int64_t)c * 2 + 1) * N + s] = v[c];
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* threads                                                                    */
+/* ------------------------------------------------------------------------- */
+static int g_threads = 0;
+void orc_set_threads(int n) { g_threads = n; }
+int orc_get_threads(void)
+{
+#ifdef _OPENMP
+    return g_threads > 0 ? g_threads : omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------------- */
+/* geometry                                                                   */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+    int64_t nx, ny, nz, N, syz;
+    int lo, hix, hiy, hiz;   /* evolved region: [lo, hi) per axis */
+} geo_t;
+
+static geo_t make_geo(const lat_params* p)
+{
+    geo_t g;
+    g.nx = p->nx; g.ny = p->ny; g.nz = p->nz;
+    g.N = g.nx * g.ny * g.nz;
+    g.syz = g.ny * g.nz;
+    if (p->bc == LAT_BC_FIXED) { g.lo = 1; g.hix = (int)g.nx - 1; g.hiy = (int)g.ny - 1; g.hiz = (int)g.nz - 1; }
+    else { g.lo = 0; g.hix = (int)g.nx; g.hiy = (int)g.ny; g.hiz = (int)g.nz; }
+    return g;
+}
+
+static inline int64_t wrapp(int64_t a, int64_t n) { return a + 1 == n ? 0 : a + 1; }
+static inline int64_t wrapm(int64_t a, int64_t n) { return a == 0 ? n - 1 : a - 1; }
+static inline int64_t site(const geo_t* g, int64_t i, int64_t j, int64_t k) { return (i * g->ny + j) * g->nz + k; }
+
+/* friction coefficient and damping of step n (mpi_evolution.cpp:356-368) */
+static void friction_of(const lat_params* p, int64_t n, double* damp, double* fric)
+{
+    double time = p->tau0 + n * p->dt;
+    *damp = (n < p->damped_nt) ? p->dampFac : 0;
+    *fric = *damp + p->alpha * p->scaling / time;
+}
+
+#define ST(c, t, s) st[((int64_t)(c) * 2 + (t)) * N + (s)]
+
+/* ------------------------------------------------------------------------- */
+/* Abelian-Higgs step: mpi_evolution.cpp:381-501 (== evolution.cpp:273-373 + */
+/* 1384-1402 for the fields).  Components: 0,1 = phi; 2,3,4 = theta_x,y,z.     */
+/* ------------------------------------------------------------------------- */
+static void ah_update(const lat_params* p, double* st, int64_t n)
+{
+    const geo_t G = make_geo(p);
+    const int64_t N = G.N;
+    const int tNow = (int)((n + 1) % 2), tPast = (int)(n % 2);
+    double damp, fric;
+    friction_of(p, n, &damp, &fric);
+    const double dx = p->dx, dy = p->dy, dz = p->dz, dt = p->dt;
+    const double lambda = p->lambda, eta = p->eta, g = p->g;
+    const int c[2] = {1, -1};
+
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+    for (int64_t i = G.lo; i < G.hix; ++i) {
+        const int64_t ip = wrapp(i, G.nx), im = wrapm(i, G.nx);
+        for (int64_t j = G.lo; j < G.hiy; ++j) {
+            const int64_t jp = wrapp(j, G.ny), jm = wrapm(j, G.ny);
+            for (int64_t k = G.lo; k < G.hiz; ++k) {
+                const int64_t kp = wrapp(k, G.nz), km = wrapm(k, G.nz);
+                const int64_t s = site(&G, i, j, k);
+                const int64_t ipx = site(&G, ip, j, k), imx = site(&G, im, j, k);
+                const int64_t ipy = site(&G, i, jp, k), imy = site(&G, i, jm, k);
+                const int64_t ipz = site(&G, i, j, kp), imz = site(&G, i, j, km);
+                const int64_t ipxmy = site(&G, ip, jm, k), ipxmz = site(&G, ip, j, km);
+                const int64_t imxpy = site(&G, im, jp, k), ipymz = site(&G, i, jp, km);
+                const int64_t imxpz = site(&G, im, j, kp), imypz = site(&G, i, jm, kp);
+
+                double phiMagSqr = ST(0, tNow, s) * ST(0, tNow, s) + ST(1, tNow, s) * ST(1, tNow, s);
+                for (int comp = 0; comp < 2; ++comp) {
+                    const int oc = comp + c[comp];
+                    const double cc = (double)c[comp];
+                    double phixx = (cos(ST(2, tNow, s)) * ST(comp, tNow, ipx) + cc * sin(ST(2, tNow, s)) * ST(oc, tNow, ipx) - 2 * ST(comp, tNow, s)
+                                    + cos(ST(2, tNow, imx)) * ST(comp, tNow, imx) - cc * sin(ST(2, tNow, imx)) * ST(oc, tNow, imx)) / (dx * dx);
+                    double phiyy = (cos(ST(3, tNow, s)) * ST(comp, tNow, ipy) + cc * sin(ST(3, tNow, s)) * ST(oc, tNow, ipy) - 2 * ST(comp, tNow, s)
+                                    + cos(ST(3, tNow, imy)) * ST(comp, tNow, imy) - cc * sin(ST(3, tNow, imy)) * ST(oc, tNow, imy)) / (dy * dy);
+                    double phizz = (cos(ST(4, tNow, s)) * ST(comp, tNow, ipz) + cc * sin(ST(4, tNow, s)) * ST(oc, tNow, ipz) - 2 * ST(comp, tNow, s)
+                                    + cos(ST(4, tNow, imz)) * ST(comp, tNow, imz) - cc * sin(ST(4, tNow, imz)) * ST(oc, tNow, imz)) / (dz * dz);
+                    double phitt = phixx + phiyy + phizz - 0.5 * lambda * (phiMagSqr - eta * eta) * ST(comp, tNow, s);
+                    if (fric != 0) {
+                        double phit = (ST(comp, tNow, s) - ST(comp, tPast, s)) / dt;
+                        phitt = phitt - fric * phit;
+                    }
+                    ST(comp, tPast, s) = 2 * ST(comp, tNow, s) - ST(comp, tPast, s) + dt * dt * phitt;
+                }
+
+                double curx = cos(ST(2, tNow, s)) * (ST(1, tNow, s) * ST(0, tNow, ipx) - ST(0, tNow, s) * ST(1, tNow, ipx))
+                            + sin(ST(2, tNow, s)) * (ST(0, tNow, s) * ST(0, tNow, ipx) + ST(1, tNow, s) * ST(1, tNow, ipx));
+                double cury = cos(ST(3, tNow, s)) * (ST(1, tNow, s) * ST(0, tNow, ipy) - ST(0, tNow, s) * ST(1, tNow, ipy))
+                            + sin(ST(3, tNow, s)) * (ST(0, tNow, s) * ST(0, tNow, ipy) + ST(1, tNow, s) * ST(1, tNow, ipy));
+                double curz = cos(ST(4, tNow, s)) * (ST(1, tNow, s) * ST(0, tNow, ipz) - ST(0, tNow, s) * ST(1, tNow, ipz))
+                            + sin(ST(4, tNow, s)) * (ST(0, tNow, s) * ST(0, tNow, ipz) + ST(1, tNow, s) * ST(1, tNow, ipz));
+
+                double Fxy_y = (sin(ST(2, tNow, s) + ST(3, tNow, ipx) - ST(2, tNow, ipy) - ST(3, tNow, s))
+                              - sin(ST(2, tNow, imy) + ST(3, tNow, ipxmy) - ST(2, tNow, s) - ST(3, tNow, imy))) / (dy * dy);
+                double Fxz_z = (sin(ST(2, tNow, s) + ST(4, tNow, ipx) - ST(2, tNow, ipz) - ST(4, tNow, s))
+                              - sin(ST(2, tNow, imz) + ST(4, tNow, ipxmz) - ST(2, tNow, s) - ST(4, tNow, imz))) / (dz * dz);
+                double Fyx_x = (sin(ST(3, tNow, s) + ST(2, tNow, ipy) - ST(3, tNow, ipx) - ST(2, tNow, s))
+                              - sin(ST(3, tNow, imx) + ST(2, tNow, imxpy) - ST(3, tNow, s) - ST(2, tNow, imx))) / (dx * dx);
+                double Fyz_z = (sin(ST(3, tNow, s) + ST(4, tNow, ipy) - ST(3, tNow, ipz) - ST(4, tNow, s))
+                              - sin(ST(3, tNow, imz) + ST(4, tNow, ipymz) - ST(3, tNow, s) - ST(4, tNow, imz))) / (dz * dz);
+                double Fzx_x = (sin(ST(4, tNow, s) + ST(2, tNow, ipz) - ST(4, tNow, ipx) - ST(2, tNow, s))
+                              - sin(ST(4, tNow, imx) + ST(2, tNow, imxpz) - ST(4, tNow, s) - ST(2, tNow, imx))) / (dx * dx);
+                double Fzy_y = (sin(ST(4, tNow, s) + ST(3, tNow, ipz) - ST(4, tNow, ipy) - ST(3, tNow, s))
+                              - sin(ST(4, tNow, imy) + ST(3, tNow, imypz) - ST(4, tNow, s) - ST(3, tNow, imy))) / (dy * dy);
+
+                double tt[3];
+                tt[0] = -2 * g * g * curx - Fxy_y - Fxz_z;
+                tt[1] = -2 * g * g * cury - Fyx_x - Fyz_z;
+                tt[2] = -2 * g * g * curz - Fzx_x - Fzy_y;
+                if (damp != 0) {
+                    for (int m = 0; m < 3; ++m) {
+                        double thetat = (ST(2 + m, tNow, s) - ST(2 + m, tPast, s)) / dt;
+                        tt[m] = tt[m] - damp * thetat;
+                    }
+                }
+                for (int m = 0; m < 3; ++m)
+                    ST(2 + m, tPast, s) = 2 * ST(2 + m, tNow, s) - ST(2 + m, tPast, s) + dt * dt * tt[m];
+            }
+        }
+    }
+}
+
+/* Abelian-Higgs diagnostics of level n: evolution.cpp:294-427 (energy, Gauss)
+ * or, for LAT_ENERGY_MPI, mpi_evolution.cpp:509-532 (energy). */
+static void ah_diag(const lat_params* p, const double* st, int64_t n, lat_diag* out)
+{
+    const geo_t G = make_geo(p);
+    const int64_t N = G.N;
+    const int tNow = (int)((n + 1) % 2), tPast = (int)(n % 2);
+    const double dx = p->dx, dy = p->dy, dz = p->dz, dt = p->dt;
+    const double lambda = p->lambda, eta = p->eta, g = p->g;
+    const int c[2] = {1, -1};
+    const int mpi_form = p->energy_form == LAT_ENERGY_MPI;
+    double energy = 0, dev = 0;
+
+#pragma omp parallel for schedule(static) reduction(+:energy,dev) num_threads(orc_get_threads())
+    for (int64_t i = G.lo; i < G.hix; ++i) {
+        const int64_t ip = wrapp(i, G.nx), im = wrapm(i, G.nx);
+        for (int64_t j = G.lo; j < G.hiy; ++j) {
+            const int64_t jp = wrapp(j, G.ny), jm = wrapm(j, G.ny);
+            for (int64_t k = G.lo; k < G.hiz; ++k) {
+                const int64_t kp = wrapp(k, G.nz), km = wrapm(k, G.nz);
+                const int64_t s = site(&G, i, j, k);
+                const int64_t ipx = site(&G, ip, j, k), imx = site(&G, im, j, k);
+                const int64_t ipy = site(&G, i, jp, k), imy = site(&G, i, jm, k);
+                const int64_t ipz = site(&G, i, j, kp), imz = site(&G, i, j, km);
+                double phiMagSqr = ST(0, tNow, s) * ST(0, tNow, s) + ST(1, tNow, s) * ST(1, tNow, s);
+                double phit[2], phix[2], phiy[2], phiz[2];
+                for (int comp = 0; comp < 2; ++comp) {
+                    const int oc = comp + c[comp];
+                    const double cc = (double)c[comp];
+                    phit[comp] = (ST(comp, tNow, s) - ST(comp, tPast, s)) / dt;
+                    phix[comp] = (ST(comp, tNow, s) - cos(ST(2, tNow, imx)) * ST(comp, tNow, imx) + cc * sin(ST(2, tNow, imx)) * ST(oc, tNow, imx)) / dx;
+                    phiy[comp] = (ST(comp, tNow, s) - cos(ST(3, tNow, imy)) * ST(comp, tNow, imy) + cc * sin(ST(3, tNow, imy)) * ST(oc, tNow, imy)) / dy;
+                    phiz[comp] = (ST(comp, tNow, s) - cos(ST(4, tNow, imz)) * ST(comp, tNow, imz) + cc * sin(ST(4, tNow, imz)) * ST(oc, tNow, imz)) / dz;
+                }
+                double Pxy = ST(2, tNow, s) + ST(3, tNow, ipx) - ST(2, tNow, ipy) - ST(3, tNow, s);
+                double Pxz = ST(2, tNow, s) + ST(4, tNow, ipx) - ST(2, tNow, ipz) - ST(4, tNow, s);
+                double Pyz = ST(3, tNow, s) + ST(4, tNow, ipy) - ST(3, tNow, ipz) - ST(4, tNow, s);
+                double gauss = 0, thetaDotCont, FCont;
+                if (mpi_form) {
+                    double t0 = (ST(2, tNow, s) - ST(2, tPast, s)) / dt;
+                    double t1 = (ST(3, tNow, s) - ST(3, tPast, s)) / dt;
+                    double t2 = (ST(4, tNow, s) - ST(4, tPast, s)) / dt;
+                    thetaDotCont = 0.5 * (t0 * t0 + t1 * t1 + t2 * t2);
+                    double gxy = g * dx * dy, gxz = g * dx * dz, gyz = g * dy * dz;
+                    FCont = (1 - cos(Pxy)) / (gxy * gxy) + (1 - cos(Pxz)) / (gxz * gxz) + (1 - cos(Pyz)) / (gyz * gyz);
+                }
+                if (g != 0) {
+                    double divNow = (ST(2, tNow, s) - ST(2, tNow, imx)) / (dx * dx) + (ST(3, tNow, s) - ST(3, tNow, imy)) / (dy * dy)
+                                  + (ST(4, tNow, s) - ST(4, tNow, imz)) / (dz * dz);
+                    double divPast = (ST(2, tPast, s) - ST(2, tPast, imx)) / (dx * dx) + (ST(3, tPast, s) - ST(3, tPast, imy)) / (dy * dy)
+                                   + (ST(4, tPast, s) - ST(4, tPast, imz)) / (dz * dz);
+                    double divThetat = (divNow - divPast) / dt;
+                    gauss = divThetat / g - 2 * g * (ST(1, tNow, s) * phit[0] - ST(0, tNow, s) * phit[1]);
+                    if (!mpi_form) {
+                        double t0 = (ST(2, tNow, s) - ST(2, tPast, s)) / (g * dt * dx);
+                        double t1 = (ST(3, tNow, s) - ST(3, tPast, s)) / (g * dt * dy);
+                        double t2 = (ST(4, tNow, s) - ST(4, tPast, s)) / (g * dt * dz);
+                        thetaDotCont = 0.5 * (t0 * t0 + t1 * t1 + t2 * t2);
+                        double gxy = g * dx * dy, gxz = g * dx * dz, gyz = g * dy * dz;
+                        double Fxy = (1 - cos(Pxy)) / (gxy * gxy);
+                        double Fxz = (1 - cos(Pxz)) / (gxz * gxz);
+                        double Fyz = (1 - cos(Pyz)) / (gyz * gyz);
+                        FCont = Fxy + Fxz + Fyz;
+                    }
+                } else if (!mpi_form) {
+                    thetaDotCont = 0;
+                    FCont = 0;
+                }
+                double pm = phiMagSqr - eta * eta;
+                double ed = phit[0] * phit[0] + phit[1] * phit[1] + phix[0] * phix[0] + phix[1] * phix[1] + phiy[0] * phiy[0]
+                          + phiy[1] * phiy[1] + phiz[0] * phiz[0] + phiz[1] * phiz[1] + thetaDotCont + FCont + 0.25 * lambda * (pm * pm);
+                if (mpi_form) energy += ed * dx * dy * dz;
+                else energy += dx * dy * dz * ed;
+                dev += fabs(gauss);
+            }
+        }
+    }
+    out->energy = energy;
+    out->gauss_abs_sum = dev;
+    out->sites = (int64_t)(G.hix - G.lo) * (G.hiy - G.lo) * (G.hiz - G.lo);
+    out->time_step = n;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Moore model: moore_mpi_evolution.cpp:405-550 (periodic, friction, current  */
+/* without q) and mooreEvol.cpp:187-337 + 672-692 (fixed, q-weighted current). */
+/* Components: 0,1 = phi1; 2,3 = phi2; 4,5,6 = theta_x,y,z.                    */
+/* ------------------------------------------------------------------------- */
+#define PH(f, comp) ((f) * 2 + (comp))   /* f = 0 (phi1) / 1 (phi2) */
+#define TH(m) (4 + (m))
+
+static void moore_update(const lat_params* p, double* st, int64_t n)
+{
+    const geo_t G = make_geo(p);
+    const int64_t N = G.N;
+    const int tNow = (int)((n + 1) % 2), tPast = (int)(n % 2);
+    double damp, fric;
+    friction_of(p, n, &damp, &fric);
+    const double dx = p->dx, dy = p->dy, dz = p->dz, dt = p->dt;
+    const double l1 = p->lambda, l2 = p->lambda2, l12 = p->lambda12, e1 = p->eta, e2 = p->eta2, g = p->g;
+    const double q[2] = {p->q1, p->q2};
+    const int charge = p->moore_current == LAT_MOORE_CURRENT_CHARGE;
+    const int c[2] = {1, -1};
+
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+    for (int64_t i = G.lo; i < G.hix; ++i) {
+        const int64_t ip = wrapp(i, G.nx), im = wrapm(i, G.nx);
+        for (int64_t j = G.lo; j < G.hiy; ++j) {
+            const int64_t jp = wrapp(j, G.ny), jm = wrapm(j, G.ny);
+            for (int64_t k = G.lo; k < G.hiz; ++k) {
+                const int64_t kp = wrapp(k, G.nz), km = wrapm(k, G.nz);
+                const int64_t s = site(&G, i, j, k);
+                const int64_t ipx = site(&G, ip, j, k), imx = site(&G, im, j, k);
+                const int64_t ipy = site(&G, i, jp, k), imy = site(&G, i, jm, k);
+                const int64_t ipz = site(&G, i, j, kp), imz = site(&G, i, j, km);
+                const int64_t ipxmy = site(&G, ip, jm, k), ipxmz = site(&G, ip, j, km);
+                const int64_t imxpy = site(&G, im, jp, k), ipymz = site(&G, i, jp, km);
+                const int64_t imxpz = site(&G, im, j, kp), imypz = site(&G, i, jm, kp);
+                const int64_t nb[3][2] = {{ipx, imx}, {ipy, imy}, {ipz, imz}};
+                const double d2[3] = {dx * dx, dy * dy, dz * dz};
+
+                double mag[2];
+                for (int f = 0; f < 2; ++f)
+                    mag[f] = ST(PH(f, 0), tNow, s) * ST(PH(f, 0), tNow, s) + ST(PH(f, 1), tNow, s) * ST(PH(f, 1), tNow, s);
+                for (int comp = 0; comp < 2; ++comp) {
+                    const int oc = comp + c[comp];
+                    const double cc = (double)c[comp];
+                    for (int f = 0; f < 2; ++f) {
+                        const double qf = q[f];
+                        double lap[3];
+                        for (int m = 0; m < 3; ++m) {
+                            const int64_t pp = nb[m][0], mm = nb[m][1];
+                            lap[m] = (cos(qf * ST(TH(m), tNow, s)) * ST(PH(f, comp), tNow, pp) + cc * sin(qf * ST(TH(m), tNow, s)) * ST(PH(f, oc), tNow, pp)
+                                      - 2 * ST(PH(f, comp), tNow, s)
+                                      + cos(qf * ST(TH(m), tNow, mm)) * ST(PH(f, comp), tNow, mm) - cc * sin(qf * ST(TH(m), tNow, mm)) * ST(PH(f, oc), tNow, mm)) / d2[m];
+                        }
+                        double pot = (f == 0) ? (0.5 * l1 * (mag[0] - e1 * e1) + 0.5 * l12 * (mag[1] - e2 * e2))
+                                              : (0.5 * l2 * (mag[1] - e2 * e2) + 0.5 * l12 * (mag[0] - e1 * e1));
+                        double phitt = lap[0] + lap[1] + lap[2] - pot * ST(PH(f, comp), tNow, s);
+                        if (fric != 0) {
+                            double phit = (ST(PH(f, comp), tNow, s) - ST(PH(f, comp), tPast, s)) / dt;
+                            phitt = phitt - fric * phit;
+                        }
+                        ST(PH(f, comp), tPast, s) = 2 * ST(PH(f, comp), tNow, s) - ST(PH(f, comp), tPast, s) + dt * dt * phitt;
+                    }
+                }
+
+                double cur[3];
+                for (int m = 0; m < 3; ++m) {
+                    const int64_t pp = nb[m][0];
+                    double cf[2];
+                    for (int f = 0; f < 2; ++f) {
+                        const double qf = q[f];
+                        double v = cos(qf * ST(TH(m), tNow, s)) * (ST(PH(f, 1), tNow, s) * ST(PH(f, 0), tNow, pp) - ST(PH(f, 0), tNow, s) * ST(PH(f, 1), tNow, pp))
+                                 + sin(qf * ST(TH(m), tNow, s)) * (ST(PH(f, 0), tNow, s) * ST(PH(f, 0), tNow, pp) + ST(PH(f, 1), tNow, s) * ST(PH(f, 1), tNow, pp));
+                        cf[f] = charge ? qf * v : v;
+                    }
+                    cur[m] = cf[0] + cf[1];
+                }
+
+                double Fxy_y = (sin(ST(TH(0), tNow, s) + ST(TH(1), tNow, ipx) - ST(TH(0), tNow, ipy) - ST(TH(1), tNow, s))
+                              - sin(ST(TH(0), tNow, imy) + ST(TH(1), tNow, ipxmy) - ST(TH(0), tNow, s) - ST(TH(1), tNow, imy))) / (dy * dy);
+                double Fxz_z = (sin(ST(TH(0), tNow, s) + ST(TH(2), tNow, ipx) - ST(TH(0), tNow, ipz) - ST(TH(2), tNow, s))
+                              - sin(ST(TH(0), tNow, imz) + ST(TH(2), tNow, ipxmz) - ST(TH(0), tNow, s) - ST(TH(2), tNow, imz))) / (dz * dz);
+                double Fyx_x = (sin(ST(TH(1), tNow, s) + ST(TH(0), tNow, ipy) - ST(TH(1), tNow, ipx) - ST(TH(0), tNow, s))
+                              - sin(ST(TH(1), tNow, imx) + ST(TH(0), tNow, imxpy) - ST(TH(1), tNow, s) - ST(TH(0), tNow, imx))) / (dx * dx);
+                double Fyz_z = (sin(ST(TH(1), tNow, s) + ST(TH(2), tNow, ipy) - ST(TH(1), tNow, ipz) - ST(TH(2), tNow, s))
+                              - sin(ST(TH(1), tNow, imz) + ST(TH(2), tNow, ipymz) - ST(TH(1), tNow, s) - ST(TH(2), tNow, imz))) / (dz * dz);
+                double Fzx_x = (sin(ST(TH(2), tNow, s) + ST(TH(0), tNow, ipz) - ST(TH(2), tNow, ipx) - ST(TH(0), tNow, s))
+                              - sin(ST(TH(2), tNow, imx) + ST(TH(0), tNow, imxpz) - ST(TH(2), tNow, s) - ST(TH(0), tNow, imx))) / (dx * dx);
+                double Fzy_y = (sin(ST(TH(2), tNow, s) + ST(TH(1), tNow, ipz) - ST(TH(2), tNow, ipy) - ST(TH(1), tNow, s))
+                              - sin(ST(TH(2), tNow, imy) + ST(TH(1), tNow, imypz) - ST(TH(2), tNow, s) - ST(TH(1), tNow, imy))) / (dy * dy);
+
+                double tt[3];
+                tt[0] = -2 * g * g * cur[0] - Fxy_y - Fxz_z;
+                tt[1] = -2 * g * g * cur[1] - Fyx_x - Fyz_z;
+                tt[2] = -2 * g * g * cur[2] - Fzx_x - Fzy_y;
+                if (damp != 0) {
+                    for (int m = 0; m < 3; ++m) {
+                        double thetat = (ST(TH(m), tNow, s) - ST(TH(m), tPast, s)) / dt;
+                        tt[m] = tt[m] - damp * thetat;
+                    }
+                }
+                for (int m = 0; m < 3; ++m)
+                    ST(TH(m), tPast, s) = 2 * ST(TH(m), tNow, s) - ST(TH(m), tPast, s) + dt * dt * tt[m];
+            }
+        }
+    }
+}
+
+/* Moore diagnostics: mooreEvol.cpp:339-391 (energy + Gauss with charges) or
+ * moore_mpi_evolution.cpp:558-588 (LAT_ENERGY_MPI energy). */
+static void moore_diag(const lat_params* p, const double* st, int64_t n, lat_diag* out)
+{
+    const geo_t G = make_geo(p);
+    const int64_t N = G.N;
+    const int tNow = (int)((n + 1) % 2), tPast = (int)(n % 2);
+    const double dx = p->dx, dy = p->dy, dz = p->dz, dt = p->dt;
+    const double l1 = p->lambda, l2 = p->lambda2, l12 = p->lambda12, e1 = p->eta, e2 = p->eta2, g = p->g;
+    const double q[2] = {p->q1, p->q2};
+    const int c[2] = {1, -1};
+    const int mpi_form = p->energy_form == LAT_ENERGY_MPI;
+    double energy = 0, dev = 0;
+
+#pragma omp parallel for schedule(static) reduction(+:energy,dev) num_threads(orc_get_threads())
+    for (int64_t i = G.lo; i < G.hix; ++i) {
+        const int64_t ip = wrapp(i, G.nx), im = wrapm(i, G.nx);
+        for (int64_t j = G.lo; j < G.hiy; ++j) {
+            const int64_t jp = wrapp(j, G.ny), jm = wrapm(j, G.ny);
+            for (int64_t k = G.lo; k < G.hiz; ++k) {
+                const int64_t kp = wrapp(k, G.nz), km = wrapm(k, G.nz);
+                const int64_t s = site(&G, i, j, k);
+                const int64_t ipx = site(&G, ip, j, k), imx = site(&G, im, j, k);
+                const int64_t ipy = site(&G, i, jp, k), imy = site(&G, i, jm, k);
+                const int64_t ipz = site(&G, i, j, kp), imz = site(&G, i, j, km);
+                const int64_t mmv[3] = {imx, imy, imz};
+                const double dd[3] = {dx, dy, dz};
+                double mag[2];
+                for (int f = 0; f < 2; ++f)
+                    mag[f] = ST(PH(f, 0), tNow, s) * ST(PH(f, 0), tNow, s) + ST(PH(f, 1), tNow, s) * ST(PH(f, 1), tNow, s);
+                double pt[2][2], pd[2][3][2];
+                for (int comp = 0; comp < 2; ++comp) {
+                    const int oc = comp + c[comp];
+                    const double cc = (double)c[comp];
+                    for (int f = 0; f < 2; ++f) {
+                        const double qf = q[f];
+                        pt[f][comp] = (ST(PH(f, comp), tNow, s) - ST(PH(f, comp), tPast, s)) / dt;
+                        for (int m = 0; m < 3; ++m) {
+                            const int64_t mm = mmv[m];
+                            pd[f][m][comp] = (ST(PH(f, comp), tNow, s) - cos(qf * ST(TH(m), tNow, mm)) * ST(PH(f, comp), tNow, mm)
+                                              + cc * sin(qf * ST(TH(m), tNow, mm)) * ST(PH(f, oc), tNow, mm)) / dd[m];
+                        }
+                    }
+                }
+                double Pxy = ST(TH(0), tNow, s) + ST(TH(1), tNow, ipx) - ST(TH(0), tNow, ipy) - ST(TH(1), tNow, s);
+                double Pxz = ST(TH(0), tNow, s) + ST(TH(2), tNow, ipx) - ST(TH(0), tNow, ipz) - ST(TH(2), tNow, s);
+                double Pyz = ST(TH(1), tNow, s) + ST(TH(2), tNow, ipy) - ST(TH(1), tNow, ipz) - ST(TH(2), tNow, s);
+                double gauss = 0, thetaDotCont = 0, FCont = 0;
+                if (mpi_form) {
+                    double t0 = (ST(TH(0), tNow, s) - ST(TH(0), tPast, s)) / dt;
+                    double t1 = (ST(TH(1), tNow, s) - ST(TH(1), tPast, s)) / dt;
+                    double t2 = (ST(TH(2), tNow, s) - ST(TH(2), tPast, s)) / dt;
+                    thetaDotCont = 0.5 * (t0 * t0 + t1 * t1 + t2 * t2);
+                    double gxy = g * dx * dy, gxz = g * dx * dz, gyz = g * dy * dz;
+                    FCont = (1 - cos(Pxy)) / (gxy * gxy) + (1 - cos(Pxz)) / (gxz * gxz) + (1 - cos(Pyz)) / (gyz * gyz);
+                }
+                if (g != 0) {
+                    double divNow = (ST(TH(0), tNow, s) - ST(TH(0), tNow, imx)) / (dx * dx) + (ST(TH(1), tNow, s) - ST(TH(1), tNow, imy)) / (dy * dy)
+                                  + (ST(TH(2), tNow, s) - ST(TH(2), tNow, imz)) / (dz * dz);
+                    double divPast = (ST(TH(0), tPast, s) - ST(TH(0), tPast, imx)) / (dx * dx) + (ST(TH(1), tPast, s) - ST(TH(1), tPast, imy)) / (dy * dy)
+                                   + (ST(TH(2), tPast, s) - ST(TH(2), tPast, imz)) / (dz * dz);
+                    double divThetat = (divNow - divPast) / dt;
+                    gauss = divThetat / g - 2 * g * (q[0] * (ST(PH(0, 1), tNow, s) * pt[0][0] - ST(PH(0, 0), tNow, s) * pt[0][1])
+                                                   + q[1] * (ST(PH(1, 1), tNow, s) * pt[1][0] - ST(PH(1, 0), tNow, s) * pt[1][1]));
+                    if (!mpi_form) {
+                        double t0 = (ST(TH(0), tNow, s) - ST(TH(0), tPast, s)) / (g * dt * dx);
+                        double t1 = (ST(TH(1), tNow, s) - ST(TH(1), tPast, s)) / (g * dt * dy);
+                        double t2 = (ST(TH(2), tNow, s) - ST(TH(2), tPast, s)) / (g * dt * dz);
+                        thetaDotCont = 0.5 * (t0 * t0 + t1 * t1 + t2 * t2);
+                        double gxy = g * dx * dy, gxz = g * dx * dz, gyz = g * dy * dz;
+                        double Fxy = (1 - cos(Pxy)) / (gxy * gxy);
+                        double Fxz = (1 - cos(Pxz)) / (gxz * gxz);
+                        double Fyz = (1 - cos(Pyz)) / (gyz * gyz);
+                        FCont = Fxy + Fxz + Fyz;
+                    }
+                }
+                double m1 = mag[0] - e1 * e1, m2 = mag[1] - e2 * e2;
+                double ed = pt[0][0] * pt[0][0] + pt[0][1] * pt[0][1] + pd[0][0][0] * pd[0][0][0] + pd[0][0][1] * pd[0][0][1]
+                          + pd[0][1][0] * pd[0][1][0] + pd[0][1][1] * pd[0][1][1] + pd[0][2][0] * pd[0][2][0] + pd[0][2][1] * pd[0][2][1]
+                          + pt[1][0] * pt[1][0] + pt[1][1] * pt[1][1] + pd[1][0][0] * pd[1][0][0] + pd[1][0][1] * pd[1][0][1]
+                          + pd[1][1][0] * pd[1][1][0] + pd[1][1][1] * pd[1][1][1] + pd[1][2][0] * pd[1][2][0] + pd[1][2][1] * pd[1][2][1]
+                          + thetaDotCont + FCont + 0.25 * l1 * (m1 * m1) + 0.25 * l2 * (m2 * m2) + 0.5 * l12 * m1 * m2;
+                if (mpi_form) energy += ed * dx * dy * dz;
+                else energy += dx * dy * dz * ed;
+                dev += fabs(gauss);
+            }
+        }
+    }
+    out->energy = energy;
+    out->gauss_abs_sum = dev;
+    out->sites = (int64_t)(G.hix - G.lo) * (G.hiy - G.lo) * (G.hiz - G.lo);
+    out->time_step = n;
+}
+
+int orc_diagnostics(const lat_params* p, const double* st, int64_t n, lat_diag* diag)
+{
+    if (!p || !st || !diag) return LAT_ERR_INVALID;
+    if (p->model == LAT_MODEL_MOORE) moore_diag(p, st, n, diag);
+    else ah_diag(p, st, n, diag);
+    return 0;
+}
+
+int orc_step(const lat_params* p, double* st, int64_t n, lat_diag* diag)
+{
+    if (!p || !st) return LAT_ERR_INVALID;
+    if (diag) orc_diagnostics(p, st, n, diag);
+    if (p->model == LAT_MODEL_MOORE) moore_update(p, st, n);
+    else ah_update(p, st, n);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* bilinear crossing detection: mpi_evolution.cpp:536-789                     */
+/* ------------------------------------------------------------------------- */
+typedef struct { double* xyz; int64_t cap, count; } sink_t;
+
+static void push(sink_t* o, double x, double y, double z)
+{
+    if (o->count < o->cap) {
+        o->xyz[3 * o->count + 0] = x;
+        o->xyz[3 * o->count + 1] = y;
+        o->xyz[3 * o->count + 2] = z;
+    }
+    o->count++;
+}
+
+/* One face.  v00 = phi at the corner (u, w), v10 at (u+du, w), v01 at (u, w+dw),
+ * v11 at (u+du, w+dw), per component.  Solutions: sol1 along u, sol2 along w.
+ * emit(sol1, sol2) maps back to (x,y,z). */
+static int face_roots(const double v00[2], const double v10[2], const double v01[2], const double v11[2],
+                      double u, double w, double du, double dw, double s1[2], double s2[2])
+{
+    double coeff1[2], coeff2[2], coeff3[2], coeff4[2];
+    for (int comp = 0; comp < 2; ++comp) {
+        coeff1[comp] = v11[comp] - v10[comp] - v01[comp] + v00[comp];
+        coeff2[comp] = (w + dw) * (v10[comp] - v00[comp]) + w * (v01[comp] - v11[comp]);
+        coeff3[comp] = (u + du) * (v01[comp] - v00[comp]) + u * (v10[comp] - v11[comp]);
+        coeff4[comp] = (u + du) * ((w + dw) * v00[comp] - w * v01[comp]) - u * ((w + dw) * v10[comp] - w * v11[comp]);
+    }
+    double a = coeff1[1] * coeff3[0] - coeff1[0] * coeff3[1];
+    double b = coeff1[1] * coeff4[0] + coeff2[1] * coeff3[0] - coeff1[0] * coeff4[1] - coeff2[0] * coeff3[1];
+    double c = coeff2[1] * coeff4[0] - coeff2[0] * coeff4[1];
+    double discrim = b * b - 4 * a * c;
+    int nroot = 0;
+    if (a == 0) {
+        if (b != 0) {
+            double sol2 = -c / b;
+            if (sol2 >= w && sol2 <= w + dw) {
+                double sol1 = -(coeff3[0] * sol2 + coeff4[0]) / (coeff1[0] * sol2 + coeff2[0]);
+                if (sol1 >= u && sol1 <= u + du) { s1[nroot] = sol1; s2[nroot] = sol2; nroot++; }
+            }
+        }
+    } else if (discrim >= 0) {
+        double sol2 = (-b + sqrt(discrim)) / (2 * a);
+        if (sol2 >= w && sol2 <= w + dw) {
+            double sol1 = -(coeff3[0] * sol2 + coeff4[0]) / (coeff1[0] * sol2 + coeff2[0]);
+            if (sol1 >= u && sol1 <= u + du) { s1[nroot] = sol1; s2[nroot] = sol2; nroot++; }
+        }
+        sol2 = (-b - sqrt(discrim)) / (2 * a);
+        if (sol2 >= w && sol2 <= w + dw) {
+            double sol1 = -(coeff3[0] * sol2 + coeff4[0]) / (coeff1[0] * sol2 + coeff2[0]);
+            if (sol1 >= u && sol1 <= u + du) { s1[nroot] = sol1; s2[nroot] = sol2; nroot++; }
+        }
+    }
+    return nroot;
+}
+
+int orc_detect(const lat_params* p, const double* st, int64_t n, int field,
+               double* xyz, int64_t cap, int64_t* count)
+{
+    if (!p || !st || !count) return LAT_ERR_INVALID;
+    if (field != 0 && !(field == 1 && p->model == LAT_MODEL_MOORE)) return LAT_ERR_INVALID;
+    const geo_t G = make_geo(p);
+    const int64_t N = G.N;
+    const int tNow = (int)((n + 1) % 2);
+    const int c0 = 2 * field;
+    const double dx = p->dx, dy = p->dy, dz = p->dz;
+    const int64_t x0 = (int64_t)(0.5 * (G.nx - 1)), y0 = (int64_t)(0.5 * (G.ny - 1)), z0 = (int64_t)(0.5 * (G.nz - 1));
+    sink_t o = {xyz, xyz ? cap : 0, 0};
+    for (int64_t i = G.lo; i < G.hix; ++i) {
+        const int64_t ip = wrapp(i, G.nx);
+        const double x = (double)(i - x0) * dx;
+        for (int64_t j = G.lo; j < G.hiy; ++j) {
+            const int64_t jp = wrapp(j, G.ny);
+            const double y = (double)(j - y0) * dy;
+            for (int64_t k = G.lo; k < G.hiz; ++k) {
+                const int64_t kp = wrapp(k, G.nz);
+                const double z = (double)(k - z0) * dz;
+                const int64_t s = site(&G, i, j, k);
+                const int64_t ipx = site(&G, ip, j, k), ipy = site(&G, i, jp, k), ipz = site(&G, i, j, kp);
+                const int64_t ipxpy = site(&G, ip, jp, k), ipxpz = site(&G, ip, j, kp), ipypz = site(&G, i, jp, kp);
+                double v0[2], vx[2], vy[2], vz[2], vxy[2], vxz[2], vyz[2];
+                for (int comp = 0; comp < 2; ++comp) {
+                    v0[comp] = ST(c0 + comp, tNow, s);
+                    vx[comp] = ST(c0 + comp, tNow, ipx);
+                    vy[comp] = ST(c0 + comp, tNow, ipy);
+                    vz[comp] = ST(c0 + comp, tNow, ipz);
+                    vxy[comp] = ST(c0 + comp, tNow, ipxpy);
+                    vxz[comp] = ST(c0 + comp, tNow, ipxpz);
+                    vyz[comp] = ST(c0 + comp, tNow, ipypz);
+                }
+                double s1[2], s2[2];
+                int nr;
+                /* z-directed face: u = x, w = y */
+                nr = face_roots(v0, vx, vy, vxy, x, y, dx, dy, s1, s2);
+                for (int r = 0; r < nr; ++r) push(&o, s1[r], s2[r], z);
+                /* y-directed face: u = x, w = z */
+                nr = face_roots(v0, vx, vz, vxz, x, z, dx, dz, s1, s2);
+                for (int r = 0; r < nr; ++r) push(&o, s1[r], y, s2[r]);
+                /* x-directed face: u = y, w = z */
+                nr = face_roots(v0, vy, vz, vyz, y, z, dy, dz, s1, s2);
+                for (int r = 0; r < nr; ++r) push(&o, x, s1[r], s2[r]);
+            }
+        }
+    }
+    *count = o.count;
+    return (xyz && o.count > cap) ? LAT_ERR_CAPACITY : 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* plaquette winding (new; definition in include/lattice_gpu.h)              */
+/* ------------------------------------------------------------------------- */
+static int edge_cross(double ax, double ay, double bx, double by)
+{
+    /* volatile keeps the two products separately rounded */
+    volatile double p1 = ax * by;
+    volatile double p2 = ay * bx;
+    double cr = p1 - p2;
+    if (ay <= 0) { if (by > 0 && cr > 0) return 1; }
+    else { if (by <= 0 && cr < 0) return -1; }
+    return 0;
+}
+
+int orc_winding(const lat_params* p, const double* st, int64_t n, int field,
+                int8_t* out, int64_t* abs_sum)
+{
+    if (!p || !st) return LAT_ERR_INVALID;
+    if (field != 0 && !(field == 1 && p->model == LAT_MODEL_MOORE)) return LAT_ERR_INVALID;
+    const geo_t G = make_geo(p);
+    const int64_t N = G.N;
+    const int tNow = (int)((n + 1) % 2);
+    const int c0 = 2 * field;
+    const int fixed = p->bc == LAT_BC_FIXED;
+    int64_t tot = 0;
+    if (out) memset(out, 0, (size_t)(3 * N));
+    for (int64_t i = 0; i < G.nx; ++i) {
+        const int64_t ip = wrapp(i, G.nx);
+        for (int64_t j = 0; j < G.ny; ++j) {
+            const int64_t jp = wrapp(j, G.ny);
+            for (int64_t k = 0; k < G.nz; ++k) {
+                const int64_t kp = wrapp(k, G.nz);
+                const int64_t s = site(&G, i, j, k);
+                /* corner lists per normal d */
+                int64_t cs[3][4] = {
+                    {s, site(&G, i, jp, k), site(&G, i, jp, kp), site(&G, i, j, kp)},
+                    {s, site(&G, i, j, kp), site(&G, ip, j, kp), site(&G, ip, j, k)},
+                    {s, site(&G, ip, j, k), site(&G, ip, jp, k), site(&G, i, jp, k)}};
+                int valid[3] = {1, 1, 1};
+                if (fixed) {
+                    valid[0] = (j + 1 < G.ny) && (k + 1 < G.nz);
+                    valid[1] = (k + 1 < G.nz) && (i + 1 < G.nx);
+                    valid[2] = (i + 1 < G.nx) && (j + 1 < G.ny);
+                }
+                for (int d = 0; d < 3; ++d) {
+                    if (!valid[d]) continue;
+                    int w = 0;
+                    for (int e = 0; e < 4; ++e) {
+                        const int64_t a = cs[d][e], b = cs[d][(e + 1) & 3];
+                        w += edge_cross(ST(c0, tNow, a), ST(c0 + 1, tNow, a), ST(c0, tNow, b), ST(c0 + 1, tNow, b));
+                    }
+                    if (out) out[d * N + s] = (int8_t)w;
+                    tot += w < 0 ? -w : w;
+                }
+            }
+        }
+    }
+    if (abs_sum) *abs_sum = tot;
+    return 0;
+}

@@ -1,0 +1,62 @@
+/*
+ * lattice_oracle.h — CPU restatement of the reference's lattice hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This code is the checker for the CUDA library:
+ * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it.
+ * The product (liblattice_gpu.so and the drop-in programs) never links it.
+ *
+ * Parity: pinned against the reference itself.  oracle/ref/build_ref.py
+ * compiles the reference programs from their own sources (single-rank MPI
+ * stub, 17-digit output); tests/golden/make_golden.py runs them and stores
+ * their outputs as fixtures; tests/test_oracle_golden.py checks this
+ * restatement against those fixtures.
+ *
+ * State layout (same as the reference's calcInd, mpi_evolution.cpp:62):
+ *   st[(comp*2 + slot)*N + pos], pos = (i*ny + j)*nz + k, slot = time-level
+ *   parity; at TimeStep n, tNow = (n+1)%2 and tPast = n%2.
+ *   Components as in include/lattice_gpu.h (AH: 5, Moore: 7).
+ */
+#ifndef AXIONS_LATTICE_ORACLE_H
+#define AXIONS_LATTICE_ORACLE_H
+
+#include <stdint.h>
+#include "../include/lattice_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* mt19937 + uniform_real_distribution<double>(0, 2*pi) as libstdc++ computes
+ * them (generate_canonical with two 32-bit draws).  Used by
+ * mpi_evolution.cpp:290-312. */
+typedef struct orc_mt19937 { uint32_t mt[624]; int idx; } orc_mt19937;
+void orc_mt_seed(orc_mt19937* g, uint32_t seed);
+uint32_t orc_mt_next(orc_mt19937* g);
+double orc_uniform_0_2pi(orc_mt19937* g);
+
+/* random-phase IC into a full state (both slots equal, theta = 0) */
+int orc_random_phase_ic(const lat_params* p, uint32_t seed, int independent, double* st);
+
+/* set the number of OpenMP threads used by step/diagnostics (<=0: default) */
+void orc_set_threads(int n);
+int orc_get_threads(void);
+
+/* One leapfrog step at TimeStep n, in place.  If diag != NULL the
+ * diagnostics of the level n (before the update) are computed first. */
+int orc_step(const lat_params* p, double* st, int64_t n, lat_diag* diag);
+
+/* diagnostics of level n without stepping */
+int orc_diagnostics(const lat_params* p, const double* st, int64_t n, lat_diag* diag);
+
+/* bilinear crossings of scalar `field` on level n (tNow slot) */
+int orc_detect(const lat_params* p, const double* st, int64_t n, int field,
+               double* xyz, int64_t cap, int64_t* count);
+
+/* plaquette winding of scalar `field` on level n, out = int8[3][N] (may be NULL) */
+int orc_winding(const lat_params* p, const double* st, int64_t n, int field,
+                int8_t* out, int64_t* abs_sum);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,146 @@
+"""Python access to the oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module; it is the checker, never the thing measured or shipped.
+
+State arrays use the reference layout (see oracle/lattice_oracle.h):
+shape (ncomp, 2, N) float64, slot = time-level parity.
+"""
+from __future__ import annotations
+
+import ctypes
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+from axions_gb300.params import LatParams
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "liblattice_oracle.so"
+
+
+class LatDiag(ctypes.Structure):
+    _fields_ = [("energy", ctypes.c_double), ("gauss_abs_sum", ctypes.c_double),
+                ("sites", ctypes.c_int64), ("time_step", ctypes.c_int64)]
+
+
+_lib = None
+
+
+def build() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            build()
+        L = ctypes.CDLL(str(LIB_PATH))
+        P = ctypes.POINTER
+        dp = P(ctypes.c_double)
+        L.orc_step.argtypes = [P(LatParams), dp, ctypes.c_int64, P(LatDiag)]
+        L.orc_diagnostics.argtypes = [P(LatParams), dp, ctypes.c_int64, P(LatDiag)]
+        L.orc_detect.argtypes = [P(LatParams), dp, ctypes.c_int64, ctypes.c_int, dp, ctypes.c_int64,
+                                 P(ctypes.c_int64)]
+        L.orc_winding.argtypes = [P(LatParams), dp, ctypes.c_int64, ctypes.c_int, P(ctypes.c_int8),
+                                  P(ctypes.c_int64)]
+        L.orc_random_phase_ic.argtypes = [P(LatParams), ctypes.c_uint32, ctypes.c_int, dp]
+        L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_get_threads.restype = ctypes.c_int
+        L.orc_mt_seed.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
+        L.orc_uniform_0_2pi.argtypes = [ctypes.c_void_p]
+        L.orc_uniform_0_2pi.restype = ctypes.c_double
+        _lib = L
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def set_threads(n: int) -> None:
+    lib().orc_set_threads(int(n))
+
+
+def get_threads() -> int:
+    return int(lib().orc_get_threads())
+
+
+def empty_state(p: LatParams) -> np.ndarray:
+    return np.zeros((p.ncomp, 2, p.N), dtype=np.float64)
+
+
+def random_phase_ic(p: LatParams, seed: int, independent: bool = False) -> np.ndarray:
+    st = empty_state(p)
+    lib().orc_random_phase_ic(ctypes.byref(p), ctypes.c_uint32(seed), int(independent), _dp(st))
+    return st
+
+
+def uniform_phases(seed: int, count: int) -> np.ndarray:
+    """The first `count` draws of uniform_real_distribution(0, 2pi) over mt19937(seed)."""
+    g = ctypes.create_string_buffer(624 * 4 + 8)
+    L = lib()
+    L.orc_mt_seed(g, ctypes.c_uint32(seed))
+    return np.array([L.orc_uniform_0_2pi(g) for _ in range(count)])
+
+
+def step(p: LatParams, st: np.ndarray, n: int, diag: bool = False):
+    d = LatDiag()
+    rc = lib().orc_step(ctypes.byref(p), _dp(st), int(n), ctypes.byref(d) if diag else None)
+    if rc != 0:
+        raise RuntimeError(f"orc_step rc={rc}")
+    return d if diag else None
+
+
+def diagnostics(p: LatParams, st: np.ndarray, n: int) -> LatDiag:
+    d = LatDiag()
+    rc = lib().orc_diagnostics(ctypes.byref(p), _dp(st), int(n), ctypes.byref(d))
+    if rc != 0:
+        raise RuntimeError(f"orc_diagnostics rc={rc}")
+    return d
+
+
+def evolve(p: LatParams, st: np.ndarray, n0: int, nsteps: int, diag_every: int = 0):
+    """Run nsteps from TimeStep n0; return list of (n, energy, gauss_abs_sum)."""
+    out = []
+    for n in range(n0, n0 + nsteps):
+        want = diag_every > 0 and n % diag_every == 0
+        d = step(p, st, n, diag=want)
+        if want:
+            out.append((n, d.energy, d.gauss_abs_sum))
+    return out
+
+
+def detect(p: LatParams, st: np.ndarray, n: int, field: int = 0) -> np.ndarray:
+    L = lib()
+    cnt = ctypes.c_int64(0)
+    rc = L.orc_detect(ctypes.byref(p), _dp(st), int(n), int(field), None, 0, ctypes.byref(cnt))
+    if rc != 0:
+        raise RuntimeError(f"orc_detect rc={rc}")
+    xyz = np.zeros((max(cnt.value, 1), 3), dtype=np.float64)
+    rc = L.orc_detect(ctypes.byref(p), _dp(st), int(n), int(field), _dp(xyz), cnt.value, ctypes.byref(cnt))
+    if rc != 0:
+        raise RuntimeError(f"orc_detect rc={rc}")
+    return xyz[: cnt.value]
+
+
+def winding(p: LatParams, st: np.ndarray, n: int, field: int = 0):
+    out = np.zeros((3, p.N), dtype=np.int8)
+    tot = ctypes.c_int64(0)
+    rc = lib().orc_winding(ctypes.byref(p), _dp(st), int(n), int(field),
+                           out.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)), ctypes.byref(tot))
+    if rc != 0:
+        raise RuntimeError(f"orc_winding rc={rc}")
+    return out, int(tot.value)
+
+
+def now_slot(n: int) -> int:
+    return (n + 1) % 2
+
+
+def past_slot(n: int) -> int:
+    return n % 2

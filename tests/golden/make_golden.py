@@ -1,0 +1,223 @@
+"""Generate golden fixtures by running the reference programs themselves.
+
+The reference ships no tests, fixtures or golden outputs.  This script builds
+its programs with oracle/ref/build_ref.py (parameters substituted into a
+scratch copy; 17-digit output; a single-rank MPI stub that dumps the fields),
+runs them on small seeded lattices, and stores inputs and outputs as .npz files
+next to this script.  tests/test_oracle_golden.py then pins the oracle's CPU
+restatement against these files, and the GPU parity tests use them directly.
+
+Run it in a container that has the reference sources:
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle.ref import build_ref  # noqa: E402
+from axions_gb300.params import (BC_FIXED, BC_PERIODIC, ENERGY_EVOLUTION, ENERGY_MPI,  # noqa: E402
+                                 MODEL_AH, MODEL_MOORE, MOORE_CURRENT_CHARGE, MOORE_CURRENT_PLAIN,
+                                 make_params)
+
+OUT = Path(__file__).resolve().parent
+
+
+def _fmt(v: float) -> str:
+    return repr(float(v))
+
+
+def _params_json(p) -> str:
+    return json.dumps(p.as_dict())
+
+
+def read_dump(work: Path, ncomp: int, N: int) -> np.ndarray:
+    raw = np.fromfile(work / "Data" / "axr_fields.bin", dtype=np.float64)
+    assert raw.size == ncomp * 2 * N, (raw.size, ncomp, N)
+    return raw.reshape(ncomp, 2, N)
+
+
+def read_frames(work: Path, prefix: str):
+    frames = []
+    f = 0
+    while True:
+        path = work / "GifData" / f"{prefix}{f}.txt"
+        if not path.exists():
+            break
+        vals = build_ref.read_columns(path)
+        frames.append(vals.reshape(-1, 3))
+        f += 1
+    return frames
+
+
+def pack_frames(frames):
+    counts = np.array([len(a) for a in frames], dtype=np.int64)
+    xyz = np.concatenate(frames, axis=0) if frames else np.zeros((0, 3))
+    return counts, xyz
+
+
+# --------------------------------------------------------------------------
+# mpi_evolution.cpp: random-phase IC from mt19937, in-place update, PRS + damping
+# --------------------------------------------------------------------------
+def gen_mpi_ah(name, nx, ny, nz, nt, lam, g, damped_nt, dampFac, alpha, seed, saveFreq, dt=0.1, d=0.5):
+    consts = {"nx": nx, "ny": ny, "nz": nz, "nt": nt, "dx": d, "dy": d, "dz": d, "dt": dt,
+              "lambda": lam, "eta": 1.0, "g": g, "damped_nt": damped_nt, "dampFac": dampFac,
+              "alpha": alpha, "scaling": 1.0, "makeStringPosGif": True, "saveFreq": saveFreq,
+              "countRate": 10, "outTag": "g", "ic_type": "random", "seed": seed,
+              "stringDetect": True, "detectBuffer": True, "calcEnergy": True}
+    build_ref.build("mpi_evolution", name, consts)
+    work = build_ref.run(name)
+    p = make_params(MODEL_AH, nx=nx, ny=ny, nz=nz, d=d, dt=dt, lam=lam, eta=1.0, g=g,
+                    damped_nt=damped_nt, dampFac=dampFac, alpha=alpha, scaling=1.0, tau0=1.0,
+                    energy_form=ENERGY_MPI, bc=BC_PERIODIC)
+    N = nx * ny * nz
+    final = read_dump(work, 5, N)
+    energy = build_ref.read_columns(work / "Data" / f"valsPerLoop_g_nx{nx}_seed{seed}.txt")
+    frames = read_frames(work, f"gifStringPosData_g_nx{nx}_seed{seed}_")
+    counts, xyz = pack_frames(frames)
+    np.savez_compressed(OUT / f"{name}.npz", program="mpi_evolution", params=_params_json(p), seed=seed,
+                        nt=nt, save_freq=saveFreq, final=final, energy=energy,
+                        frame_counts=counts, frame_xyz=xyz)
+    print(name, "energy lines", energy.size, "frames", counts.tolist())
+
+
+def gen_mpi_ah_ic(name, nx, ny, nz, seed):
+    consts = {"nx": nx, "ny": ny, "nz": nz, "nt": 0, "ic_type": "random", "seed": seed, "eta": 1.0}
+    build_ref.build("mpi_evolution", name, consts)
+    work = build_ref.run(name)
+    N = nx * ny * nz
+    ic = read_dump(work, 5, N)
+    np.savez_compressed(OUT / f"{name}.npz", program="mpi_evolution", seed=seed, nx=nx, ny=ny, nz=nz, ic=ic)
+    print(name, "ic ok")
+
+
+# --------------------------------------------------------------------------
+# moore_mpi_evolution.cpp: equal-phase random IC, current without q
+# --------------------------------------------------------------------------
+def gen_moore_mpi(name, nx, ny, nz, nt, lam1, lam2, lam12, q1, q2, damped_nt, dampFac, alpha, seed,
+                  saveFreq, dt=0.1, d=0.5):
+    consts = {"nx": nx, "ny": ny, "nz": nz, "nt": nt, "dx": d, "dy": d, "dz": d, "dt": dt,
+              "lambda1": lam1, "lambda2": lam2, "lambda12": lam12, "eta1": 1.0, "eta2": 1.0,
+              "q1": q1, "q2": q2, "damped_nt": damped_nt, "dampFac": dampFac, "alpha": alpha,
+              "scaling": 1.0, "makeStringPosGif": True, "saveFreq": saveFreq, "countRate": 10,
+              "outTag": "g", "ic_type": "random", "seed": seed, "stringDetect": True,
+              "detectBuffer": True, "calcEnergy": True}
+    build_ref.build("moore_mpi_evolution", name, consts)
+    work = build_ref.run(name)
+    g = float(np.sqrt(0.5 * lam1 * 1.0 ** 2 / (q1 * q1 + q2 * q2)))
+    p = make_params(MODEL_MOORE, nx=nx, ny=ny, nz=nz, d=d, dt=dt, lam=lam1, lambda2=lam2, lambda12=lam12,
+                    eta=1.0, eta2=1.0, q1=float(q1), q2=float(q2), g=g, damped_nt=damped_nt,
+                    dampFac=dampFac, alpha=alpha, scaling=1.0, tau0=1.0, energy_form=ENERGY_MPI,
+                    bc=BC_PERIODIC, moore_current=MOORE_CURRENT_PLAIN)
+    N = nx * ny * nz
+    final = read_dump(work, 7, N)
+    energy = build_ref.read_columns(work / "Data" / f"valsPerLoop_g_nx{nx}_q1{q1}_seed{seed}.txt")
+    frames = read_frames(work, f"gifStringPosData_g_nx{nx}_q1{q1}_seed{seed}_")
+    counts, xyz = pack_frames(frames)
+    np.savez_compressed(OUT / f"{name}.npz", program="moore_mpi_evolution", params=_params_json(p), seed=seed,
+                        nt=nt, save_freq=saveFreq, final=final, energy=energy,
+                        frame_counts=counts, frame_xyz=xyz)
+    print(name, "energy lines", energy.size, "frames", counts.tolist())
+
+
+# --------------------------------------------------------------------------
+# evolution.cpp: two-level IC from a file, energy + Gauss every step
+# --------------------------------------------------------------------------
+def _two_level_ic(rng, N, ncomp_phi, amp_theta):
+    """Random |phi| and phase, small random link phases; past level perturbed."""
+    now = []
+    for _ in range(ncomp_phi // 2):
+        r = 0.3 + 0.9 * rng.random(N)
+        ph = 2 * np.pi * rng.random(N)
+        now += [r * np.cos(ph), r * np.sin(ph)]
+    for _ in range(3):
+        now.append(amp_theta * (2 * rng.random(N) - 1))
+    now = np.array(now)
+    past = now + 0.02 * (2 * rng.random(now.shape) - 1)
+    return now, past
+
+
+def gen_evolution(name, nx, ny, nz, nt, lam, g, alpha, bc, seed, saveFreq=4, dt=0.1, d=0.5):
+    rng = np.random.default_rng(seed)
+    N = nx * ny * nz
+    now, past = _two_level_ic(rng, N, 2, 0.4)
+    bcs = "periodic" if bc == BC_PERIODIC else "fixed"
+    consts = {"nx": nx, "ny": ny, "nz": nz, "nt": nt, "dx": d, "dy": d, "dz": d, "dt": dt,
+              "lambda": lam, "eta": 1.0, "g": g, "damped_nt": 0, "dampFac": 0.0, "alpha": alpha,
+              "scaling": 1.0, "makeGif": False, "makeStringPosGif": True, "saveFreq": saveFreq,
+              "xyBC": bcs, "zBC": bcs, "stringPos": False, "stationary_ic": False,
+              "stringDetect": True, "detectBuffer": False, "splitLength": False, "finalOut": True}
+    build_ref.build("evolution", name, consts)
+    # "data" IC: level block 0 = slot 0 (past at step 0), block 1 = slot 1 (now)
+    lines = []
+    for lev in (past, now):
+        for s in range(N):
+            lines.append(" ".join(_fmt(lev[c, s]) for c in range(5)))
+    work = build_ref.run(name, stdin="g\n", ic_lines=lines)
+    vals = build_ref.read_columns(work / "Data" / "valsPerLoop_g.txt").reshape(nt, -1)
+    final_newest = build_ref.read_columns(work / "Data" / "finalField.txt").reshape(N, 5).T.copy()
+    frames = read_frames(work, "gifStringPosData_")
+    counts, xyz = pack_frames(frames)
+    p = make_params(MODEL_AH, nx=nx, ny=ny, nz=nz, d=d, dt=dt, lam=lam, eta=1.0, g=g, damped_nt=0,
+                    dampFac=0.0, alpha=alpha, scaling=1.0, tau0=1.0, energy_form=ENERGY_EVOLUTION, bc=bc)
+    ic = np.stack([past, now], axis=1)  # (comp, slot, N)
+    np.savez_compressed(OUT / f"{name}.npz", program="evolution", params=_params_json(p), nt=nt,
+                        save_freq=saveFreq, ic=ic, final_newest=final_newest, energy=vals[:, 0],
+                        deviation=vals[:, 1], frame_counts=counts, frame_xyz=xyz)
+    print(name, "vals", vals.shape, "frames", counts.tolist())
+
+
+# --------------------------------------------------------------------------
+# mooreEvol.cpp: fixed boundaries, stationary IC from file, q-weighted current
+# --------------------------------------------------------------------------
+def gen_moore_evol(name, nx, ny, nz, nt, lam1, lam2, lam12, q1, q2, seed, dt=0.1, d=0.5):
+    rng = np.random.default_rng(seed)
+    N = nx * ny * nz
+    now, _ = _two_level_ic(rng, N, 4, 0.4)
+    consts = {"nx": nx, "ny": ny, "nz": nz, "nt": nt, "dx": d, "dy": d, "dz": d, "dt": dt,
+              "eta1": 1.0, "eta2": 1.0, "lambda1": lam1, "lambda2": lam2, "lambda12": lam12,
+              "q1": q1, "q2": q2, "makeGif": False, "saveFreq": 10, "xyBC": "fixed"}
+    build_ref.build("mooreEvol", name, consts)
+    lines = [" ".join(_fmt(now[c, s]) for c in range(7)) for s in range(N)]
+    work = build_ref.run(name, ic_lines=lines, ic_name="moore_ic.txt")
+    vals = build_ref.read_columns(work / "Data" / "valsPerLoop.txt").reshape(nt, 2)
+    final_newest = build_ref.read_columns(work / "Data" / "finalField.txt").reshape(N, 7).T.copy()
+    g = float(np.sqrt(0.5 * lam1 * 1.0 ** 2 / (q1 * q1 + q2 * q2)))
+    p = make_params(MODEL_MOORE, nx=nx, ny=ny, nz=nz, d=d, dt=dt, lam=lam1, lambda2=lam2, lambda12=lam12,
+                    eta=1.0, eta2=1.0, q1=float(q1), q2=float(q2), g=g, damped_nt=0, dampFac=0.0,
+                    alpha=0.0, scaling=1.0, tau0=1.0, energy_form=ENERGY_EVOLUTION, bc=BC_FIXED,
+                    moore_current=MOORE_CURRENT_CHARGE)
+    ic = np.stack([now, now], axis=1)
+    np.savez_compressed(OUT / f"{name}.npz", program="mooreEvol", params=_params_json(p), nt=nt, ic=ic,
+                        final_newest=final_newest, energy=vals[:, 0], deviation=vals[:, 1])
+    print(name, "vals", vals.shape)
+
+
+def main():
+    if not build_ref.reference_available():
+        raise SystemExit("reference sources not found; fixtures can only be made where they are")
+    gen_mpi_ah_ic("ref_mpi_ah_ic_s7", 6, 5, 4, seed=7)
+    # config-1 physics (lambda=2, e=1, dx=0.5, dt=0.1, Minkowski, no damping)
+    gen_mpi_ah("ref_mpi_ah_c1", 14, 12, 10, 30, lam=2.0, g=1.0, damped_nt=0, dampFac=0.0, alpha=0.0,
+               seed=42, saveFreq=10)
+    # PRS friction + damping phase + detection buffer
+    gen_mpi_ah("ref_mpi_ah_prs", 12, 10, 8, 20, lam=2.0, g=1.0, damped_nt=6, dampFac=0.5, alpha=3.0,
+               seed=5, saveFreq=5)
+    # global strings (g = 0), the reference default
+    gen_mpi_ah("ref_mpi_ah_global", 10, 10, 10, 12, lam=1.0, g=0.0, damped_nt=4, dampFac=0.5, alpha=3.0,
+               seed=3, saveFreq=4)
+    gen_evolution("ref_evol_ah_periodic", 12, 10, 8, 12, lam=2.0, g=1.0, alpha=3.0, bc=BC_PERIODIC, seed=11)
+    gen_evolution("ref_evol_ah_fixed", 11, 10, 9, 10, lam=2.0, g=0.7, alpha=0.0, bc=BC_FIXED, seed=12)
+    gen_moore_mpi("ref_moore_mpi", 12, 10, 8, 20, 2.0, 2.0, 0.5, 2, 1, damped_nt=6, dampFac=0.5, alpha=3.0,
+                  seed=9, saveFreq=5)
+    gen_moore_evol("ref_moore_evol", 10, 9, 8, 12, 2.0, 2.0, 0.5, 2, 1, seed=13)
+
+
+if __name__ == "__main__":
+    main()

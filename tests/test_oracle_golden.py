@@ -1,0 +1,99 @@
+"""Pin the oracle (CPU restatement) against outputs of the reference itself.
+
+The fixtures in tests/golden/ were produced by running the reference programs
+(tests/golden/make_golden.py).  Fields, energies and crossing lists must agree
+bit for bit; the only exception is mooreEvol's deviation column, which the
+reference normalises per site before summing (mooreEvol.cpp:383), so it is
+compared to 1e-13 relative.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, params_from_json
+
+MPI_CASES = ["ref_mpi_ah_c1", "ref_mpi_ah_prs", "ref_mpi_ah_global", "ref_moore_mpi"]
+OMP_CASES = ["ref_evol_ah_periodic", "ref_evol_ah_fixed", "ref_moore_evol"]
+
+
+def test_random_ic_matches_reference_mt19937(oracle_mod):
+    from axions_gb300.params import make_params
+    z = load_golden("ref_mpi_ah_ic_s7")
+    p = make_params(0, nx=int(z["nx"]), ny=int(z["ny"]), nz=int(z["nz"]))
+    st = oracle_mod.random_phase_ic(p, int(z["seed"]))
+    assert np.array_equal(st, z["ic"])
+
+
+def _run_mpi_program(O, z, p):
+    """Replay the reference loop: detection (with the stringsExist latch) then step."""
+    O.set_threads(1)
+    st = O.random_phase_ic(p, int(z["seed"]))
+    nt, sf = int(z["nt"]), int(z["save_freq"])
+    energies, frames, exist = [], [], True
+    for n in range(nt):
+        if n % sf == 0 and n >= p.damped_nt and exist:
+            xyz = O.detect(p, st, n, 0)
+            frames.append(xyz)
+            exist = len(xyz) > 0
+        energies.append(O.step(p, st, n, diag=True).energy)
+    return st, np.array(energies), frames
+
+
+@pytest.mark.parametrize("name", MPI_CASES)
+def test_mpi_programs_bit_exact(oracle_mod, name):
+    z = load_golden(name)
+    p = params_from_json(z["params"])
+    st, energy, frames = _run_mpi_program(oracle_mod, z, p)
+    assert np.array_equal(st, z["final"]), "fields (both time slots) differ from the reference"
+    assert np.array_equal(energy, z["energy"], equal_nan=True)
+    assert [len(f) for f in frames] == z["frame_counts"].tolist()
+    assert np.array_equal(np.concatenate(frames), z["frame_xyz"])
+
+
+@pytest.mark.parametrize("name", OMP_CASES)
+def test_openmp_programs_bit_exact(oracle_mod, name):
+    O = oracle_mod
+    O.set_threads(1)
+    z = load_golden(name)
+    p = params_from_json(z["params"])
+    st = z["ic"].copy()
+    nt = int(z["nt"])
+    sf = int(z["save_freq"]) if "save_freq" in z.files else 0
+    E, D, frames = [], [], []
+    for n in range(nt):
+        if sf and n % sf == 0:
+            frames.append(O.detect(p, st, n, 0))
+        d = O.step(p, st, n, diag=True)
+        E.append(d.energy)
+        D.append(d.gauss_abs_sum)
+    E, D = np.array(E), np.array(D)
+    assert np.array_equal(st[:, (nt + 1) % 2, :], z["final_newest"])
+    assert np.array_equal(E, z["energy"])
+    if p.model == 0:
+        if p.bc == 0:
+            dev = D / (p.nx * p.ny) / p.nz                      # evolution.cpp:1404-1408
+        else:
+            dev = D / ((p.nx - 2) * (p.ny - 2)) / (p.nz - 2)
+        assert np.array_equal(dev, z["deviation"])
+    else:
+        c = (p.nx - 2) * (p.ny - 2) * (p.nz - 2)               # mooreEvol.cpp:383,697
+        np.testing.assert_allclose(D / c / c, z["deviation"], rtol=1e-13, atol=0)
+    if sf:
+        assert [len(f) for f in frames] == z["frame_counts"].tolist()
+        assert np.array_equal(np.concatenate(frames), z["frame_xyz"])
+
+
+def test_oracle_threads_do_not_change_fields(oracle_mod):
+    """The in-place update is race-free: any thread count gives identical fields."""
+    O = oracle_mod
+    z = load_golden("ref_mpi_ah_prs")
+    p = params_from_json(z["params"])
+    outs = []
+    for t in (1, 4):
+        O.set_threads(t)
+        st = O.random_phase_ic(p, int(z["seed"]))
+        for n in range(int(z["nt"])):
+            O.step(p, st, n)
+        outs.append(st)
+    O.set_threads(1)
+    assert np.array_equal(outs[0], outs[1])
+    assert np.array_equal(outs[0], z["final"])
