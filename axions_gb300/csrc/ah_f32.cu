@@ -1,0 +1,18 @@
+// Abelian-Higgs step kernels, float instantiation.
+#include "ah_step.cuh"
+
+namespace lat {
+
+cudaError_t launch_ah_step_f32(const Geom& g, const Fields<float, 5>& f, const StepCoef& c, const DiagOut& d, bool diag,
+                               cudaStream_t st)
+{
+    return launch_ah_step_t<float>(g, f, c, d, diag, st);
+}
+
+cudaError_t launch_divergence_f32(const Geom& g, const float* tx, const float* ty, const float* tz, const StepCoef& c,
+                                  float* out, cudaStream_t st)
+{
+    return launch_divergence_t<float>(g, tx, ty, tz, c, out, st);
+}
+
+}  // namespace lat

@@ -1,0 +1,126 @@
+// Internal declarations shared by the CUDA translation units of
+// liblattice_gpu.so.  Not part of the C ABI (that is include/lattice_gpu.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/lattice_gpu.h"
+
+namespace lat {
+
+// ---------------------------------------------------------------------------
+// geometry of the evolved region
+// ---------------------------------------------------------------------------
+struct Geom {
+    int nx, ny, nz;       // lattice sides
+    int syz;              // ny*nz
+    int lo;               // first evolved index per axis (0 periodic, 1 fixed)
+    int hix, hiy, hiz;    // one past the last evolved index per axis
+};
+
+// thread-block shape of the site kernels: 32 along z (coalesced), 8 along y
+constexpr int BZ = 32;
+constexpr int BY = 8;
+constexpr int BLOCK = BZ * BY;
+
+inline dim3 site_grid(const Geom& g)
+{
+    return dim3((unsigned)((g.hiz - g.lo + BZ - 1) / BZ), (unsigned)((g.hiy - g.lo + BY - 1) / BY),
+                (unsigned)(g.hix - g.lo));
+}
+
+// ---------------------------------------------------------------------------
+// per-step coefficients.  Each is the exact double the reference evaluates
+// (same operands, same order), so an FP64 kernel reproduces its arithmetic.
+// ---------------------------------------------------------------------------
+struct StepCoef {
+    double dx2, dy2, dz2;        // dx*dx ...
+    double dt, dt2;              // dt, dt*dt
+    double halfLambda, etaSq;    // 0.5*lambda, eta*eta        (AH; Moore phi1)
+    double halfLambda2, eta2Sq;  // 0.5*lambda2, eta2*eta2     (Moore phi2)
+    double halfLambda12;         // 0.5*lambda12               (Moore)
+    double m2gg;                 // (-2*g)*g
+    double fric;                 // damp + alpha*scaling/tau
+    double damp;                 // dampFac or 0
+    double q1, q2;               // Moore charges
+    // diagnostics
+    double dx, dy, dz, g;
+    double gdtdx, gdtdy, gdtdz;  // (g*dt)*dmu
+    double gxy2, gxz2, gyz2;     // ((g*dx)*dy)^2 ...
+    double dV;                   // (dx*dy)*dz
+    double quarterLambda, quarterLambda2, halfLambda12e;  // 0.25*lambda, 0.25*lambda2, 0.5*lambda12
+    double twog;                 // 2*g
+    // reciprocals for the FP32 path
+    double inv_dx2, inv_dy2, inv_dz2, inv_dt, inv_dx, inv_dy, inv_dz, inv_g;
+};
+
+StepCoef make_coef(const lat_params& p, int64_t n);
+Geom make_geom(const lat_params& p);
+
+// Kernel argument block: base pointers of the two slots of every component.
+template <class T, int NC>
+struct Fields {
+    const T* __restrict__ now[NC];
+    T* past[NC];
+};
+
+struct DiagOut {
+    double* partials;    // [2 * nblocks]: energy, |G| per block (or nullptr)
+    void* divbuf;        // divergence of theta at one level, [N] of T
+    int use_div;         // the diagnostic reads divbuf as the past-level divergence
+    int store_div;       // write the now-level divergence into divbuf
+    int energy_form;     // LAT_ENERGY_*
+    int charge_current;  // Moore: q-weighted current
+    int write;           // 0: diagnostics only, the state is left unchanged
+};
+
+// launchers (one translation unit per model/precision)
+cudaError_t launch_ah_step_f64(const Geom&, const Fields<double, 5>&, const StepCoef&, const DiagOut&, bool diag,
+                               cudaStream_t);
+cudaError_t launch_ah_step_f32(const Geom&, const Fields<float, 5>&, const StepCoef&, const DiagOut&, bool diag,
+                               cudaStream_t);
+cudaError_t launch_moore_step_f64(const Geom&, const Fields<double, 7>&, const StepCoef&, const DiagOut&, bool diag,
+                                  cudaStream_t);
+cudaError_t launch_moore_step_f32(const Geom&, const Fields<float, 7>&, const StepCoef&, const DiagOut&, bool diag,
+                                  cudaStream_t);
+// divergence of theta on one level into divbuf (used when no previous step stored it)
+cudaError_t launch_divergence_f64(const Geom&, const double* thx, const double* thy, const double* thz,
+                                  const StepCoef&, double* out, cudaStream_t);
+cudaError_t launch_divergence_f32(const Geom&, const float* thx, const float* thy, const float* thz,
+                                  const StepCoef&, float* out, cudaStream_t);
+
+// deterministic sum of per-block partials into out[0..1] (energy, |G|)
+cudaError_t launch_finalize(const double* partials, int nblocks, double* out, cudaStream_t);
+
+// conversions between the double host layout and FP32 device fields
+cudaError_t launch_d2f(const double* in, float* out, int64_t n, cudaStream_t);
+cudaError_t launch_f2d(const float* in, double* out, int64_t n, cudaStream_t);
+
+// detection
+struct DetectArgs {
+    int nx, ny, nz, syz, lo, hix, hiy, hiz;
+    double dx, dy, dz;
+    int x0, y0, z0;
+};
+int detect_block_sites();
+cudaError_t launch_detect_count_f64(const DetectArgs&, const double* re, const double* im, long long* block_totals,
+                                    int nblocks, cudaStream_t);
+cudaError_t launch_detect_count_f32(const DetectArgs&, const float* re, const float* im, long long* block_totals,
+                                    int nblocks, cudaStream_t);
+cudaError_t launch_scan_totals(long long* block_totals, int nblocks, long long* total, cudaStream_t);
+cudaError_t launch_detect_write_f64(const DetectArgs&, const double* re, const double* im, const long long* block_offsets,
+                                    int nblocks, double* xyz, long long cap, cudaStream_t);
+cudaError_t launch_detect_write_f32(const DetectArgs&, const float* re, const float* im, const long long* block_offsets,
+                                    int nblocks, double* xyz, long long cap, cudaStream_t);
+cudaError_t launch_winding_f64(const DetectArgs&, int fixed, const double* re, const double* im, int8_t* out,
+                               unsigned long long* abs_sum, cudaStream_t);
+cudaError_t launch_winding_f32(const DetectArgs&, int fixed, const float* re, const float* im, int8_t* out,
+                               unsigned long long* abs_sum, cudaStream_t);
+
+// error reporting
+void set_error(const std::string& msg);
+
+}  // namespace lat

@@ -1,0 +1,92 @@
+// Device helpers shared by the site kernels.
+#pragma once
+
+#include "lattice_internal.cuh"
+
+namespace lat {
+
+// Transcendentals by precision.  The FP64 path calls CUDA's double-precision
+// sin/cos, the FP32 path the full-accuracy single-precision ones.
+template <class T>
+struct Trig;
+template <>
+struct Trig<double> {
+    static __device__ __forceinline__ double sin(double x) { return ::sin(x); }
+    static __device__ __forceinline__ double cos(double x) { return ::cos(x); }
+    static __device__ __forceinline__ void sincos(double x, double* s, double* c) { ::sincos(x, s, c); }
+};
+template <>
+struct Trig<float> {
+    static __device__ __forceinline__ float sin(float x) { return ::sinf(x); }
+    static __device__ __forceinline__ float cos(float x) { return ::cosf(x); }
+    static __device__ __forceinline__ void sincos(float x, float* s, float* c) { ::sincosf(x, s, c); }
+};
+
+// a / b.  FP64 divides (the reference's rounding); FP32 multiplies by the
+// reciprocal computed once on the host.
+template <class T>
+__device__ __forceinline__ T qdiv(T a, double b, double inv_b)
+{
+    if constexpr (sizeof(T) == 8) return a / b;
+    else return a * (T)inv_b;
+}
+
+// Leapfrog update X^{n+1} from X^n, X^{n-1} and the acceleration.
+// FP64 keeps the reference's expression 2*X - Xp + dt^2*a
+// (mpi_evolution.cpp:432).  FP32 uses X + (X - Xp) + dt^2*a: the difference
+// of two consecutive levels is exact in floating point (they are within a
+// factor two of each other), so only the velocity term is rounded.
+template <class T>
+__device__ __forceinline__ T leapfrog(T xn, T xp, T dt2, T acc)
+{
+    if constexpr (sizeof(T) == 8) return 2 * xn - xp + dt2 * acc;
+    else return xn + (xn - xp) + dt2 * acc;
+}
+
+// Periodic / fixed neighbour offsets of one site.
+struct Nbr {
+    int s, xp, xm, yp, ym, zp, zm;  // xp = offset to i+1 etc.
+};
+
+__device__ __forceinline__ Nbr make_nbr(const Geom& g, int i, int j, int k)
+{
+    Nbr n;
+    n.s = (i * g.ny + j) * g.nz + k;
+    n.xp = (i + 1 == g.nx) ? -(g.nx - 1) * g.syz : g.syz;
+    n.xm = (i == 0) ? (g.nx - 1) * g.syz : -g.syz;
+    n.yp = (j + 1 == g.ny) ? -(g.ny - 1) * g.nz : g.nz;
+    n.ym = (j == 0) ? (g.ny - 1) * g.nz : -g.nz;
+    n.zp = (k + 1 == g.nz) ? -(g.nz - 1) : 1;
+    n.zm = (k == 0) ? (g.nz - 1) : -1;
+    return n;
+}
+
+// Sum two doubles over the block (BLOCK threads) and write them to
+// partials[2*b], partials[2*b+1].  Fixed tree: deterministic for a fixed grid.
+__device__ __forceinline__ void block_sum2_store(double a, double b, double* partials)
+{
+    __shared__ double red[2][BLOCK / 32];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if ((tid & 31) == 0) {
+        red[0][tid >> 5] = a;
+        red[1][tid >> 5] = b;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double sa = 0, sb = 0;
+        for (int w = 0; w < BLOCK / 32; ++w) {
+            sa += red[0][w];
+            sb += red[1][w];
+        }
+        const int blk = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+        partials[2 * blk] = sa;
+        partials[2 * blk + 1] = sb;
+    }
+}
+
+}  // namespace lat

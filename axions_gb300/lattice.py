@@ -1,0 +1,227 @@
+"""Python mirror of the C ABI in include/lattice_gpu.h (ctypes).
+
+This is how tests, the benchmark and Python users drive the CUDA library.  It
+loads axions_gb300/liblattice_gpu.so from this package directory and raises if
+it is missing or cannot reach a GPU: there is no CPU fallback.
+
+Array conventions (same as the C ABI): a level is float64 of shape
+(ncomp, nx*ny*nz); components AH = (phi_re, phi_im, theta_x, theta_y,
+theta_z), Moore = (phi1_re, phi1_im, phi2_re, phi2_im, theta_x, theta_y,
+theta_z); sites in linear order (i*ny + j)*nz + k.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from .params import (LAT_ERR_CAPACITY, LAT_OK, LatParams, MODEL_AH, make_params)  # noqa: F401
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "liblattice_gpu.so"
+
+# every entry point declared in include/lattice_gpu.h
+EXPORTS = [
+    "lat_version", "lat_last_error", "lat_params_init", "lat_random_phase_ic", "lat_create", "lat_destroy",
+    "lat_set_stream", "lat_get_params", "lat_num_components", "lat_time_step", "lat_device_bytes",
+    "lat_kernel_launches",
+    "lat_set_state", "lat_get_state", "lat_step", "lat_step_diag", "lat_advance", "lat_diagnostics",
+    "lat_detect_crossings", "lat_winding",
+]
+
+
+class LatDiag(ctypes.Structure):
+    _fields_ = [("energy", ctypes.c_double), ("gauss_abs_sum", ctypes.c_double),
+                ("sites", ctypes.c_int64), ("time_step", ctypes.c_int64)]
+
+
+class LatticeError(RuntimeError):
+    def __init__(self, fn: str, code: int, msg: str):
+        super().__init__(f"{fn} failed with status {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load_library(path: Path | None = None):
+    """Load the CUDA library (build it first with axions_gb300.build)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} not found: build it with `python -m axions_gb300.build` "
+                           "(no CPU fallback exists)")
+    L = ctypes.CDLL(str(p))
+    P = ctypes.POINTER
+    vp = ctypes.c_void_p
+    dp = P(ctypes.c_double)
+    L.lat_version.restype = ctypes.c_char_p
+    L.lat_last_error.restype = ctypes.c_char_p
+    L.lat_params_init.argtypes = [P(LatParams), ctypes.c_int32]
+    L.lat_random_phase_ic.argtypes = [P(LatParams), ctypes.c_uint32, ctypes.c_int32, dp]
+    L.lat_create.argtypes = [P(LatParams), P(vp)]
+    L.lat_destroy.argtypes = [vp]
+    L.lat_set_stream.argtypes = [vp, vp]
+    L.lat_get_params.argtypes = [vp, P(LatParams)]
+    L.lat_num_components.argtypes = [vp]
+    L.lat_time_step.argtypes = [vp]
+    L.lat_time_step.restype = ctypes.c_int64
+    L.lat_device_bytes.argtypes = [vp]
+    L.lat_device_bytes.restype = ctypes.c_int64
+    L.lat_kernel_launches.argtypes = [vp]
+    L.lat_kernel_launches.restype = ctypes.c_int64
+    L.lat_set_state.argtypes = [vp, dp, dp, ctypes.c_int64]
+    L.lat_get_state.argtypes = [vp, dp, dp]
+    L.lat_step.argtypes = [vp, ctypes.c_int32]
+    L.lat_step_diag.argtypes = [vp, P(LatDiag)]
+    L.lat_advance.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, P(LatDiag), ctypes.c_int64, P(ctypes.c_int64)]
+    L.lat_diagnostics.argtypes = [vp, P(LatDiag)]
+    L.lat_detect_crossings.argtypes = [vp, ctypes.c_int32, dp, ctypes.c_int64, P(ctypes.c_int64)]
+    L.lat_winding.argtypes = [vp, ctypes.c_int32, P(ctypes.c_int8), P(ctypes.c_int64)]
+    if path is None:
+        _lib = L
+    return L
+
+
+def _dp(a: np.ndarray):
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous float64 array")
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _check(fn: str, rc: int):
+    if rc != LAT_OK:
+        raise LatticeError(fn, rc, (load_library().lat_last_error() or b"").decode())
+
+
+def params_init(model: int = MODEL_AH) -> LatParams:
+    p = LatParams()
+    _check("lat_params_init", load_library().lat_params_init(ctypes.byref(p), int(model)))
+    return p
+
+
+def random_phase_ic(p: LatParams, seed: int, independent: bool = False) -> np.ndarray:
+    """Seeded uniform-phase IC of mpi_evolution.cpp:287-312 (one level, (ncomp, N))."""
+    out = np.zeros((p.ncomp, p.N), dtype=np.float64)
+    _check("lat_random_phase_ic",
+           load_library().lat_random_phase_ic(ctypes.byref(p), ctypes.c_uint32(seed), int(bool(independent)), _dp(out)))
+    return out
+
+
+class Lattice:
+    """One lattice resident on the current CUDA device."""
+
+    def __init__(self, params: LatParams):
+        self.L = load_library()
+        self.params = params.copy()
+        h = ctypes.c_void_p()
+        _check("lat_create", self.L.lat_create(ctypes.byref(self.params), ctypes.byref(h)))
+        self.h = h
+        self.ncomp = self.params.ncomp
+        self.N = self.params.N
+
+    # lifetime ------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.L.lat_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # properties ------------------------------------------------------------
+    @property
+    def time_step(self) -> int:
+        return int(self.L.lat_time_step(self.h))
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.L.lat_kernel_launches(self.h))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.L.lat_device_bytes(self.h))
+
+    def set_stream(self, stream_handle: int | None):
+        _check("lat_set_stream", self.L.lat_set_stream(self.h, ctypes.c_void_p(stream_handle or 0)))
+
+    # state -----------------------------------------------------------------
+    def set_state(self, now: np.ndarray, past: np.ndarray | None = None, time_step: int = 0):
+        now = np.ascontiguousarray(now, dtype=np.float64).reshape(self.ncomp, self.N)
+        past = now if past is None else np.ascontiguousarray(past, dtype=np.float64).reshape(self.ncomp, self.N)
+        _check("lat_set_state", self.L.lat_set_state(self.h, _dp(now), _dp(past), int(time_step)))
+
+    def set_slots(self, st: np.ndarray, time_step: int):
+        """Upload a reference-layout state (ncomp, 2, N) whose slot parity matches time_step."""
+        now = np.ascontiguousarray(st[:, (time_step + 1) % 2, :])
+        past = np.ascontiguousarray(st[:, time_step % 2, :])
+        self.set_state(now, past, time_step)
+
+    def get_state(self):
+        now = np.empty((self.ncomp, self.N), dtype=np.float64)
+        past = np.empty((self.ncomp, self.N), dtype=np.float64)
+        _check("lat_get_state", self.L.lat_get_state(self.h, _dp(now), _dp(past)))
+        return now, past
+
+    def get_slots(self) -> np.ndarray:
+        n = self.time_step
+        now, past = self.get_state()
+        st = np.empty((self.ncomp, 2, self.N), dtype=np.float64)
+        st[:, (n + 1) % 2, :] = now
+        st[:, n % 2, :] = past
+        return st
+
+    # evolution ---------------------------------------------------------------
+    def step(self, nsteps: int = 1):
+        _check("lat_step", self.L.lat_step(self.h, int(nsteps)))
+
+    def step_diag(self) -> LatDiag:
+        d = LatDiag()
+        _check("lat_step_diag", self.L.lat_step_diag(self.h, ctypes.byref(d)))
+        return d
+
+    def advance(self, nsteps: int, diag_every: int = 0):
+        """Run nsteps; return a list of (time_step, energy, gauss_abs_sum)."""
+        cap = 0
+        if diag_every > 0:
+            n0 = self.time_step
+            cap = sum(1 for n in range(n0, n0 + nsteps) if n % diag_every == 0)
+        buf = (LatDiag * max(cap, 1))()
+        cnt = ctypes.c_int64(0)
+        _check("lat_advance", self.L.lat_advance(self.h, int(nsteps), int(diag_every), buf, int(cap), ctypes.byref(cnt)))
+        return [(buf[q].time_step, buf[q].energy, buf[q].gauss_abs_sum) for q in range(cnt.value)]
+
+    def diagnostics(self) -> LatDiag:
+        d = LatDiag()
+        _check("lat_diagnostics", self.L.lat_diagnostics(self.h, ctypes.byref(d)))
+        return d
+
+    # detection -----------------------------------------------------------------
+    def detect(self, field: int = 0) -> np.ndarray:
+        cnt = ctypes.c_int64(0)
+        _check("lat_detect_crossings", self.L.lat_detect_crossings(self.h, int(field), None, 0, ctypes.byref(cnt)))
+        n = cnt.value
+        xyz = np.zeros((max(n, 1), 3), dtype=np.float64)
+        if n:
+            _check("lat_detect_crossings",
+                   self.L.lat_detect_crossings(self.h, int(field), _dp(xyz), n, ctypes.byref(cnt)))
+        return xyz[:n]
+
+    def winding(self, field: int = 0, want_array: bool = True):
+        tot = ctypes.c_int64(0)
+        out = np.zeros((3, self.N), dtype=np.int8) if want_array else None
+        ptr = out.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)) if want_array else None
+        _check("lat_winding", self.L.lat_winding(self.h, int(field), ptr, ctypes.byref(tot)))
+        return out, int(tot.value)

@@ -1,0 +1,367 @@
+#!/usr/bin/env python
+"""Benchmark of the lattice evolution hot path on GB300.
+
+Workload (one "step" = one leapfrog step of the whole lattice): Abelian-Higgs,
+512^3 periodic, lambda=2, e=1, eta=1, dx=0.5, dt=0.1, PRS expansion friction
+alpha=3 (a ~ tau, tau0=1), energy + Gauss diagnostics every 20 steps, seeded
+uniform-phase ICs (mt19937, as mpi_evolution.cpp:287-312).  The plain FP64
+path is the headline; the FP32 form is measured in the same run.
+
+Reported (one JSON line on rank 0):
+  value        site-updates/s with the state resident in HBM (CUDA events on the
+               library's stream around the K timed steps);
+  e2e          the same metric through the C ABI with host buffers: upload of
+               the state from pinned memory, the K steps (diagnostics copied
+               back at their cadence) and download of the final state, all
+               inside the timed region;
+  roofline     dominant kernel (the step kernel): algorithmic bytes per
+               site-update x sites / its average launch time, against the
+               measured HBM copy bandwidth;
+  cpu_baseline the oracle's CPU restatement (same arithmetic as the reference)
+               on all host cores, on a bounded sample of the workload.
+
+--impl reference times that CPU implementation alone for the same metric.
+Multi-GPU: independent replicas (the path is not sharded), one per rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+BYTES_PER_SITE = {"f64": 120, "f32": 60}     # 5 values x (read now, read past, write new)
+DIAG_EVERY = 20
+
+
+def workload_params(n: int, precision: str):
+    from axions_gb300.params import ENERGY_EVOLUTION, F32, F64, make_params
+    return make_params(0, n=n, d=0.5, dt=0.1, lam=2.0, eta=1.0, g=1.0, damped_nt=0, dampFac=0.0, alpha=3.0,
+                       scaling=1.0, tau0=1.0, energy_form=ENERGY_EVOLUTION,
+                       precision=F64 if precision == "f64" else F32)
+
+
+def workload_name(n: int) -> str:
+    return (f"Abelian-Higgs {n}^3 periodic, lambda=2, e=1, eta=1, dx=0.5, dt=0.1, PRS friction alpha=3 "
+            f"(a~tau, tau0=1), energy+Gauss every {DIAG_EVERY} steps")
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in rows for q in range(4) if r[5 + q].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers (replicas)
+# ---------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws: int, backend: str):
+    if ws > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group(backend=backend)
+
+
+def dist_barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def dist_max(ws: int, x: float, device=None) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(ws: int, x: float, device=None) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# CPU implementation (the oracle's restatement of the reference arithmetic)
+# ---------------------------------------------------------------------------
+def cpu_rate(n: int, seconds: float, min_steps: int = 2):
+    """Site-updates/s of the CPU implementation on all host cores, on an n^3
+    sample of the workload; steps are run until `seconds` have passed."""
+    from oracle import oracle as O
+    p = workload_params(n, "f64")
+    st = O.random_phase_ic(p, 42)
+    O.step(p, st, 0)  # first touch
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        n_step = 1 + steps
+        d = n_step % DIAG_EVERY == 0
+        O.step(p, st, n_step, diag=d)
+        steps += 1
+        el = time.perf_counter() - t0
+        if steps >= min_steps and el >= seconds:
+            break
+    return p.N * steps / el, O.get_threads(), steps, el
+
+
+# ---------------------------------------------------------------------------
+# GPU measurement
+# ---------------------------------------------------------------------------
+def load_traffic(precision: str, n: int):
+    """DRAM traffic per launch of the step kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "traffic.json"
+    if not f.exists():
+        return None
+    try:
+        d = json.loads(f.read_text())
+        e = d.get(f"ah_step_{precision}")
+        if not e:
+            return None
+        return e["bytes_per_site"] * n ** 3
+    except Exception:
+        return None
+
+
+def measure_gpu(n: int, precision: str, steps: int, warmup: int, ws: int, local: int, peaks: dict):
+    import numpy as np
+    import torch
+
+    from axions_gb300 import lattice
+
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    p = workload_params(n, precision)
+    ic = lattice.random_phase_ic(p, 42 + local)
+    lat = lattice.Lattice(p)
+    lat.set_stream(stream.cuda_stream)
+    lat.set_state(ic, ic, 0)
+
+    def one_step():
+        return lat.advance(1, DIAG_EVERY)
+
+    for _ in range(warmup):
+        one_step()
+    torch.cuda.synchronize(dev)
+    dist_barrier(ws)
+    torch.cuda.synchronize(dev)
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kinds = []
+    clock = ClockSampler(local)
+    clock.start()
+    launches0 = lat.kernel_launches
+    t_start.record(stream)
+    for q in range(steps):
+        nstep = lat.time_step
+        kinds.append("diag" if nstep % DIAG_EVERY == 0 else ("store" if (nstep + 1) % DIAG_EVERY == 0 else "plain"))
+        evs[q][0].record(stream)
+        one_step()
+        evs[q][1].record(stream)
+    t_end.record(stream)
+    torch.cuda.synchronize(dev)
+    launches = lat.kernel_launches - launches0
+    dist_barrier(ws)
+    torch.cuda.synchronize(dev)
+    clocks = clock.stop()
+    total_ms = t_start.elapsed_time(t_end)
+    per = [a.elapsed_time(b) for a, b in evs]
+    plain = [t for t, k in zip(per, kinds) if k == "plain"] or per
+    kern_ms = statistics.median(plain)
+
+    # end to end through the C ABI with host buffers (pinned), timed the same way
+    nc, N = lat.ncomp, lat.N
+    pin_now = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
+    pin_past = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
+    pin_now.numpy()[:] = ic
+    pin_past.numpy()[:] = ic
+    out_now = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
+    out_past = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
+    dist_barrier(ws)
+    torch.cuda.synchronize(dev)
+    e0 = time.perf_counter()
+    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_start.record(stream)
+    lat.set_state(pin_now.numpy(), pin_past.numpy(), 0)
+    diags = lat.advance(steps, DIAG_EVERY)
+    lat.L.lat_get_state(lat.h, out_now.numpy().ctypes.data_as(lattice.ctypes.POINTER(lattice.ctypes.c_double)),
+                        out_past.numpy().ctypes.data_as(lattice.ctypes.POINTER(lattice.ctypes.c_double)))
+    e_end.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_wall = time.perf_counter() - e0
+    e2e_ms = e_start.elapsed_time(e_end)
+    if not np.isfinite(out_now.numpy()).all():
+        raise RuntimeError("non-finite field after the end-to-end run")
+    lat.close()
+    del pin_now, pin_past, out_now, out_past
+
+    state_bytes = 2 * nc * N * 8
+    return {
+        "total_ms": total_ms, "kern_ms": kern_ms, "per_ms": per, "kinds": kinds, "launches": launches,
+        "clocks": clocks, "e2e_ms": max(e2e_ms, 1e3 * e2e_wall), "e2e_h2d": state_bytes / steps,
+        "e2e_d2h": (state_bytes + 16 * len(diags)) / steps, "sites": N,
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=512, help="lattice side (workload: 512)")
+    ap.add_argument("--cpu-n", type=int, default=256, help="side of the CPU sample lattice")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    steps, warmup, n = args.steps, max(args.warmup, 0), args.n
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        rates = []
+        from oracle import oracle as O  # noqa: F401
+        for _ in range(warmup):
+            cpu_rate(args.cpu_n, 0.0, min_steps=1)
+        t0 = time.perf_counter()
+        r, cores, ns, el = cpu_rate(args.cpu_n, 0.0, min_steps=steps)
+        rates.append(r)
+        line = {"impl": "reference", "metric": "site-updates/s", "value": r, "unit": "site-updates/s",
+                "n_gpus": args.gpus, "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * el / ns,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic: seeded uniform-phase IC (mt19937)",
+                "config": {"workload": workload_name(n), "lattice": n, "sample_lattice": args.cpu_n,
+                           "model": "abelian-higgs", "parallelism": "replicas"},
+                "cpu_baseline": {"value": r, "unit": "site-updates/s", "cores": cores, "kind": "port",
+                                 "sample": f"{args.cpu_n}^3 lattice of the same physics, {ns} steps"},
+                "e2e": {"value": r, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    # CPU baseline before the first CUDA call (rank 0, one GPU only)
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        r, cores, ns, el = cpu_rate(args.cpu_n, args.cpu_seconds)
+        cpu = {"value": r, "unit": "site-updates/s", "cores": cores, "kind": "port",
+               "sample": f"{args.cpu_n}^3 lattice of the same physics, {ns} steps in {el:.1f} s"}
+
+    import torch
+    torch.cuda.set_device(local)
+    dist_init(ws, "nccl")
+    dev = torch.device("cuda", local)
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    hbm = peaks.get("hbm_gbs")
+    peak_src = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+
+    res = measure_gpu(n, "f64", steps, warmup, ws, local, peaks)
+    t_max = dist_max(ws, res["total_ms"], dev)
+    units = dist_sum(ws, float(res["sites"]) * steps, dev)
+    e2e_max = dist_max(ws, res["e2e_ms"], dev)
+    fp32 = None
+    if not args.no_fp32:
+        r32 = measure_gpu(n, "f32", steps, warmup, ws, local, peaks)
+        t32 = dist_max(ws, r32["total_ms"], dev)
+        achieved32 = BYTES_PER_SITE["f32"] * r32["sites"] / (r32["kern_ms"] * 1e-3) / 1e9
+        fp32 = {"value": units / (t32 * 1e-3), "ms_per_step": t32 / steps, "dtype": "f32",
+                "kernel_ms": r32["kern_ms"],
+                "roofline": {"bound": "hbm", "achieved": achieved32, "peak": hbm, "unit": "GB/s",
+                             "frac": achieved32 / hbm, "traffic": load_traffic("f32", n)},
+                "speedup_vs_f64": res["total_ms"] / r32["total_ms"]}
+    if rank != 0:
+        return
+    achieved = BYTES_PER_SITE["f64"] * res["sites"] / (res["kern_ms"] * 1e-3) / 1e9
+    line = {
+        "metric": "site-updates/s", "value": units / (t_max * 1e-3), "unit": "site-updates/s", "n_gpus": ws,
+        "steps": steps, "warmup": warmup, "ms_per_step": t_max / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded uniform-phase IC (mt19937, mpi_evolution.cpp:287-312)",
+        "config": {"workload": workload_name(n), "model": "abelian-higgs", "lattice": n, "precision": "f64",
+                   "diag_every": DIAG_EVERY, "l2": f"inputs larger than L2 ({2 * 5 * 8 * n ** 3 / 1e9:.1f} GB state)",
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": load_traffic("f64", n), "peak_source": peak_src,
+                     "kernel": "ah_step_kernel<double>", "kernel_ms": res["kern_ms"],
+                     "bytes_per_site": BYTES_PER_SITE["f64"]},
+        "cpu_baseline": cpu,
+        "e2e": {"value": units / (e2e_max * 1e-3), "unit": "site-updates/s",
+                "h2d_bytes_per_step": res["e2e_h2d"], "d2h_bytes_per_step": res["e2e_d2h"]},
+        "gpu_launches": res["launches"],
+        "clocks": res["clocks"],
+        "fp32": fp32,
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -154,6 +154,9 @@ int lat_num_components(const lat_handle* h);
 int64_t lat_time_step(const lat_handle* h);
 /* bytes of device memory the handle holds */
 int64_t lat_device_bytes(const lat_handle* h);
+/* number of CUDA kernels this handle has launched so far (for benchmarks that
+ * report their launch count; no counterpart in the reference) */
+int64_t lat_kernel_launches(const lat_handle* h);
 
 /* Upload the state: `now` is the level at TimeStep `time_step`, `past` the one
  * before (for a stationary start pass the same array twice, as

@@ -109,3 +109,15 @@ def read_columns(path: Path):
     import numpy as np
     txt = path.read_text().split()
     return np.array([float(t) for t in txt], dtype=np.float64)
+
+
+def build_defaults() -> list[Path]:
+    """Build each reference program once with a small configuration (the build
+    check of __graft_entry__.build(); tests/golden/make_golden.py builds and runs
+    the configurations of the fixtures)."""
+    small = {"nx": 8, "ny": 8, "nz": 8, "nt": 2}
+    out = [build("mpi_evolution", "mpi_evolution_small", small),
+           build("moore_mpi_evolution", "moore_mpi_evolution_small", small),
+           build("evolution", "evolution_small", small),
+           build("mooreEvol", "mooreEvol_small", small)]
+    return out

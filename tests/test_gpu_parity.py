@@ -1,0 +1,227 @@
+"""GPU parity through the C ABI against the reference (golden fixtures) and the
+oracle (live, on the same seeded inputs).
+
+Tolerances (FP64 path):
+  * fields: normwise, max|d|/max|ref| <= 1e-12 and ||d||_2/||ref||_2 <= 1e-12.
+    The GPU's sin/cos differ from libm's in the last bit for some arguments, so
+    element-wise equality is not possible; normwise agreement is the bar.
+  * energy and summed Gauss deviation: relative 1e-12 (different summation
+    order on top of the above).
+  * string detection on identical fields: bit-exact (same double operations,
+    -fmad=false, IEEE sqrt and division on both sides).
+  * plaquette winding on identical fields: bit-exact.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, params_from_json
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def normwise(a, b):
+    d = np.abs(a - b)
+    return d.max() / np.abs(b).max(), np.linalg.norm(d) / np.linalg.norm(b)
+
+
+def assert_fields_close(a, b, tol=TOL):
+    mx, l2 = normwise(a, b)
+    assert mx <= tol and l2 <= tol, f"max {mx:.3e} l2 {l2:.3e}"
+
+
+@pytest.fixture(scope="module")
+def lattice_mod():
+    from axions_gb300 import lattice
+    lattice.load_library()
+    return lattice
+
+
+def _replay_mpi(lattice_mod, z, p, precision=0):
+    """The reference MPI loop body: detection (stringsExist latch) then a step
+    with energy, through the C ABI."""
+    p = p.copy()
+    p.precision = precision
+    lat = lattice_mod.Lattice(p)
+    ic = lattice_mod.random_phase_ic(p, int(z["seed"]))
+    lat.set_state(ic, ic, 0)
+    nt, sf = int(z["nt"]), int(z["save_freq"])
+    energies, frames, exist = [], [], True
+    for n in range(nt):
+        if n % sf == 0 and n >= p.damped_nt and exist:
+            xyz = lat.detect(0)
+            frames.append(xyz)
+            exist = len(xyz) > 0
+        energies.append(lat.step_diag().energy)
+    st = lat.get_slots()
+    lat.close()
+    return st, np.array(energies), frames
+
+
+@pytest.mark.parametrize("name", ["ref_mpi_ah_c1", "ref_mpi_ah_prs", "ref_mpi_ah_global", "ref_moore_mpi"])
+def test_mpi_programs_against_reference(lattice_mod, name):
+    z = load_golden(name)
+    p = params_from_json(z["params"])
+    st, energy, frames = _replay_mpi(lattice_mod, z, p)
+    assert_fields_close(st, z["final"])
+    ref_e = z["energy"]
+    if np.all(np.isnan(ref_e)):       # g = 0: the reference's MPI energy is 0/0
+        assert np.all(np.isnan(energy))
+    else:
+        np.testing.assert_allclose(energy, ref_e, rtol=TOL, atol=0)
+    assert [len(f) for f in frames] == z["frame_counts"].tolist()
+    np.testing.assert_allclose(np.concatenate(frames), z["frame_xyz"], rtol=0, atol=1e-9)
+
+
+@pytest.mark.parametrize("name", ["ref_evol_ah_periodic", "ref_evol_ah_fixed", "ref_moore_evol"])
+def test_openmp_programs_against_reference(lattice_mod, name):
+    z = load_golden(name)
+    p = params_from_json(z["params"])
+    lat = lattice_mod.Lattice(p)
+    lat.set_slots(z["ic"], 0)
+    nt = int(z["nt"])
+    out = lat.advance(nt, diag_every=1)
+    E = np.array([o[1] for o in out])
+    D = np.array([o[2] for o in out])
+    now, _ = lat.get_state()
+    assert_fields_close(now, z["final_newest"])
+    np.testing.assert_allclose(E, z["energy"], rtol=TOL, atol=0)
+    if p.model == 0:
+        c = p.nx * p.ny * p.nz if p.bc == 0 else (p.nx - 2) * (p.ny - 2) * (p.nz - 2)
+        np.testing.assert_allclose(D / c, z["deviation"], rtol=TOL, atol=0)
+    else:
+        c = (p.nx - 2) * (p.ny - 2) * (p.nz - 2)
+        np.testing.assert_allclose(D / c / c, z["deviation"], rtol=TOL, atol=0)
+    lat.close()
+
+
+def test_config1_physics_64cubed_300_steps(lattice_mod, oracle_mod):
+    """Config-1 physics (lambda=2, e=1, eta=1, dx=0.5, dt=0.1, Minkowski) on a
+    64^3 seeded random-phase lattice, 300 steps, energy/Gauss every 10 steps."""
+    from axions_gb300.params import ENERGY_EVOLUTION, make_params
+    p = make_params(0, n=64, d=0.5, dt=0.1, lam=2.0, eta=1.0, g=1.0, damped_nt=0, dampFac=0.0, alpha=0.0,
+                    energy_form=ENERGY_EVOLUTION)
+    st = oracle_mod.random_phase_ic(p, 42)
+    ref_diag = oracle_mod.evolve(p, st, 0, 300, diag_every=10)
+    lat = lattice_mod.Lattice(p)
+    lat.set_state(lattice_mod.random_phase_ic(p, 42), None, 0)
+    out = lat.advance(300, diag_every=10)
+    gpu = lat.get_slots()
+    assert_fields_close(gpu, st)
+    assert [o[0] for o in out] == [r[0] for r in ref_diag]
+    np.testing.assert_allclose([o[1] for o in out], [r[1] for r in ref_diag], rtol=TOL)
+    np.testing.assert_allclose([o[2] for o in out], [r[2] for r in ref_diag], rtol=1e-10)
+    lat.close()
+
+
+def test_prs_moore_48cubed(lattice_mod, oracle_mod):
+    """Moore model, charges 1 and 2, PRS friction, independent phases, 100 steps."""
+    from axions_gb300.params import MODEL_MOORE, make_params
+    p = make_params(MODEL_MOORE, nx=48, ny=40, nz=36, d=0.5, dt=0.1, lam=2.0, lambda2=2.0, lambda12=0.3,
+                    eta=1.0, eta2=1.0, q1=1.0, q2=2.0, g=1.0, damped_nt=20, dampFac=0.5, alpha=3.0)
+    st = oracle_mod.random_phase_ic(p, 7, independent=True)
+    ref = oracle_mod.evolve(p, st, 0, 100, diag_every=25)
+    lat = lattice_mod.Lattice(p)
+    lat.set_state(lattice_mod.random_phase_ic(p, 7, True), None, 0)
+    out = lat.advance(100, diag_every=25)
+    assert_fields_close(lat.get_slots(), st)
+    np.testing.assert_allclose([o[1] for o in out], [r[1] for r in ref], rtol=TOL)
+    for fld in (0, 1):   # fields agree to ~1e-13 here, so crossings agree to tolerance
+        got, ref = lat.detect(fld), oracle_mod.detect(p, st, 100, fld)
+        assert got.shape == ref.shape
+        np.testing.assert_allclose(got, ref, rtol=0, atol=1e-9)
+    lat.close()
+
+
+@pytest.mark.parametrize("model", [0, 1])
+def test_detection_bit_exact_on_identical_fields(lattice_mod, oracle_mod, model):
+    from axions_gb300.params import make_params
+    p = make_params(model, nx=40, ny=36, nz=32, d=0.5, dt=0.1, lam=2.0, g=1.0, damped_nt=0, alpha=0.0)
+    st = oracle_mod.random_phase_ic(p, 3, independent=True)
+    oracle_mod.evolve(p, st, 0, 20)
+    lat = lattice_mod.Lattice(p)
+    lat.set_slots(st, 20)
+    for fld in range(1 + model):
+        ref = oracle_mod.detect(p, st, 20, fld)
+        got = lat.detect(fld)
+        assert got.shape == ref.shape and len(ref) > 100
+        assert np.array_equal(got, ref)
+        w_ref, t_ref = oracle_mod.winding(p, st, 20, fld)
+        w_got, t_got = lat.winding(fld)
+        assert t_got == t_ref and np.array_equal(w_got, w_ref)
+    lat.close()
+
+
+def test_winding_conserved_through_every_cube(lattice_mod):
+    """Strings neither begin nor end: the outward windings of the six faces of
+    every cube sum to zero (exactly, as every edge enters two faces with
+    opposite orientation)."""
+    from axions_gb300.params import make_params
+    p = make_params(0, nx=24, ny=20, nz=16)
+    lat = lattice_mod.Lattice(p)
+    ic = lattice_mod.random_phase_ic(p, 11)
+    lat.set_state(ic, ic, 0)
+    w, tot = lat.winding(0)
+    assert tot > 0
+    W = w.reshape(3, p.nx, p.ny, p.nz).astype(np.int32)
+    div = (np.roll(W[0], -1, 0) - W[0]) + (np.roll(W[1], -1, 1) - W[1]) + (np.roll(W[2], -1, 2) - W[2])
+    assert np.all(div == 0)
+    assert tot == int(np.abs(W).sum())
+    lat.close()
+
+
+def test_diagnostics_read_only_and_consistent(lattice_mod, oracle_mod):
+    from axions_gb300.params import ENERGY_EVOLUTION, make_params
+    p = make_params(0, nx=20, ny=18, nz=16, d=0.5, dt=0.1, lam=2.0, g=1.0, damped_nt=0, alpha=3.0,
+                    energy_form=ENERGY_EVOLUTION)
+    st = oracle_mod.random_phase_ic(p, 5)
+    oracle_mod.evolve(p, st, 0, 7)
+    lat = lattice_mod.Lattice(p)
+    lat.set_slots(st, 7)
+    before = lat.get_slots()
+    d1 = lat.diagnostics()
+    assert np.array_equal(lat.get_slots(), before) and lat.time_step == 7
+    d2 = lat.step_diag()
+    ref = oracle_mod.diagnostics(p, st, 7)
+    assert d1.time_step == d2.time_step == 7
+    assert d1.energy == d2.energy and d1.gauss_abs_sum == d2.gauss_abs_sum
+    np.testing.assert_allclose([d1.energy, d1.gauss_abs_sum], [ref.energy, ref.gauss_abs_sum], rtol=1e-12)
+    lat.close()
+
+
+def test_capacity_error_keeps_count(lattice_mod):
+    import ctypes
+    from axions_gb300.params import LAT_ERR_CAPACITY, make_params
+    p = make_params(0, n=16)
+    lat = lattice_mod.Lattice(p)
+    ic = lattice_mod.random_phase_ic(p, 1)
+    lat.set_state(ic, ic, 0)
+    full = lat.detect(0)
+    buf = np.zeros((5, 3))
+    cnt = ctypes.c_int64(0)
+    rc = lat.L.lat_detect_crossings(lat.h, 0, buf.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 5,
+                                    ctypes.byref(cnt))
+    assert rc == LAT_ERR_CAPACITY and cnt.value == len(full)
+    assert np.array_equal(buf, full[:5])
+    lat.close()
+
+
+def test_fp32_path_tracks_fp64(lattice_mod):
+    """FP32 fields with FP64 reductions stay close to the FP64 path over a short run."""
+    from axions_gb300.params import ENERGY_EVOLUTION, F32, make_params
+    p = make_params(0, n=32, d=0.5, dt=0.1, lam=2.0, g=1.0, damped_nt=0, alpha=0.0, energy_form=ENERGY_EVOLUTION)
+    ic = lattice_mod.random_phase_ic(p, 9)
+    outs = []
+    for prec in (0, F32):
+        q = p.copy()
+        q.precision = prec
+        lat = lattice_mod.Lattice(q)
+        lat.set_state(ic, ic, 0)
+        outs.append((lat.advance(20, diag_every=5), lat.get_slots()))
+        lat.close()
+    (d64, s64), (d32, s32) = outs
+    mx, l2 = normwise(s32, s64)
+    assert l2 < 1e-4, l2
+    np.testing.assert_allclose([d[1] for d in d32], [d[1] for d in d64], rtol=1e-5)
+    np.testing.assert_allclose([d[2] for d in d32], [d[2] for d in d64], rtol=1e-3)
