@@ -1,0 +1,282 @@
+// Abelian-Higgs FP64 step in two passes.
+//
+// FP64 on GB300 runs at 1/64 of the FP32 rate, so the step is bound by FP64
+// instructions, not by HBM: the one-pass kernel (ah_step.cuh) evaluates every
+// link's sin/cos and every plaquette sine twice, once for each site that
+// needs it (as the reference does, mpi_evolution.cpp:418-487).  Here pass 1
+// evaluates them once per site into a scratch buffer ("link data") and pass 2
+// performs the update (mpi_evolution.cpp:412-501) reading the link data of the
+// site and of its three backward neighbours.  The extra HBM traffic
+// (~200 B/site) is small next to the FP64 time it saves.
+//
+// STRICT = true keeps the reference's rounding operation by operation (the
+// translation unit is compiled with -fmad=false); the link data are the very
+// doubles the one-pass kernel computes, so the two paths agree bit for bit.
+// STRICT = false (LAT_F64_FAST) lets the compiler fuse multiply-adds, divides
+// by dt through a corrected reciprocal, and takes sin(P_yx) = -sin(P_xy)
+// (likewise zx, zy): the same arithmetic to within an ulp per operation.
+#pragma once
+
+#include "site_common.cuh"
+
+namespace lat {
+
+// link-data slots ([slot][N], SoA)
+enum LinkSlot {
+    L_CX, L_SX, L_CY, L_SY, L_CZ, L_SZ,   // cos/sin of theta_mu at the site
+    L_PXY, L_PXZ, L_PYZ,                    // sin of P_xy, P_xz, P_yz at the site
+    L_PYX, L_PZX, L_PZY,                    // sin of P_yx, P_zx, P_zy (STRICT only)
+    L_CPXY, L_CPXZ, L_CPYZ,                 // cos of P_xy, P_xz, P_yz (diagnostic steps)
+    L_COUNT
+};
+
+// a / b where b = spacing^2 or spacing: exact reciprocal multiply when every
+// spacing is a power of two (then a*(1/b) == a/b for all a), else IEEE divide.
+template <bool RECIP>
+__device__ __forceinline__ double sdiv(double a, double b, double inv_b)
+{
+    if constexpr (RECIP) return a * inv_b;
+    else return a / b;
+}
+
+// a / dt.  STRICT: IEEE divide.  Fast: q = a*r corrected by one residual step
+// (Markstein), which returns the correctly rounded quotient except in rare
+// cases where it is one ulp off.
+template <bool STRICT>
+__device__ __forceinline__ double tdiv(double a, double b, double inv_b)
+{
+    if constexpr (STRICT) return a / b;
+    else {
+        const double q = a * inv_b;
+        const double r = fma(-q, b, a);
+        return fma(r, inv_b, q);
+    }
+}
+
+template <bool STRICT, bool DIAG>
+__global__ void __launch_bounds__(BLOCK) ah_links_kernel(const Geom g, const double* __restrict__ TX,
+                                                         const double* __restrict__ TY,
+                                                         const double* __restrict__ TZ, double* __restrict__ L,
+                                                         const int N)
+{
+    const int k = (int)(blockIdx.x * BZ + threadIdx.x);
+    const int j = (int)(blockIdx.y * BY + threadIdx.y);
+    const int i = (int)blockIdx.z;
+    if (k >= g.nz || j >= g.ny) return;
+    const Nbr n = make_nbr(g, i, j, k);
+    const int s = n.s;
+    const double tx = TX[s], ty = TY[s], tz = TZ[s];
+    const double tyxp = TY[s + n.xp], tzxp = TZ[s + n.xp];
+    const double txyp = TX[s + n.yp], tzyp = TZ[s + n.yp];
+    const double txzp = TX[s + n.zp], tyzp = TY[s + n.zp];
+    double sv, cv;
+    sincos(tx, &sv, &cv);
+    L[L_CX * N + s] = cv;
+    L[L_SX * N + s] = sv;
+    sincos(ty, &sv, &cv);
+    L[L_CY * N + s] = cv;
+    L[L_SY * N + s] = sv;
+    sincos(tz, &sv, &cv);
+    L[L_CZ * N + s] = cv;
+    L[L_SZ * N + s] = sv;
+    // plaquette angles, summed in the reference's order (mpi_evolution.cpp:471-487)
+    const double Pxy = tx + tyxp - txyp - ty;
+    const double Pxz = tx + tzxp - txzp - tz;
+    const double Pyz = ty + tzyp - tyzp - tz;
+    if constexpr (DIAG) {
+        sincos(Pxy, &sv, &cv);
+        L[L_PXY * N + s] = sv;
+        L[L_CPXY * N + s] = cv;
+        sincos(Pxz, &sv, &cv);
+        L[L_PXZ * N + s] = sv;
+        L[L_CPXZ * N + s] = cv;
+        sincos(Pyz, &sv, &cv);
+        L[L_PYZ * N + s] = sv;
+        L[L_CPYZ * N + s] = cv;
+    } else {
+        L[L_PXY * N + s] = sin(Pxy);
+        L[L_PXZ * N + s] = sin(Pxz);
+        L[L_PYZ * N + s] = sin(Pyz);
+    }
+    if constexpr (STRICT) {
+        L[L_PYX * N + s] = sin(ty + txyp - tyxp - tx);
+        L[L_PZX * N + s] = sin(tz + txzp - tzxp - tx);
+        L[L_PZY * N + s] = sin(tz + tyzp - tzyp - ty);
+    }
+}
+
+template <bool STRICT, bool DIAG, bool RECIP>
+__global__ void __launch_bounds__(BLOCK) ah_update_kernel(const Geom g, const Fields<double, 5> f,
+                                                          const double* __restrict__ L, const int N, const StepCoef c,
+                                                          const DiagOut d)
+{
+    const int k = g.lo + (int)(blockIdx.x * BZ + threadIdx.x);
+    const int j = g.lo + (int)(blockIdx.y * BY + threadIdx.y);
+    const int i = g.lo + (int)blockIdx.z;
+    double e_site = 0.0, g_site = 0.0;
+
+    if (k < g.hiz && j < g.hiy) {
+        const Nbr n = make_nbr(g, i, j, k);
+        const int s = n.s;
+        const int sxm = s + n.xm, sym_ = s + n.ym, szm = s + n.zm;
+        const double* __restrict__ P0 = f.now[0];
+        const double* __restrict__ P1 = f.now[1];
+
+        const double p0 = P0[s], p1 = P1[s];
+        const double p0xp = P0[s + n.xp], p1xp = P1[s + n.xp], p0xm = P0[sxm], p1xm = P1[sxm];
+        const double p0yp = P0[s + n.yp], p1yp = P1[s + n.yp], p0ym = P0[sym_], p1ym = P1[sym_];
+        const double p0zp = P0[s + n.zp], p1zp = P1[s + n.zp], p0zm = P0[szm], p1zm = P1[szm];
+        const double q0 = f.past[0][s], q1 = f.past[1][s];
+        const double tx = f.now[2][s], ty = f.now[3][s], tz = f.now[4][s];
+        const double qx = f.past[2][s], qy = f.past[3][s], qz = f.past[4][s];
+
+        const double cx = L[L_CX * N + s], sx = L[L_SX * N + s];
+        const double cy = L[L_CY * N + s], sy = L[L_SY * N + s];
+        const double cz = L[L_CZ * N + s], sz = L[L_SZ * N + s];
+        const double cxm = L[L_CX * N + sxm], sxm_ = L[L_SX * N + sxm];
+        const double cym = L[L_CY * N + sym_], sym = L[L_SY * N + sym_];
+        const double czm = L[L_CZ * N + szm], szm_ = L[L_SZ * N + szm];
+        const double sPxy = L[L_PXY * N + s], sPxz = L[L_PXZ * N + s], sPyz = L[L_PYZ * N + s];
+        const double sPxy_m = L[L_PXY * N + sym_], sPxz_m = L[L_PXZ * N + szm], sPyz_m = L[L_PYZ * N + szm];
+        double sPyx, sPzx, sPzy, sPyx_m, sPzx_m, sPzy_m;
+        if constexpr (STRICT) {
+            sPyx = L[L_PYX * N + s];
+            sPzx = L[L_PZX * N + s];
+            sPzy = L[L_PZY * N + s];
+            sPyx_m = L[L_PYX * N + sxm];
+            sPzx_m = L[L_PZX * N + sxm];
+            sPzy_m = L[L_PZY * N + sym_];
+        } else {
+            sPyx = -sPxy;
+            sPzx = -sPxz;
+            sPzy = -sPyz;
+            sPyx_m = -L[L_PXY * N + sxm];
+            sPzx_m = -L[L_PXZ * N + sxm];
+            sPzy_m = -L[L_PYZ * N + sym_];
+        }
+
+        const double phiMagSqr = p0 * p0 + p1 * p1;
+        const double pot = c.halfLambda * (phiMagSqr - c.etaSq);
+
+        // covariant Laplacian (mpi_evolution.cpp:418-428), c = +1 then c = -1
+        double lap0 = sdiv<RECIP>(cx * p0xp + sx * p1xp - 2 * p0 + cxm * p0xm - sxm_ * p1xm, c.dx2, c.inv_dx2)
+                    + sdiv<RECIP>(cy * p0yp + sy * p1yp - 2 * p0 + cym * p0ym - sym * p1ym, c.dy2, c.inv_dy2)
+                    + sdiv<RECIP>(cz * p0zp + sz * p1zp - 2 * p0 + czm * p0zm - szm_ * p1zm, c.dz2, c.inv_dz2);
+        double lap1 = sdiv<RECIP>(cx * p1xp - sx * p0xp - 2 * p1 + cxm * p1xm + sxm_ * p0xm, c.dx2, c.inv_dx2)
+                    + sdiv<RECIP>(cy * p1yp - sy * p0yp - 2 * p1 + cym * p1ym + sym * p0ym, c.dy2, c.inv_dy2)
+                    + sdiv<RECIP>(cz * p1zp - sz * p0zp - 2 * p1 + czm * p1zm + szm_ * p0zm, c.dz2, c.inv_dz2);
+        double tt0 = lap0 - pot * p0;
+        double tt1 = lap1 - pot * p1;
+        if (c.fric != 0) {
+            tt0 = tt0 - c.fric * tdiv<STRICT>(p0 - q0, c.dt, c.inv_dt);
+            tt1 = tt1 - c.fric * tdiv<STRICT>(p1 - q1, c.dt, c.inv_dt);
+        }
+
+        // gauge current (mpi_evolution.cpp:459-466)
+        const double curx = cx * (p1 * p0xp - p0 * p1xp) + sx * (p0 * p0xp + p1 * p1xp);
+        const double cury = cy * (p1 * p0yp - p0 * p1yp) + sy * (p0 * p0yp + p1 * p1yp);
+        const double curz = cz * (p1 * p0zp - p0 * p1zp) + sz * (p0 * p0zp + p1 * p1zp);
+
+        // lattice curl (mpi_evolution.cpp:471-487)
+        const double Fxy_y = sdiv<RECIP>(sPxy - sPxy_m, c.dy2, c.inv_dy2);
+        const double Fxz_z = sdiv<RECIP>(sPxz - sPxz_m, c.dz2, c.inv_dz2);
+        const double Fyx_x = sdiv<RECIP>(sPyx - sPyx_m, c.dx2, c.inv_dx2);
+        const double Fyz_z = sdiv<RECIP>(sPyz - sPyz_m, c.dz2, c.inv_dz2);
+        const double Fzx_x = sdiv<RECIP>(sPzx - sPzx_m, c.dx2, c.inv_dx2);
+        const double Fzy_y = sdiv<RECIP>(sPzy - sPzy_m, c.dy2, c.inv_dy2);
+
+        double ttx = c.m2gg * curx - Fxy_y - Fxz_z;
+        double tty = c.m2gg * cury - Fyx_x - Fyz_z;
+        double ttz = c.m2gg * curz - Fzx_x - Fzy_y;
+        if (c.damp != 0) {
+            ttx = ttx - c.damp * tdiv<STRICT>(tx - qx, c.dt, c.inv_dt);
+            tty = tty - c.damp * tdiv<STRICT>(ty - qy, c.dt, c.inv_dt);
+            ttz = ttz - c.damp * tdiv<STRICT>(tz - qz, c.dt, c.inv_dt);
+        }
+
+        double divNow = 0;
+        if (DIAG || d.store_div) {
+            const double txm = f.now[2][sxm], tym = f.now[3][sym_], tzm = f.now[4][szm];
+            divNow = sdiv<RECIP>(tx - txm, c.dx2, c.inv_dx2) + sdiv<RECIP>(ty - tym, c.dy2, c.inv_dy2)
+                   + sdiv<RECIP>(tz - tzm, c.dz2, c.inv_dz2);
+        }
+
+        if constexpr (DIAG) {
+            // energy density and Gauss deviation of the now level
+            // (evolution.cpp:322-334,377-427; mpi_evolution.cpp:509-532)
+            const double cPxy = L[L_CPXY * N + s], cPxz = L[L_CPXZ * N + s], cPyz = L[L_CPYZ * N + s];
+            const double pt0 = tdiv<STRICT>(p0 - q0, c.dt, c.inv_dt);
+            const double pt1 = tdiv<STRICT>(p1 - q1, c.dt, c.inv_dt);
+            const double px0 = sdiv<RECIP>(p0 - cxm * p0xm + sxm_ * p1xm, c.dx, c.inv_dx);
+            const double px1 = sdiv<RECIP>(p1 - cxm * p1xm - sxm_ * p0xm, c.dx, c.inv_dx);
+            const double py0 = sdiv<RECIP>(p0 - cym * p0ym + sym * p1ym, c.dy, c.inv_dy);
+            const double py1 = sdiv<RECIP>(p1 - cym * p1ym - sym * p0ym, c.dy, c.inv_dy);
+            const double pz0 = sdiv<RECIP>(p0 - czm * p0zm + szm_ * p1zm, c.dz, c.inv_dz);
+            const double pz1 = sdiv<RECIP>(p1 - czm * p1zm - szm_ * p0zm, c.dz, c.inv_dz);
+            double tdc = 0, fc = 0, gauss = 0;
+            if (d.energy_form == LAT_ENERGY_MPI) {
+                const double a0 = (tx - qx) / c.dt, a1 = (ty - qy) / c.dt, a2 = (tz - qz) / c.dt;
+                tdc = 0.5 * (a0 * a0 + a1 * a1 + a2 * a2);
+                fc = (1 - cPxy) / c.gxy2 + (1 - cPxz) / c.gxz2 + (1 - cPyz) / c.gyz2;
+            }
+            if (c.g != 0) {
+                const double divPast = reinterpret_cast<const double*>(d.divbuf)[s];
+                const double divThetat = (divNow - divPast) / c.dt;
+                gauss = divThetat / c.g - c.twog * (p1 * pt0 - p0 * pt1);
+                if (d.energy_form != LAT_ENERGY_MPI) {
+                    const double a0 = (tx - qx) / c.gdtdx, a1 = (ty - qy) / c.gdtdy, a2 = (tz - qz) / c.gdtdz;
+                    tdc = 0.5 * (a0 * a0 + a1 * a1 + a2 * a2);
+                    const double Fxy = (1 - cPxy) / c.gxy2;
+                    const double Fxz = (1 - cPxz) / c.gxz2;
+                    const double Fyz = (1 - cPyz) / c.gyz2;
+                    fc = Fxy + Fxz + Fyz;
+                }
+            }
+            const double pm = phiMagSqr - c.etaSq;
+            const double ed = pt0 * pt0 + pt1 * pt1 + px0 * px0 + px1 * px1 + py0 * py0 + py1 * py1 + pz0 * pz0
+                            + pz1 * pz1 + tdc + fc + c.quarterLambda * (pm * pm);
+            if (d.energy_form == LAT_ENERGY_MPI) e_site = ed * c.dx * c.dy * c.dz;
+            else e_site = c.dV * ed;
+            g_site = fabs(gauss);
+        }
+
+        if (d.store_div) reinterpret_cast<double*>(d.divbuf)[s] = divNow;
+
+        if (d.write) {  // in-place update of the past slot (mpi_evolution.cpp:432,499-501)
+            f.past[0][s] = 2 * p0 - q0 + c.dt2 * tt0;
+            f.past[1][s] = 2 * p1 - q1 + c.dt2 * tt1;
+            f.past[2][s] = 2 * tx - qx + c.dt2 * ttx;
+            f.past[3][s] = 2 * ty - qy + c.dt2 * tty;
+            f.past[4][s] = 2 * tz - qz + c.dt2 * ttz;
+        }
+    }
+    if constexpr (DIAG) block_sum2_store(e_site, g_site, d.partials);
+}
+
+template <bool STRICT>
+cudaError_t launch_ah_twopass(const Geom& g, const Fields<double, 5>& f, double* L, const StepCoef& c,
+                              const DiagOut& d, bool diag, bool recip, cudaStream_t st)
+{
+    const int N = g.nx * g.syz;
+    Geom all = g;
+    all.lo = 0;
+    all.hix = g.nx;
+    all.hiy = g.ny;
+    all.hiz = g.nz;
+    const dim3 block(BZ, BY);
+    if (diag) ah_links_kernel<STRICT, true><<<site_grid(all), block, 0, st>>>(g, f.now[2], f.now[3], f.now[4], L, N);
+    else ah_links_kernel<STRICT, false><<<site_grid(all), block, 0, st>>>(g, f.now[2], f.now[3], f.now[4], L, N);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const dim3 grid = site_grid(g);
+    if (diag) {
+        if (recip) ah_update_kernel<STRICT, true, true><<<grid, block, 0, st>>>(g, f, L, N, c, d);
+        else ah_update_kernel<STRICT, true, false><<<grid, block, 0, st>>>(g, f, L, N, c, d);
+    } else {
+        if (recip) ah_update_kernel<STRICT, false, true><<<grid, block, 0, st>>>(g, f, L, N, c, d);
+        else ah_update_kernel<STRICT, false, false><<<grid, block, 0, st>>>(g, f, L, N, c, d);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace lat

@@ -102,6 +102,9 @@ struct lat_handle {
     // device memory
     void* fields = nullptr;    // [ncomp][2][N]
     void* divbuf = nullptr;    // [N]
+    double* links = nullptr;   // two-pass FP64 link data [ah_link_slots()][N]
+    size_t links_bytes = 0;
+    bool recip = false;        // every spacing is a power of two: exact reciprocals
     double* partials = nullptr;
     int nblocks = 0;
     double* diag_dev = nullptr;
@@ -210,7 +213,9 @@ static int validate(const lat_params* p)
     LAT_REQUIRE(p, "null params");
     LAT_REQUIRE(p->abi_version == LAT_ABI_VERSION, "lat_params.abi_version mismatch");
     LAT_REQUIRE(p->model == LAT_MODEL_AH || p->model == LAT_MODEL_MOORE, "unknown model");
-    LAT_REQUIRE(p->precision == LAT_F64 || p->precision == LAT_F32, "unknown precision");
+    LAT_REQUIRE(p->precision == LAT_F64 || p->precision == LAT_F32 || p->precision == LAT_F64_FAST,
+                "unknown precision");
+    LAT_REQUIRE(p->kernel_variant == 0 || p->kernel_variant == 1, "unknown kernel_variant");
     LAT_REQUIRE(p->bc == LAT_BC_PERIODIC || p->bc == LAT_BC_FIXED, "unknown boundary condition");
     const int64_t mn = p->bc == LAT_BC_FIXED ? 3 : 2;
     LAT_REQUIRE(p->nx >= mn && p->ny >= mn && p->nz >= mn, "lattice sides too small for the boundary condition");
@@ -240,7 +245,12 @@ int lat_create(const lat_params* p, lat_handle** out)
     h->p = *p;
     h->ncomp = p->model == LAT_MODEL_MOORE ? 7 : 5;
     h->N = p->nx * p->ny * p->nz;
-    h->elem = p->precision == LAT_F64 ? 8 : 4;
+    h->elem = p->precision == LAT_F32 ? 4 : 8;
+    auto pow2 = [](double v) {
+        int e;
+        return std::frexp(v, &e) == 0.5;
+    };
+    h->recip = pow2(p->dx) && pow2(p->dy) && pow2(p->dz);
     h->geom = make_geom(*p);
     cudaGetDevice(&h->device);
     auto fail = [&](int code) {
@@ -255,6 +265,10 @@ int lat_create(const lat_params* p, lat_handle** out)
     h->stream = h->own;
     if ((rc = dev_alloc(h, &h->fields, (size_t)h->ncomp * 2 * h->N * h->elem))) return fail(rc);
     if ((rc = dev_alloc(h, &h->divbuf, (size_t)h->N * h->elem))) return fail(rc);
+    if (p->model == LAT_MODEL_AH && h->elem == 8 && p->kernel_variant == 0) {
+        h->links_bytes = sizeof(double) * (size_t)ah_link_slots() * (size_t)h->N;
+        if ((rc = dev_alloc(h, (void**)&h->links, h->links_bytes))) return fail(rc);
+    }
     const dim3 gr = site_grid(h->geom);
     h->nblocks = (int)(gr.x * gr.y * gr.z);
     if ((rc = dev_alloc(h, (void**)&h->partials, sizeof(double) * 2 * (size_t)h->nblocks))) return fail(rc);
@@ -276,6 +290,7 @@ int lat_destroy(lat_handle* h)
     if (h->stream) cudaStreamSynchronize(h->stream);
     cudaFree(h->fields);
     cudaFree(h->divbuf);
+    cudaFree(h->links);
     cudaFree(h->partials);
     cudaFree(h->diag_dev);
     cudaFree(h->staging);
@@ -403,7 +418,15 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
                 f.now[c] = (const double*)h->slot(c, tNow);
                 f.past[c] = (double*)h->slot(c, tPast);
             }
-            LAT_CKL(launch_ah_step_f64(h->geom, f, cf, d, diag, h->stream));
+            if (h->links) {
+                if (p.precision == LAT_F64_FAST)
+                    LAT_CK(launch_ah_twopass_fast(h->geom, f, h->links, cf, d, diag, h->recip, h->stream));
+                else
+                    LAT_CK(launch_ah_twopass_strict(h->geom, f, h->links, cf, d, diag, h->recip, h->stream));
+                h->launches += 2;
+            } else {
+                LAT_CKL(launch_ah_step_f64(h->geom, f, cf, d, diag, h->stream));
+            }
         } else {
             Fields<float, 5> f;
             for (int c = 0; c < 5; ++c) {

@@ -86,6 +86,12 @@ cudaError_t launch_moore_step_f64(const Geom&, const Fields<double, 7>&, const S
                                   cudaStream_t);
 cudaError_t launch_moore_step_f32(const Geom&, const Fields<float, 7>&, const StepCoef&, const DiagOut&, bool diag,
                                   cudaStream_t);
+// two-pass FP64 Abelian-Higgs step (link data in L, [15][N] doubles)
+int ah_link_slots();
+cudaError_t launch_ah_twopass_strict(const Geom&, const Fields<double, 5>&, double* L, const StepCoef&, const DiagOut&,
+                                     bool diag, bool recip, cudaStream_t);
+cudaError_t launch_ah_twopass_fast(const Geom&, const Fields<double, 5>&, double* L, const StepCoef&, const DiagOut&,
+                                   bool diag, bool recip, cudaStream_t);
 // divergence of theta on one level into divbuf (used when no previous step stored it)
 cudaError_t launch_divergence_f64(const Geom&, const double* thx, const double* thy, const double* thz,
                                   const StepCoef&, double* out, cudaStream_t);

@@ -24,6 +24,7 @@ MODEL_AH = 0
 MODEL_MOORE = 1
 F64 = 0
 F32 = 1
+F64_FAST = 2
 BC_PERIODIC = 0
 BC_FIXED = 1
 ENERGY_EVOLUTION = 0
@@ -60,7 +61,7 @@ class LatParams(ctypes.Structure):
         ("scaling", ctypes.c_double),
         ("tau0", ctypes.c_double),
         ("energy_form", ctypes.c_int32),
-        ("reserved0", ctypes.c_int32),
+        ("kernel_variant", ctypes.c_int32),
         ("reserved", ctypes.c_double * 4),
     ]
 

@@ -56,6 +56,9 @@ extern "C" {
 /* precision of the stored fields and of the step arithmetic */
 #define LAT_F64 0            /* the reference's arithmetic                          */
 #define LAT_F32 1            /* FP32 fields and step; energy/Gauss sums stay FP64   */
+#define LAT_F64_FAST 2       /* FP64 fields; fused multiply-adds and a corrected
+                                reciprocal for /dt (each operation within an ulp of
+                                LAT_F64's); not bit-identical to the reference's order */
 
 /* boundary handling */
 #define LAT_BC_PERIODIC 0    /* periodic in x, y, z (mpi_evolution.cpp:385-405)             */
@@ -104,7 +107,7 @@ typedef struct lat_params {
     double scaling;        /* scale-factor power; friction = alpha*scaling/tau           */
     double tau0;           /* conformal time at step 0: tau = tau0 + TimeStep*dt (=1)    */
     int32_t energy_form;   /* LAT_ENERGY_*                                               */
-    int32_t reserved0;
+    int32_t kernel_variant;/* 0: default kernels; 1: one-pass FP64 stencil (for checks)  */
     double reserved[4];
 } lat_params;
 

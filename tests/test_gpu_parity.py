@@ -127,10 +127,11 @@ def test_prs_moore_48cubed(lattice_mod, oracle_mod):
     out = lat.advance(100, diag_every=25)
     assert_fields_close(lat.get_slots(), st)
     np.testing.assert_allclose([o[1] for o in out], [r[1] for r in ref], rtol=TOL)
-    for fld in (0, 1):   # fields agree to ~1e-13 here, so crossings agree to tolerance
+    for fld in (0, 1):   # fields agree to ~1e-13 here; a root of the bilinear
+        # quadratic amplifies that near double roots, so crossings agree to 1e-6
         got, ref = lat.detect(fld), oracle_mod.detect(p, st, 100, fld)
         assert got.shape == ref.shape
-        np.testing.assert_allclose(got, ref, rtol=0, atol=1e-9)
+        np.testing.assert_allclose(got, ref, rtol=0, atol=1e-6)
     lat.close()
 
 
@@ -225,3 +226,58 @@ def test_fp32_path_tracks_fp64(lattice_mod):
     assert l2 < 1e-4, l2
     np.testing.assert_allclose([d[1] for d in d32], [d[1] for d in d64], rtol=1e-5)
     np.testing.assert_allclose([d[2] for d in d32], [d[2] for d in d64], rtol=1e-3)
+
+
+def test_twopass_strict_bitwise_equals_onepass(lattice_mod):
+    """The two-pass FP64 step computes each link's sin/cos and plaquette sine
+    once per site; in strict mode it must give the very same doubles as the
+    one-pass kernel that evaluates them per use (as the reference does)."""
+    from axions_gb300.params import ENERGY_EVOLUTION, make_params
+    p = make_params(0, nx=30, ny=26, nz=22, d=0.5, dt=0.1, lam=2.0, g=1.0, damped_nt=5, dampFac=0.5, alpha=3.0,
+                    energy_form=ENERGY_EVOLUTION)
+    ic = lattice_mod.random_phase_ic(p, 17)
+    res = []
+    for variant in (0, 1):
+        q = p.copy()
+        q.kernel_variant = variant
+        lat = lattice_mod.Lattice(q)
+        lat.set_state(ic, ic, 0)
+        d = lat.advance(30, diag_every=3)
+        res.append((lat.get_slots(), d))
+        lat.close()
+    assert np.array_equal(res[0][0], res[1][0])
+    assert res[0][1] == res[1][1]
+
+
+@pytest.mark.parametrize("d", [0.5, 0.35])
+def test_fp64_fast_meets_parity_bar(lattice_mod, oracle_mod, d):
+    """LAT_F64_FAST (fused multiply-adds) against the oracle: 48^3, 300 steps,
+    config-1 physics; also a spacing that is not a power of two."""
+    from axions_gb300.params import ENERGY_EVOLUTION, F64_FAST, make_params
+    p = make_params(0, n=48, d=d, dt=0.1, lam=2.0, eta=1.0, g=1.0, damped_nt=0, alpha=0.0,
+                    energy_form=ENERGY_EVOLUTION)
+    st = oracle_mod.random_phase_ic(p, 4)
+    ref = oracle_mod.evolve(p, st, 0, 300, diag_every=50)
+    q = p.copy()
+    q.precision = F64_FAST
+    lat = lattice_mod.Lattice(q)
+    lat.set_state(lattice_mod.random_phase_ic(p, 4), None, 0)
+    out = lat.advance(300, diag_every=50)
+    assert_fields_close(lat.get_slots(), st)
+    np.testing.assert_allclose([o[1] for o in out], [r[1] for r in ref], rtol=TOL)
+    lat.close()
+
+
+def test_strict_non_power_of_two_spacing(lattice_mod, oracle_mod):
+    from axions_gb300.params import ENERGY_EVOLUTION, make_params
+    p = make_params(0, nx=36, ny=32, nz=28, d=0.35, dt=0.05, lam=1.0, eta=1.0, g=0.8, damped_nt=10, dampFac=0.5,
+                    alpha=3.0, energy_form=ENERGY_EVOLUTION)
+    st = oracle_mod.random_phase_ic(p, 8)
+    ref = oracle_mod.evolve(p, st, 0, 60, diag_every=20)
+    lat = lattice_mod.Lattice(p)
+    lat.set_state(lattice_mod.random_phase_ic(p, 8), None, 0)
+    out = lat.advance(60, diag_every=20)
+    assert_fields_close(lat.get_slots(), st)
+    np.testing.assert_allclose([o[1] for o in out], [r[1] for r in ref], rtol=TOL)
+    np.testing.assert_allclose([o[2] for o in out], [r[2] for r in ref], rtol=1e-10)
+    lat.close()
