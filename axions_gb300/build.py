@@ -32,6 +32,7 @@ UNITS = {
     "ah_f64.cu": ["-fmad=false"],
     "moore_f64.cu": ["-fmad=false"],
     "detect.cu": ["-fmad=false"],
+    "noalloc.cu": ["-fmad=false"],
     "ah_f64_fast.cu": [],
     "ah_f32.cu": [],
     "moore_f32.cu": [],

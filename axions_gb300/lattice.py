@@ -27,7 +27,7 @@ EXPORTS = [
     "lat_set_stream", "lat_get_params", "lat_num_components", "lat_time_step", "lat_device_bytes",
     "lat_kernel_launches",
     "lat_set_state", "lat_get_state", "lat_step", "lat_step_diag", "lat_advance", "lat_diagnostics",
-    "lat_detect_crossings", "lat_winding",
+    "lat_detect_crossings", "lat_winding", "lat_ah_step_f64_noalloc",
 ]
 
 
@@ -81,6 +81,7 @@ def load_library(path: Path | None = None):
     L.lat_diagnostics.argtypes = [vp, P(LatDiag)]
     L.lat_detect_crossings.argtypes = [vp, ctypes.c_int32, dp, ctypes.c_int64, P(ctypes.c_int64)]
     L.lat_winding.argtypes = [vp, ctypes.c_int32, P(ctypes.c_int8), P(ctypes.c_int64)]
+    L.lat_ah_step_f64_noalloc.argtypes = [P(LatParams), vp, ctypes.c_int64, ctypes.c_int32, vp]
     if path is None:
         _lib = L
     return L

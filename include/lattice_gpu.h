@@ -216,6 +216,32 @@ int lat_detect_crossings(lat_handle* h, int32_t field, double* xyz, int64_t cap,
  * the lattice are 0. */
 int lat_winding(lat_handle* h, int32_t field, int8_t* out, int64_t* abs_sum);
 
+/* ---- stepping without allocation ---------------------------------------------- */
+/* Largest lattice (sites) lat_ah_step_f64_noalloc accepts: 64^3. */
+#define LAT_NOALLOC_MAX_SITES 262144
+
+/* Advance `nsteps` Abelian-Higgs steps (strict FP64, the same kernels and
+ * results as lat_step on a LAT_F64 handle) on fields the caller owns, without
+ * allocating any device memory.  No counterpart in the reference: it exists for
+ * callers that cannot let a library allocate, e.g. a host application that
+ * owns all device memory through its own pool or a fixed budget, or a tight
+ * stepping loop that cannot afford cudaMalloc's synchronisation of the device.
+ *   fields     device pointer, [5 components][2 slots][nx*ny*nz] doubles in the
+ *              reference's slot layout (slot (n+1)%2 holds level n, slot n%2
+ *              level n-1; mpi_evolution.cpp:62,370-371); updated in place.
+ *   time_step  the TimeStep of the first step (its now level).
+ *   stream     cudaStream_t to launch on (NULL: the default stream).  The call
+ *              only enqueues work; synchronise the stream before reading.
+ * The step's per-site scratch (link data) lives in a fixed array inside the
+ * library, LAT_NOALLOC_MAX_SITES*15 doubles (31.5 MiB), held by every GPU that
+ * loads the library until the process exits.  Larger lattices are rejected
+ * with LAT_ERR_INVALID.  The first call on a device looks up that array's
+ * device address (make it before any stream capture).  All calls on a device
+ * share the array, so calls whose work overlaps on the GPU (different streams,
+ * threads or processes sharing the context) race; serialise them. */
+int lat_ah_step_f64_noalloc(const lat_params* p, double* fields, int64_t time_step, int32_t nsteps,
+                            void* stream);
+
 #ifdef __cplusplus
 }
 #endif
