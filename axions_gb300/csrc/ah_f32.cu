@@ -1,5 +1,6 @@
 // Abelian-Higgs step kernels, float instantiation.
 #include "ah_step.cuh"
+#include "ah_tiled.cuh"
 
 namespace lat {
 
@@ -7,6 +8,12 @@ cudaError_t launch_ah_step_f32(const Geom& g, const Fields<float, 5>& f, const S
                                cudaStream_t st)
 {
     return launch_ah_step_t<float>(g, f, c, d, diag, st);
+}
+
+cudaError_t launch_ah_tiled_f32(const Geom& g, const Fields<float, 5>& f, const StepCoef& c, const DiagOut& d,
+                                bool diag, int chunk, cudaStream_t st)
+{
+    return launch_ah_tiled_t<float>(g, f, c, d, diag, chunk, st);
 }
 
 cudaError_t launch_divergence_f32(const Geom& g, const float* tx, const float* ty, const float* tz, const StepCoef& c,

@@ -15,7 +15,7 @@
 namespace lat {
 
 template <class T, bool DIAG>
-__global__ void __launch_bounds__(BLOCK) ah_step_kernel(const Geom g, const Fields<T, 5> f, const StepCoef c,
+__global__ void __launch_bounds__(BLOCK) ah_step_kernel(const Geom g, const Fields<T, 5> f, const StepCoefT<T> c,
                                                         const DiagOut d)
 {
     using TR = Trig<T>;
@@ -147,21 +147,21 @@ __global__ void __launch_bounds__(BLOCK) ah_step_kernel(const Geom g, const Fiel
                 const T a1 = qdiv<T>(ty - qy, c.dt, c.inv_dt);
                 const T a2 = qdiv<T>(tz - qz, c.dt, c.inv_dt);
                 tdc = (T)0.5 * (a0 * a0 + a1 * a1 + a2 * a2);
-                fc = qdiv<T>(1 - cPxy, c.gxy2, 1.0 / c.gxy2) + qdiv<T>(1 - cPxz, c.gxz2, 1.0 / c.gxz2)
-                   + qdiv<T>(1 - cPyz, c.gyz2, 1.0 / c.gyz2);
+                fc = qdiv<T>(1 - cPxy, c.gxy2, c.inv_gxy2) + qdiv<T>(1 - cPxz, c.gxz2, c.inv_gxz2)
+                   + qdiv<T>(1 - cPyz, c.gyz2, c.inv_gyz2);
             }
             if (c.g != 0) {
                 const T divPast = reinterpret_cast<const T*>(d.divbuf)[s];
                 const T divThetat = qdiv<T>(divNow - divPast, c.dt, c.inv_dt);
                 gauss = qdiv<T>(divThetat, c.g, c.inv_g) - (T)c.twog * (p1 * pt0 - p0 * pt1);
                 if (d.energy_form != LAT_ENERGY_MPI) {
-                    const T a0 = qdiv<T>(tx - qx, c.gdtdx, 1.0 / c.gdtdx);
-                    const T a1 = qdiv<T>(ty - qy, c.gdtdy, 1.0 / c.gdtdy);
-                    const T a2 = qdiv<T>(tz - qz, c.gdtdz, 1.0 / c.gdtdz);
+                    const T a0 = qdiv<T>(tx - qx, c.gdtdx, c.inv_gdtdx);
+                    const T a1 = qdiv<T>(ty - qy, c.gdtdy, c.inv_gdtdy);
+                    const T a2 = qdiv<T>(tz - qz, c.gdtdz, c.inv_gdtdz);
                     tdc = (T)0.5 * (a0 * a0 + a1 * a1 + a2 * a2);
-                    const T Fxy = qdiv<T>(1 - cPxy, c.gxy2, 1.0 / c.gxy2);
-                    const T Fxz = qdiv<T>(1 - cPxz, c.gxz2, 1.0 / c.gxz2);
-                    const T Fyz = qdiv<T>(1 - cPyz, c.gyz2, 1.0 / c.gyz2);
+                    const T Fxy = qdiv<T>(1 - cPxy, c.gxy2, c.inv_gxy2);
+                    const T Fxz = qdiv<T>(1 - cPxz, c.gxz2, c.inv_gxz2);
+                    const T Fyz = qdiv<T>(1 - cPyz, c.gyz2, c.inv_gyz2);
                     fc = Fxy + Fxz + Fyz;
                 }
             }
@@ -189,9 +189,10 @@ __global__ void __launch_bounds__(BLOCK) ah_step_kernel(const Geom g, const Fiel
 }
 
 template <class T>
-cudaError_t launch_ah_step_t(const Geom& g, const Fields<T, 5>& f, const StepCoef& c, const DiagOut& d, bool diag,
+cudaError_t launch_ah_step_t(const Geom& g, const Fields<T, 5>& f, const StepCoef& c64, const DiagOut& d, bool diag,
                              cudaStream_t st)
 {
+    const StepCoefT<T> c = coef_as<T>(c64);
     const dim3 grid = site_grid(g);
     const dim3 block(BZ, BY);
     if (diag) ah_step_kernel<T, true><<<grid, block, 0, st>>>(g, f, c, d);
@@ -204,7 +205,7 @@ cudaError_t launch_ah_step_t(const Geom& g, const Fields<T, 5>& f, const StepCoe
 template <class T>
 __global__ void __launch_bounds__(BLOCK) divergence_kernel(const Geom g, const T* __restrict__ TX,
                                                            const T* __restrict__ TY, const T* __restrict__ TZ,
-                                                           const StepCoef c, T* __restrict__ out)
+                                                           const StepCoefT<T> c, T* __restrict__ out)
 {
     const int k = g.lo + (int)(blockIdx.x * BZ + threadIdx.x);
     const int j = g.lo + (int)(blockIdx.y * BY + threadIdx.y);
@@ -220,7 +221,7 @@ template <class T>
 cudaError_t launch_divergence_t(const Geom& g, const T* tx, const T* ty, const T* tz, const StepCoef& c, T* out,
                                 cudaStream_t st)
 {
-    divergence_kernel<T><<<site_grid(g), dim3(BZ, BY), 0, st>>>(g, tx, ty, tz, c, out);
+    divergence_kernel<T><<<site_grid(g), dim3(BZ, BY), 0, st>>>(g, tx, ty, tz, coef_as<T>(c), out);
     return cudaGetLastError();
 }
 

@@ -81,6 +81,12 @@ StepCoef make_coef(const lat_params& p, int64_t n)
     c.inv_dy = 1.0 / p.dy;
     c.inv_dz = 1.0 / p.dz;
     c.inv_g = p.g != 0 ? 1.0 / p.g : 0.0;
+    c.inv_gdtdx = c.gdtdx != 0 ? 1.0 / c.gdtdx : 0.0;
+    c.inv_gdtdy = c.gdtdy != 0 ? 1.0 / c.gdtdy : 0.0;
+    c.inv_gdtdz = c.gdtdz != 0 ? 1.0 / c.gdtdz : 0.0;
+    c.inv_gxy2 = c.gxy2 != 0 ? 1.0 / c.gxy2 : 0.0;
+    c.inv_gxz2 = c.gxz2 != 0 ? 1.0 / c.gxz2 : 0.0;
+    c.inv_gyz2 = c.gyz2 != 0 ? 1.0 / c.gyz2 : 0.0;
     return c;
 }
 
@@ -105,6 +111,7 @@ struct lat_handle {
     double* links = nullptr;   // two-pass FP64 link data [ah_link_slots()][N]
     size_t links_bytes = 0;
     bool recip = false;        // every spacing is a power of two: exact reciprocals
+    int chunk = 32;            // x-planes per CTA of the tiled FP32 kernel
     double* partials = nullptr;
     int nblocks = 0;
     double* diag_dev = nullptr;
@@ -433,7 +440,8 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
                 f.now[c] = (const float*)h->slot(c, tNow);
                 f.past[c] = (float*)h->slot(c, tPast);
             }
-            LAT_CKL(launch_ah_step_f32(h->geom, f, cf, d, diag, h->stream));
+            if (p.kernel_variant == 0) LAT_CKL(launch_ah_tiled_f32(h->geom, f, cf, d, diag, h->chunk, h->stream));
+            else LAT_CKL(launch_ah_step_f32(h->geom, f, cf, d, diag, h->stream));
         }
     } else {
         if (h->elem == 8) {

@@ -36,26 +36,44 @@ inline dim3 site_grid(const Geom& g)
 // per-step coefficients.  Each is the exact double the reference evaluates
 // (same operands, same order), so an FP64 kernel reproduces its arithmetic.
 // ---------------------------------------------------------------------------
-struct StepCoef {
-    double dx2, dy2, dz2;        // dx*dx ...
-    double dt, dt2;              // dt, dt*dt
-    double halfLambda, etaSq;    // 0.5*lambda, eta*eta        (AH; Moore phi1)
-    double halfLambda2, eta2Sq;  // 0.5*lambda2, eta2*eta2     (Moore phi2)
-    double halfLambda12;         // 0.5*lambda12               (Moore)
-    double m2gg;                 // (-2*g)*g
-    double fric;                 // damp + alpha*scaling/tau
-    double damp;                 // dampFac or 0
-    double q1, q2;               // Moore charges
-    // diagnostics
-    double dx, dy, dz, g;
-    double gdtdx, gdtdy, gdtdz;  // (g*dt)*dmu
-    double gxy2, gxz2, gyz2;     // ((g*dx)*dy)^2 ...
-    double dV;                   // (dx*dy)*dz
-    double quarterLambda, quarterLambda2, halfLambda12e;  // 0.25*lambda, 0.25*lambda2, 0.5*lambda12
-    double twog;                 // 2*g
-    // reciprocals for the FP32 path
-    double inv_dx2, inv_dy2, inv_dz2, inv_dt, inv_dx, inv_dy, inv_dz, inv_g;
+// Field list of the step coefficients (X-macro), so that the FP32 kernels get
+// native-float copies instead of converting doubles at every use.
+#define LAT_COEF_FIELDS(X)                                                   \
+    X(dx2) X(dy2) X(dz2)                 /* dx*dx ...                      */ \
+    X(dt) X(dt2)                         /* dt, dt*dt                      */ \
+    X(halfLambda) X(etaSq)               /* 0.5*lambda, eta*eta            */ \
+    X(halfLambda2) X(eta2Sq)             /* 0.5*lambda2, eta2*eta2 (Moore) */ \
+    X(halfLambda12)                      /* 0.5*lambda12 (Moore)           */ \
+    X(m2gg)                              /* (-2*g)*g                       */ \
+    X(fric)                              /* damp + alpha*scaling/tau       */ \
+    X(damp)                              /* dampFac or 0                   */ \
+    X(q1) X(q2)                          /* Moore charges                  */ \
+    X(dx) X(dy) X(dz) X(g)                                                    \
+    X(gdtdx) X(gdtdy) X(gdtdz)           /* (g*dt)*dmu                     */ \
+    X(gxy2) X(gxz2) X(gyz2)              /* ((g*dx)*dy)^2 ...              */ \
+    X(dV)                                /* (dx*dy)*dz                     */ \
+    X(quarterLambda) X(quarterLambda2) X(halfLambda12e)                       \
+    X(twog)                              /* 2*g                            */ \
+    X(inv_dx2) X(inv_dy2) X(inv_dz2) X(inv_dt) X(inv_dx) X(inv_dy) X(inv_dz) X(inv_g) \
+    X(inv_gdtdx) X(inv_gdtdy) X(inv_gdtdz) X(inv_gxy2) X(inv_gxz2) X(inv_gyz2)
+
+template <class R>
+struct StepCoefT {
+#define LAT_COEF_DECL(name) R name;
+    LAT_COEF_FIELDS(LAT_COEF_DECL)
+#undef LAT_COEF_DECL
 };
+using StepCoef = StepCoefT<double>;
+
+template <class R>
+inline StepCoefT<R> coef_as(const StepCoef& c)
+{
+    StepCoefT<R> o;
+#define LAT_COEF_CAST(name) o.name = (R)c.name;
+    LAT_COEF_FIELDS(LAT_COEF_CAST)
+#undef LAT_COEF_CAST
+    return o;
+}
 
 StepCoef make_coef(const lat_params& p, int64_t n);
 Geom make_geom(const lat_params& p);
@@ -92,6 +110,9 @@ cudaError_t launch_ah_twopass_strict(const Geom&, const Fields<double, 5>&, doub
                                      bool diag, bool recip, cudaStream_t);
 cudaError_t launch_ah_twopass_fast(const Geom&, const Fields<double, 5>&, double* L, const StepCoef&, const DiagOut&,
                                    bool diag, bool recip, cudaStream_t);
+// tiled, x-marching FP32 Abelian-Higgs step; `chunk` x-planes per CTA
+cudaError_t launch_ah_tiled_f32(const Geom&, const Fields<float, 5>&, const StepCoef&, const DiagOut&, bool diag,
+                                int chunk, cudaStream_t);
 // divergence of theta on one level into divbuf (used when no previous step stored it)
 cudaError_t launch_divergence_f64(const Geom&, const double* thx, const double* thy, const double* thz,
                                   const StepCoef&, double* out, cudaStream_t);

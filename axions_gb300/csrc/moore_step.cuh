@@ -13,7 +13,7 @@
 namespace lat {
 
 template <class T, bool DIAG>
-__global__ void __launch_bounds__(BLOCK) moore_step_kernel(const Geom g, const Fields<T, 7> f, const StepCoef c,
+__global__ void __launch_bounds__(BLOCK) moore_step_kernel(const Geom g, const Fields<T, 7> f, const StepCoefT<T> c,
                                                            const DiagOut d)
 {
     using TR = Trig<T>;
@@ -27,10 +27,10 @@ __global__ void __launch_bounds__(BLOCK) moore_step_kernel(const Geom g, const F
         const int s = n.s;
         const int pp[3] = {n.xp, n.yp, n.zp};
         const int mm[3] = {n.xm, n.ym, n.zm};
-        const double d2[3] = {c.dx2, c.dy2, c.dz2};
-        const double id2[3] = {c.inv_dx2, c.inv_dy2, c.inv_dz2};
-        const double dd[3] = {c.dx, c.dy, c.dz};
-        const double idd[3] = {c.inv_dx, c.inv_dy, c.inv_dz};
+        const T d2[3] = {c.dx2, c.dy2, c.dz2};
+        const T id2[3] = {c.inv_dx2, c.inv_dy2, c.inv_dz2};
+        const T dd[3] = {c.dx, c.dy, c.dz};
+        const T idd[3] = {c.inv_dx, c.inv_dy, c.inv_dz};
         const T q[2] = {(T)c.q1, (T)c.q2};
         const T dt2 = (T)c.dt2;
         const T* __restrict__ TH[3] = {f.now[4], f.now[5], f.now[6]};
@@ -183,8 +183,8 @@ __global__ void __launch_bounds__(BLOCK) moore_step_kernel(const Geom g, const F
                 const T a1 = qdiv<T>(ty - qth[1], c.dt, c.inv_dt);
                 const T a2 = qdiv<T>(tz - qth[2], c.dt, c.inv_dt);
                 tdc = (T)0.5 * (a0 * a0 + a1 * a1 + a2 * a2);
-                fc = qdiv<T>(1 - cPxy, c.gxy2, 1.0 / c.gxy2) + qdiv<T>(1 - cPxz, c.gxz2, 1.0 / c.gxz2)
-                   + qdiv<T>(1 - cPyz, c.gyz2, 1.0 / c.gyz2);
+                fc = qdiv<T>(1 - cPxy, c.gxy2, c.inv_gxy2) + qdiv<T>(1 - cPxz, c.gxz2, c.inv_gxz2)
+                   + qdiv<T>(1 - cPyz, c.gyz2, c.inv_gyz2);
             }
             if (c.g != 0) {
                 const T divPast = reinterpret_cast<const T*>(d.divbuf)[s];
@@ -193,13 +193,13 @@ __global__ void __launch_bounds__(BLOCK) moore_step_kernel(const Geom g, const F
                       - (T)c.twog * (q[0] * (v[0][1] * pt[0][0] - v[0][0] * pt[0][1])
                                     + q[1] * (v[1][1] * pt[1][0] - v[1][0] * pt[1][1]));
                 if (d.energy_form != LAT_ENERGY_MPI) {
-                    const T a0 = qdiv<T>(tx - qth[0], c.gdtdx, 1.0 / c.gdtdx);
-                    const T a1 = qdiv<T>(ty - qth[1], c.gdtdy, 1.0 / c.gdtdy);
-                    const T a2 = qdiv<T>(tz - qth[2], c.gdtdz, 1.0 / c.gdtdz);
+                    const T a0 = qdiv<T>(tx - qth[0], c.gdtdx, c.inv_gdtdx);
+                    const T a1 = qdiv<T>(ty - qth[1], c.gdtdy, c.inv_gdtdy);
+                    const T a2 = qdiv<T>(tz - qth[2], c.gdtdz, c.inv_gdtdz);
                     tdc = (T)0.5 * (a0 * a0 + a1 * a1 + a2 * a2);
-                    const T Fxy = qdiv<T>(1 - cPxy, c.gxy2, 1.0 / c.gxy2);
-                    const T Fxz = qdiv<T>(1 - cPxz, c.gxz2, 1.0 / c.gxz2);
-                    const T Fyz = qdiv<T>(1 - cPyz, c.gyz2, 1.0 / c.gyz2);
+                    const T Fxy = qdiv<T>(1 - cPxy, c.gxy2, c.inv_gxy2);
+                    const T Fxz = qdiv<T>(1 - cPxz, c.gxz2, c.inv_gxz2);
+                    const T Fyz = qdiv<T>(1 - cPyz, c.gyz2, c.inv_gyz2);
                     fc = Fxy + Fxz + Fyz;
                 }
             }
@@ -232,9 +232,10 @@ __global__ void __launch_bounds__(BLOCK) moore_step_kernel(const Geom g, const F
 }
 
 template <class T>
-cudaError_t launch_moore_step_t(const Geom& g, const Fields<T, 7>& f, const StepCoef& c, const DiagOut& d, bool diag,
+cudaError_t launch_moore_step_t(const Geom& g, const Fields<T, 7>& f, const StepCoef& c64, const DiagOut& d, bool diag,
                                 cudaStream_t st)
 {
+    const StepCoefT<T> c = coef_as<T>(c64);
     const dim3 grid = site_grid(g);
     const dim3 block(BZ, BY);
     if (diag) moore_step_kernel<T, true><<<grid, block, 0, st>>>(g, f, c, d);

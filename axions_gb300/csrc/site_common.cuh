@@ -25,10 +25,10 @@ struct Trig<float> {
 // a / b.  FP64 divides (the reference's rounding); FP32 multiplies by the
 // reciprocal computed once on the host.
 template <class T>
-__device__ __forceinline__ T qdiv(T a, double b, double inv_b)
+__device__ __forceinline__ T qdiv(T a, T b, T inv_b)
 {
     if constexpr (sizeof(T) == 8) return a / b;
-    else return a * (T)inv_b;
+    else return a * inv_b;
 }
 
 // Leapfrog update X^{n+1} from X^n, X^{n-1} and the acceleration.

@@ -40,6 +40,9 @@ sys.path.insert(0, str(ROOT))
 
 BYTES_PER_SITE = {"f64": 120, "f64_fast": 120, "f32": 60}  # 5 values x (read now, read past, write new)
 DIAG_EVERY = 20
+KERNEL_NAME = {"f64": "ah_links_kernel + ah_update_kernel (strict FP64 two-pass step)",
+               "f64_fast": "ah_links_kernel + ah_update_kernel (fast FP64 two-pass step)",
+               "f32": "ah_tiled_kernel<float> (FP32 fused tiled step)"}
 
 
 def workload_params(n: int, precision: str):
@@ -351,7 +354,7 @@ def main():
                    "parallelism": "replicas" if ws > 1 else "single"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": load_traffic(head, n), "peak_source": peak_src,
-                     "kernel": "ah_links_kernel + ah_update_kernel (FP64 step)", "kernel_ms": res["kern_ms"],
+                     "kernel": KERNEL_NAME[head], "kernel_ms": res["kern_ms"],
                      "bytes_per_site": BYTES_PER_SITE[head]},
         "cpu_baseline": cpu,
         "e2e": {"value": units / (e2e_max * 1e-3), "unit": "site-updates/s",

@@ -281,3 +281,32 @@ def test_strict_non_power_of_two_spacing(lattice_mod, oracle_mod):
     np.testing.assert_allclose([o[1] for o in out], [r[1] for r in ref], rtol=TOL)
     np.testing.assert_allclose([o[2] for o in out], [r[2] for r in ref], rtol=1e-10)
     lat.close()
+
+
+@pytest.mark.parametrize("bc", [0, 1])
+def test_fp32_tiled_kernel_odd_sizes(lattice_mod, bc):
+    """The tiled FP32 kernel (x-march, shared-memory staging) on sides that are
+    not multiples of its tile (32 x 8) or of its x-chunk, periodic and fixed
+    boundaries: it must track the FP64 path, and the one-pass FP32 kernel, to
+    FP32 accuracy."""
+    from axions_gb300.params import ENERGY_EVOLUTION, F32, make_params
+    p = make_params(0, nx=70, ny=29, nz=45, d=0.5, dt=0.1, lam=2.0, g=1.0, damped_nt=3, dampFac=0.5, alpha=3.0,
+                    energy_form=ENERGY_EVOLUTION, bc=bc)
+    ic = lattice_mod.random_phase_ic(p, 23)
+    res = {}
+    for name, prec, var in (("f64", 0, 0), ("f32", F32, 0), ("f32_onepass", F32, 1)):
+        q = p.copy()
+        q.precision = prec
+        q.kernel_variant = var
+        lat = lattice_mod.Lattice(q)
+        lat.set_state(ic, ic, 0)
+        d = lat.advance(12, diag_every=4)
+        res[name] = (lat.get_slots(), d)
+        lat.close()
+    s64 = res["f64"][0]
+    for name in ("f32", "f32_onepass"):
+        s, d = res[name]
+        mx, l2 = normwise(s, s64)
+        assert l2 < 2e-6 and mx < 2e-5, (name, mx, l2)
+        np.testing.assert_allclose([x[1] for x in d], [x[1] for x in res["f64"][1]], rtol=1e-5)
+        np.testing.assert_allclose([x[2] for x in d], [x[2] for x in res["f64"][1]], rtol=1e-4)
