@@ -90,7 +90,7 @@ def build_programs(verbose: bool = False) -> list[Path]:
             outs.append(exe)
             continue
         cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I", str(ROOT / "include"), str(s)] + [str(c) for c in common]
-        cmd += ["-L", str(PKG), "-llattice_gpu", f"-Wl,-rpath,{PKG}", "-o", str(exe)]
+        cmd += ["-L", str(PKG), "-llattice_gpu", "-Wl,-rpath,$ORIGIN/..", "-o", str(exe)]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)

@@ -1,0 +1,574 @@
+// Drop-in host programs: see evolve.hpp.
+#include "evolve.hpp"
+
+#include <sys/stat.h>
+#include <sys/time.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "lattice_gpu.h"
+
+namespace axh {
+
+namespace {
+
+bool is_moore(Program p) { return p == Program::MooreMpiEvolution || p == Program::MooreEvol; }
+bool is_mpi(Program p) { return p == Program::MpiEvolution || p == Program::MooreMpiEvolution; }
+
+std::string trim(const std::string& s)
+{
+    const size_t a = s.find_first_not_of(" \t\r\n");
+    if (a == std::string::npos) return "";
+    const size_t b = s.find_last_not_of(" \t\r\n");
+    return s.substr(a, b - a + 1);
+}
+
+void fail(const std::string& msg)
+{
+    throw std::runtime_error(msg);
+}
+
+void check(int rc, const char* what)
+{
+    if (rc != LAT_OK) fail(std::string(what) + " failed (" + std::to_string(rc) + "): " + lat_last_error());
+}
+
+}  // namespace
+
+// Reference defaults: mpi_evolution.cpp:17-57, evolution.cpp:23-56,
+// moore_mpi_evolution.cpp:17-63, mooreEvol.cpp:19-41.
+Params::Params(Program prog)
+{
+    auto& v = vals_;
+    v["precision"] = "f64";     // f64 | f32 | f64_fast  (this library)
+    v["out_dir"] = ".";         // where Data/ and GifData/ live (reference: next to its source)
+    v["digits"] = "6";          // ostream precision of the text output (reference default 6)
+    v["countRate"] = "10";
+    v["scaling"] = "1";
+    switch (prog) {
+    case Program::MpiEvolution:
+        v["nx"] = v["ny"] = v["nz"] = "1001";
+        v["nt"] = "2501";
+        v["dx"] = v["dy"] = v["dz"] = "0.25";
+        v["dt"] = "0.05";
+        v["lambda"] = "1";
+        v["eta"] = "1";
+        v["g"] = "0";
+        v["damped_nt"] = "200";
+        v["dampFac"] = "0.5";
+        v["alpha"] = "3";
+        v["makeGif"] = "false";
+        v["makeStringPosGif"] = "true";
+        v["saveFreq"] = "5";
+        v["outTag"] = "global_PRS_dx0p25";
+        v["ic_type"] = "random";
+        v["seed"] = "42";
+        v["stringPos"] = "false";
+        v["stringDetect"] = "true";
+        v["detectBuffer"] = "true";
+        v["splitLength"] = "false";
+        v["finalOut"] = "false";
+        v["calcEnergy"] = "false";
+        break;
+    case Program::Evolution:
+        v["nx"] = v["ny"] = v["nz"] = "101";
+        v["nt"] = "1001";
+        v["dx"] = v["dy"] = v["dz"] = "0.5";
+        v["dt"] = "0.05";
+        v["lambda"] = "1";
+        v["eta"] = "1";
+        v["g"] = "0";
+        v["damped_nt"] = "200";
+        v["dampFac"] = "0.5";
+        v["alpha"] = "3";
+        v["makeGif"] = "false";
+        v["makeStringPosGif"] = "true";
+        v["saveFreq"] = "5";
+        v["xyBC"] = "periodic";
+        v["zBC"] = "periodic";
+        v["stringPos"] = "false";
+        v["stationary_ic"] = "true";
+        v["stringDetect"] = "true";
+        v["detectBuffer"] = "true";
+        v["splitLength"] = "false";
+        v["finalOut"] = "false";
+        break;
+    case Program::MooreMpiEvolution:
+        v["nx"] = v["ny"] = v["nz"] = "1001";
+        v["nt"] = "2501";
+        v["dx"] = v["dy"] = v["dz"] = "0.25";
+        v["dt"] = "0.05";
+        v["lambda1"] = "1";
+        v["lambda2"] = "1";
+        v["lambda12"] = "0";
+        v["eta1"] = "1";
+        v["eta2"] = "1";
+        v["q1"] = "2";
+        v["q2"] = "";           // default q1 - 1 (moore_mpi_evolution.cpp:34)
+        v["g"] = "";            // default from lambda1, eta1, q1, q2 (:35)
+        v["damped_nt"] = "200";
+        v["dampFac"] = "0.5";
+        v["alpha"] = "3";
+        v["makeGif"] = "false";
+        v["makeStringPosGif"] = "true";
+        v["saveFreq"] = "5";
+        v["outTag"] = "Moore_PRS_dx0p25";
+        v["ic_type"] = "random";
+        v["seed"] = "42";
+        v["stringPos"] = "false";
+        v["stringDetect"] = "true";
+        v["detectBuffer"] = "true";
+        v["splitLength"] = "false";
+        v["finalOut"] = "false";
+        v["calcEnergy"] = "false";
+        v["moore_ic_phase"] = "equal";   // equal (reference) | independent
+        v["detect_phi2"] = "false";      // also write phi2 crossings (extension)
+        break;
+    case Program::MooreEvol:
+        v["nx"] = "201";
+        v["ny"] = "201";
+        v["nz"] = "51";
+        v["nt"] = "6001";
+        v["dx"] = v["dy"] = v["dz"] = "0.7";
+        v["dt"] = "0.3";
+        v["eta1"] = "1";
+        v["eta2"] = "1";
+        v["lambda1"] = "2";
+        v["lambda2"] = "2";
+        v["lambda12"] = "0";
+        v["q1"] = "2";
+        v["q2"] = "";
+        v["g"] = "";
+        v["makeGif"] = "true";
+        v["saveFreq"] = "10";
+        v["xyBC"] = "fixed";
+        break;
+    }
+}
+
+void Params::set(const std::string& key, const std::string& value)
+{
+    if (!vals_.count(key)) fail("unknown parameter '" + key + "'");
+    vals_[key] = value;
+}
+
+void Params::parse_args(int argc, char** argv)
+{
+    for (int a = 1; a < argc; ++a) {
+        const std::string arg = argv[a];
+        const size_t eq = arg.find('=');
+        if (eq == std::string::npos) fail("arguments are key=value, got '" + arg + "'");
+        const std::string key = trim(arg.substr(0, eq)), val = trim(arg.substr(eq + 1));
+        if (key == "params") {
+            std::ifstream in(val);
+            if (!in) fail("cannot read parameter file " + val);
+            std::string line;
+            while (std::getline(in, line)) {
+                const size_t hash = line.find('#');
+                if (hash != std::string::npos) line = line.substr(0, hash);
+                const size_t e = line.find('=');
+                if (trim(line).empty()) continue;
+                if (e == std::string::npos) fail("bad line in " + val + ": " + line);
+                set(trim(line.substr(0, e)), trim(line.substr(e + 1)));
+            }
+        }
+    }
+    for (int a = 1; a < argc; ++a) {  // command-line values win over the file
+        const std::string arg = argv[a];
+        const size_t eq = arg.find('=');
+        const std::string key = trim(arg.substr(0, eq));
+        if (key != "params") set(key, trim(arg.substr(eq + 1)));
+    }
+}
+
+double Params::num(const std::string& k) const
+{
+    const std::string& s = str(k);
+    char* end = nullptr;
+    const double v = std::strtod(s.c_str(), &end);
+    if (s.empty() || *end) fail("parameter " + k + " is not a number: '" + s + "'");
+    return v;
+}
+
+long long Params::integer(const std::string& k) const
+{
+    const double v = num(k);
+    if (v != std::floor(v)) fail("parameter " + k + " must be an integer");
+    return (long long)v;
+}
+
+bool Params::flag(const std::string& k) const
+{
+    const std::string& s = str(k);
+    if (s == "true" || s == "1") return true;
+    if (s == "false" || s == "0") return false;
+    fail("parameter " + k + " must be true or false");
+    return false;
+}
+
+const std::string& Params::str(const std::string& k) const
+{
+    auto it = vals_.find(k);
+    if (it == vals_.end()) fail("missing parameter " + k);
+    return it->second;
+}
+
+namespace {
+
+struct Run {
+    Program prog;
+    Params prm;
+    lat_params p{};
+    int ncomp = 5;
+    int64_t N = 0;
+    std::string dir;
+    int digits = 6;
+    lat_handle* h = nullptr;
+
+    explicit Run(Program pr) : prog(pr), prm(pr) {}
+    ~Run()
+    {
+        if (h) lat_destroy(h);
+    }
+
+    std::string data(const std::string& f) const { return dir + "/Data/" + f; }
+    std::string gif(const std::string& f) const { return dir + "/GifData/" + f; }
+
+    std::ofstream open_out(const std::string& path) const
+    {
+        std::ofstream o(path);
+        if (!o) fail("cannot write " + path);
+        o.precision(digits);
+        return o;
+    }
+
+    void build_params()
+    {
+        check(lat_params_init(&p, is_moore(prog) ? LAT_MODEL_MOORE : LAT_MODEL_AH), "lat_params_init");
+        const std::string prec = prm.str("precision");
+        if (prec == "f64") p.precision = LAT_F64;
+        else if (prec == "f32") p.precision = LAT_F32;
+        else if (prec == "f64_fast") p.precision = LAT_F64_FAST;
+        else fail("precision must be f64, f32 or f64_fast");
+        p.nx = prm.integer("nx");
+        p.ny = prm.integer("ny");
+        p.nz = prm.integer("nz");
+        p.dx = prm.num("dx");
+        p.dy = prm.num("dy");
+        p.dz = prm.num("dz");
+        p.dt = prm.num("dt");
+        p.tau0 = 1;  // conformal time starts at 1 (mpi_evolution.cpp:356)
+        p.scaling = prm.num("scaling");
+        if (is_moore(prog)) {
+            p.lambda = prm.num("lambda1");
+            p.lambda2 = prm.num("lambda2");
+            p.lambda12 = prm.num("lambda12");
+            p.eta = prm.num("eta1");
+            p.eta2 = prm.num("eta2");
+            p.q1 = (double)prm.integer("q1");
+            p.q2 = prm.str("q2").empty() ? p.q1 - 1 : (double)prm.integer("q2");
+            // moore_mpi_evolution.cpp:35 / mooreEvol.cpp:36
+            p.g = prm.str("g").empty() ? std::sqrt(0.5 * p.lambda * std::pow(p.eta, 2) / (p.q1 * p.q1 + p.q2 * p.q2))
+                                       : prm.num("g");
+        } else {
+            p.lambda = prm.num("lambda");
+            p.eta = prm.num("eta");
+            p.g = prm.num("g");
+        }
+        if (prog == Program::MooreEvol) {  // no damping or expansion at all (mooreEvol.cpp:270-271)
+            p.damped_nt = 0;
+            p.dampFac = 0;
+            p.alpha = 0;
+        } else {
+            p.damped_nt = (int32_t)prm.integer("damped_nt");
+            p.dampFac = prm.num("dampFac");
+            p.alpha = prm.num("alpha");
+        }
+        p.energy_form = is_mpi(prog) ? LAT_ENERGY_MPI : LAT_ENERGY_EVOLUTION;
+        p.moore_current = prog == Program::MooreEvol ? LAT_MOORE_CURRENT_CHARGE : LAT_MOORE_CURRENT_PLAIN;
+        p.bc = LAT_BC_PERIODIC;
+        if (prog == Program::Evolution || prog == Program::MooreEvol) {
+            const std::string xy = prm.str("xyBC");
+            const std::string z = prog == Program::Evolution ? prm.str("zBC") : std::string("fixed");
+            auto kind = [](const std::string& b) {
+                if (b == "periodic") return 0;
+                if (b == "neumann" || b == "absorbing") return -1;
+                return 1;  // any other string selects fixed boundaries (evolution.cpp:52-53)
+            };
+            const int kxy = kind(xy), kz = kind(z);
+            if (kxy < 0 || kz < 0) fail("neumann and absorbing boundaries are not provided by this library");
+            if (kxy != kz) fail("mixed periodic/fixed boundaries are not provided by this library");
+            p.bc = kxy == 0 ? LAT_BC_PERIODIC : LAT_BC_FIXED;
+        }
+        ncomp = is_moore(prog) ? 7 : 5;
+        N = p.nx * p.ny * p.nz;
+        dir = prm.str("out_dir");
+        digits = (int)prm.integer("digits");
+        ::mkdir((dir + "/Data").c_str(), 0755);
+        ::mkdir((dir + "/GifData").c_str(), 0755);
+    }
+
+    // Whitespace-separated columns, one line per site in linear order.
+    void read_ic(const std::string& path, int cols, int levels, std::vector<double>& lv0, std::vector<double>& lv1)
+    {
+        std::ifstream ic(path);
+        if (!ic) fail("cannot read " + path);
+        lv0.assign((size_t)ncomp * N, 0.0);
+        lv1.assign((size_t)ncomp * N, 0.0);
+        for (int t = 0; t < levels; ++t) {
+            std::vector<double>& dst = t == 0 ? lv0 : lv1;
+            for (int64_t s = 0; s < N; ++s)
+                for (int c = 0; c < cols; ++c) {
+                    double v;
+                    if (!(ic >> v)) fail(path + ": expected " + std::to_string(levels * N) + " lines of " +
+                                         std::to_string(cols) + " values");
+                    if (!std::isfinite(v)) fail(path + ": non-finite value");
+                    dst[(size_t)c * N + s] = v;
+                }
+        }
+        if (levels == 1) lv1 = lv0;
+    }
+
+    // Write the crossing list of one frame (mpi_evolution.cpp:795-888).
+    int64_t write_crossings(int field, const std::string& path)
+    {
+        int64_t n = 0;
+        check(lat_detect_crossings(h, field, nullptr, 0, &n), "lat_detect_crossings");
+        std::vector<double> xyz((size_t)std::max<int64_t>(n, 1) * 3);
+        if (n) check(lat_detect_crossings(h, field, xyz.data(), n, &n), "lat_detect_crossings");
+        std::ofstream o = open_out(path);
+        for (int64_t q = 0; q < n; ++q) o << xyz[3 * q] << " " << xyz[3 * q + 1] << " " << xyz[3 * q + 2] << std::endl;
+        return n;
+    }
+
+    void write_field_magnitudes(const std::string& path)
+    {
+        std::vector<double> now((size_t)ncomp * N);
+        check(lat_get_state(h, now.data(), nullptr), "lat_get_state");
+        std::ofstream o = open_out(path);
+        for (int64_t s = 0; s < N; ++s) {
+            const double a = std::pow(now[s], 2) + std::pow(now[N + s], 2);
+            if (is_moore(prog)) o << a << " " << std::pow(now[2 * N + s], 2) + std::pow(now[3 * N + s], 2) << std::endl;
+            else o << a << std::endl;
+        }
+    }
+
+    void write_final_field(const std::string& path)
+    {
+        std::vector<double> now((size_t)ncomp * N);
+        check(lat_get_state(h, now.data(), nullptr), "lat_get_state");
+        std::ofstream o = open_out(path);
+        for (int64_t s = 0; s < N; ++s) {
+            for (int c = 0; c < ncomp; ++c) o << (c ? " " : "") << now[(size_t)c * N + s];
+            o << std::endl;
+        }
+    }
+
+    // Position of the string along y = z = 0 by a parabolic fit to the
+    // minimum of |phi|^2 (evolution.cpp:695-720).
+    double string_position()
+    {
+        std::vector<double> now((size_t)ncomp * N);
+        check(lat_get_state(h, now.data(), nullptr), "lat_get_state");
+        const int64_t x0 = (int64_t)(0.5 * (p.nx - 1)), y0 = (int64_t)(0.5 * (p.ny - 1)), z0 = (int64_t)(0.5 * (p.nz - 1));
+        auto mag = [&](int64_t i) {
+            const int64_t s = (i * p.ny + y0) * p.nz + z0;
+            return std::pow(now[s], 2) + std::pow(now[N + s], 2);
+        };
+        double smallest = 1;
+        int64_t is = 0;
+        for (int64_t i = 0; i < p.nx; ++i)
+            if (mag(i) < smallest) {
+                smallest = mag(i);
+                is = i;
+            }
+        if (is < 1 || is + 1 >= p.nx) return (is - x0) * p.dx;
+        const double l = mag(is - 1), r = mag(is + 1);
+        return (is - x0) * p.dx + p.dx * (l - r) / (2 * l - 4 * smallest + 2 * r);
+    }
+};
+
+void progress(long long TimeStep, long long& counter, long long countRate)
+{
+    if (TimeStep > counter) {
+        std::cout << "\rTimestep " << TimeStep - 1 << " completed." << std::flush;
+        counter += countRate;
+    }
+}
+
+int run_mpi(Run& r)
+{
+    // mpi_evolution.cpp:354-995 / moore_mpi_evolution.cpp:378-1063
+    Params& q = r.prm;
+    const long long nt = q.integer("nt"), saveFreq = q.integer("saveFreq"), countRate = q.integer("countRate");
+    const long long seed = q.integer("seed");
+    const bool detect = q.flag("stringDetect"), buffer = q.flag("detectBuffer"), posGif = q.flag("makeStringPosGif");
+    const bool calcEnergy = q.flag("calcEnergy");
+    const bool moore = is_moore(r.prog);
+    struct timeval start, end;
+    gettimeofday(&start, nullptr);
+
+    std::string tagPart = q.str("outTag") + "_nx" + std::to_string(r.p.nx);
+    if (moore) tagPart += "_q1" + std::to_string((long long)r.p.q1);
+    tagPart += "_seed" + std::to_string(seed);
+    std::ofstream valsPerLoop = r.open_out(r.data("valsPerLoop_" + tagPart + ".txt"));
+    { std::ofstream ff = r.open_out(r.data("finalField.txt")); }  // opened, never written (mpi_evolution.cpp:126)
+
+    std::vector<double> now, past;
+    const std::string ic_type = q.str("ic_type");
+    if (ic_type == "random") {
+        now.assign((size_t)r.ncomp * r.N, 0.0);
+        const bool indep = moore && q.str("moore_ic_phase") == "independent";
+        check(lat_random_phase_ic(&r.p, (uint32_t)seed, indep, now.data()), "lat_random_phase_ic");
+        past = now;
+    } else if (ic_type == "stationary data") {
+        r.read_ic(r.data(moore ? "moore_ic.txt" : "ic.txt"), r.ncomp, 1, past, now);
+    } else if (ic_type == "data") {
+        r.read_ic(r.data(moore ? "moore_ic.txt" : "ic.txt"), r.ncomp, 2, past, now);  // block 0 = slot 0 = past
+    } else {
+        fail("ic_type must be random, data or stationary data");
+    }
+    check(lat_create(&r.p, &r.h), "lat_create");
+    check(lat_set_state(r.h, now.data(), past.data(), 0), "lat_set_state");
+    gettimeofday(&end, nullptr);
+    std::cout << "Initial data loaded/generated in: " << end.tv_sec - start.tv_sec << "s" << std::endl;
+
+    long long counter = 0, frame = 0;
+    bool stringsExist = true;
+    const bool phi2 = moore && q.flag("detect_phi2");
+    std::vector<lat_diag> diags;
+    long long n = 0;
+    while (n < nt) {
+        progress(n, counter, countRate);
+        if (detect && saveFreq > 0 && n % saveFreq == 0 && posGif && stringsExist && (!buffer || n >= r.p.damped_nt)) {
+            const std::string name = "gifStringPosData_" + tagPart + "_" + std::to_string(frame) + ".txt";
+            const int64_t cnt = r.write_crossings(LAT_FIELD_PHI1, r.gif(name));
+            if (phi2) r.write_crossings(LAT_FIELD_PHI2, r.gif("gifStringPosData2_" + tagPart + "_" + std::to_string(frame) + ".txt"));
+            ++frame;
+            if (cnt == 0) stringsExist = false;
+        }
+        // advance to the next step that prints progress or may write a frame
+        long long stop = std::min(nt, std::max(n + 1, counter + 1));
+        if (detect && saveFreq > 0 && posGif && stringsExist) stop = std::min(stop, (n / saveFreq + 1) * saveFreq);
+        const int32_t k = (int32_t)std::max(1LL, stop - n);
+        if (calcEnergy) {
+            diags.resize((size_t)k);
+            int64_t got = 0;
+            check(lat_advance(r.h, k, 1, diags.data(), k, &got), "lat_advance");
+            for (int64_t d = 0; d < got; ++d) valsPerLoop << diags[d].energy << std::endl;
+        } else {
+            check(lat_step(r.h, k), "lat_step");
+        }
+        n += k;
+    }
+    std::cout << "\rTimestep " << nt << " completed." << std::endl;
+    gettimeofday(&end, nullptr);
+    std::cout << "Time taken: " << end.tv_sec - start.tv_sec << "s" << std::endl;
+    return 0;
+}
+
+int run_openmp(Run& r)
+{
+    // evolution.cpp:60-1471 / mooreEvol.cpp:44-746
+    Params& q = r.prm;
+    const bool moore = r.prog == Program::MooreEvol;
+    const long long nt = q.integer("nt"), saveFreq = q.integer("saveFreq"), countRate = q.integer("countRate");
+    struct timeval start, end;
+    gettimeofday(&start, nullptr);
+
+    std::string tag;
+    std::string valsName = "valsPerLoop.txt";
+    if (!moore) {
+        std::cout << "Enter a tag for output files: " << std::flush;
+        std::cin >> tag;
+        valsName = "valsPerLoop_" + tag + ".txt";
+    }
+    std::vector<double> now, past;
+    if (moore) r.read_ic(r.data("moore_ic.txt"), 7, 1, past, now);
+    else r.read_ic(r.data("ic.txt"), 5, q.flag("stationary_ic") ? 1 : 2, past, now);
+    check(lat_create(&r.p, &r.h), "lat_create");
+    check(lat_set_state(r.h, now.data(), past.data(), 0), "lat_set_state");
+    std::ofstream valsPerLoop = r.open_out(r.data(valsName));
+
+    const bool makeGif = q.flag("makeGif");
+    const bool detect = !moore && q.flag("stringDetect");
+    const bool buffer = !moore && q.flag("detectBuffer");
+    const bool posGif = !moore && q.flag("makeStringPosGif");
+    const bool stringPos = !moore && q.flag("stringPos");
+    const bool split = !moore && q.flag("splitLength");
+    // deviation normalisation: evolution.cpp:1404-1408, mooreEvol.cpp:383,697
+    const double interior = (double)(r.p.nx - 2) * (r.p.ny - 2) * (r.p.nz - 2);
+    long long counter = 0, gifFrame = 0, posFrame = 0;
+    std::vector<lat_diag> diags;
+    long long n = 0;
+    while (n < nt) {
+        progress(n, counter, countRate);
+        const double pos = stringPos ? r.string_position() : 0;
+        if (detect && (!buffer || n >= r.p.damped_nt) && posGif && saveFreq > 0 && n % saveFreq == 0) {
+            r.write_crossings(LAT_FIELD_PHI1, r.gif("gifStringPosData_" + std::to_string(posFrame) + ".txt"));
+            ++posFrame;
+        }
+        long long stop = std::min(nt, std::max(n + 1, counter + 1));
+        if (saveFreq > 0 && (makeGif || (detect && posGif))) stop = std::min(stop, (n / saveFreq + 1) * saveFreq);
+        if (makeGif && saveFreq > 0 && n % saveFreq == 0) stop = n + 1;  // the frame is the level after this step
+        if (stringPos) stop = n + 1;
+        const int32_t k = (int32_t)std::max(1LL, stop - n);
+        diags.resize((size_t)k);
+        int64_t got = 0;
+        check(lat_advance(r.h, k, 1, diags.data(), k, &got), "lat_advance");
+        for (int64_t d = 0; d < got; ++d) {
+            double dev = diags[d].gauss_abs_sum;
+            if (moore) {
+                dev = dev / interior / interior;
+            } else if (r.p.bc == LAT_BC_PERIODIC) {
+                dev = dev / (double)(r.p.nx * r.p.ny) / (double)r.p.nz;
+            } else {
+                dev = dev / (double)((r.p.nx - 2) * (r.p.ny - 2)) / (double)(r.p.nz - 2);
+            }
+            valsPerLoop << diags[d].energy << " " << dev;
+            if (stringPos) valsPerLoop << " " << pos;
+            // the reference prints an uninitialised stringLength here
+            // (evolution.cpp:66,1415); this program prints 0
+            if (detect) {
+                valsPerLoop << " " << 0.0;
+                if (split) valsPerLoop << " " << 0.0;
+            }
+            valsPerLoop << std::endl;
+        }
+        if (makeGif && saveFreq > 0 && n % saveFreq == 0) {
+            r.write_field_magnitudes(r.gif("gifData_" + std::to_string(gifFrame) + ".txt"));
+            ++gifFrame;
+        }
+        n += k;
+    }
+    std::cout << "\rTimestep " << nt << " completed." << std::endl;
+    if (moore || q.flag("finalOut")) r.write_final_field(r.data("finalField.txt"));
+    gettimeofday(&end, nullptr);
+    std::cout << "Time taken: " << end.tv_sec - start.tv_sec << "s" << std::endl;
+    return 0;
+}
+
+}  // namespace
+
+int run_program(Program prog, int argc, char** argv)
+{
+    try {
+        Run r(prog);
+        r.prm.parse_args(argc, argv);
+        r.build_params();
+        return is_mpi(prog) ? run_mpi(r) : run_openmp(r);
+    } catch (const std::exception& e) {
+        std::cerr << "error: " << e.what() << std::endl;
+        return 2;
+    }
+}
+
+}  // namespace axh
