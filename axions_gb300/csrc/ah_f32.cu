@@ -1,6 +1,7 @@
-// Abelian-Higgs step kernels, float instantiation.
+// Abelian-Higgs step kernels, float instantiation: the tiled FP32 step
+// (tiled_step.cuh) and the one-pass kernel kept for cross-checks.
 #include "ah_step.cuh"
-#include "ah_tiled.cuh"
+#include "tiled_step.cuh"
 
 namespace lat {
 
@@ -13,7 +14,7 @@ cudaError_t launch_ah_step_f32(const Geom& g, const Fields<float, 5>& f, const S
 cudaError_t launch_ah_tiled_f32(const Geom& g, const Fields<float, 5>& f, const StepCoef& c, const DiagOut& d,
                                 bool diag, int chunk, cudaStream_t st)
 {
-    return launch_ah_tiled_t<float>(g, f, c, d, diag, chunk, st);
+    return launch_tiled_t<float, 1>(g, f, c, d, diag, chunk, st);
 }
 
 cudaError_t launch_divergence_f32(const Geom& g, const float* tx, const float* ty, const float* tz, const StepCoef& c,

@@ -457,7 +457,8 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
                 f.now[c] = (const float*)h->slot(c, tNow);
                 f.past[c] = (float*)h->slot(c, tPast);
             }
-            LAT_CKL(launch_moore_step_f32(h->geom, f, cf, d, diag, h->stream));
+            if (p.kernel_variant == 0) LAT_CKL(launch_moore_tiled_f32(h->geom, f, cf, d, diag, h->chunk, h->stream));
+            else LAT_CKL(launch_moore_step_f32(h->geom, f, cf, d, diag, h->stream));
         }
     }
     if (diag) LAT_CKL(launch_finalize(h->partials, h->nblocks, diag_dst, h->stream));

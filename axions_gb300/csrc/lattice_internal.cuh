@@ -113,6 +113,8 @@ cudaError_t launch_ah_twopass_fast(const Geom&, const Fields<double, 5>&, double
 // tiled, x-marching FP32 Abelian-Higgs step; `chunk` x-planes per CTA
 cudaError_t launch_ah_tiled_f32(const Geom&, const Fields<float, 5>&, const StepCoef&, const DiagOut&, bool diag,
                                 int chunk, cudaStream_t);
+cudaError_t launch_moore_tiled_f32(const Geom&, const Fields<float, 7>&, const StepCoef&, const DiagOut&, bool diag,
+                                   int chunk, cudaStream_t);
 // divergence of theta on one level into divbuf (used when no previous step stored it)
 cudaError_t launch_divergence_f64(const Geom&, const double* thx, const double* thy, const double* thz,
                                   const StepCoef&, double* out, cudaStream_t);

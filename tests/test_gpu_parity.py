@@ -310,3 +310,33 @@ def test_fp32_tiled_kernel_odd_sizes(lattice_mod, bc):
         assert l2 < 2e-6 and mx < 2e-5, (name, mx, l2)
         np.testing.assert_allclose([x[1] for x in d], [x[1] for x in res["f64"][1]], rtol=1e-5)
         np.testing.assert_allclose([x[2] for x in d], [x[2] for x in res["f64"][1]], rtol=1e-4)
+
+
+@pytest.mark.parametrize("bc,charges,current", [(0, (1.0, 2.0), 0), (1, (2.0, 1.0), 1), (0, (3.0, -1.0), 1)])
+def test_fp32_tiled_moore(lattice_mod, bc, charges, current):
+    """Moore model on the tiled FP32 kernel (two scalars, link factors
+    e^{i q theta} as powers of e^{i theta}) against the FP64 path and the
+    one-pass FP32 kernel, on sides that are not tile multiples."""
+    from axions_gb300.params import ENERGY_EVOLUTION, F32, MODEL_MOORE, make_params
+    q1, q2 = charges
+    p = make_params(MODEL_MOORE, nx=40, ny=27, nz=37, d=0.5, dt=0.1, lam=2.0, lambda2=2.0, lambda12=0.3, eta=1.0,
+                    eta2=1.0, q1=q1, q2=q2, g=0.8, damped_nt=3, dampFac=0.5, alpha=3.0, bc=bc,
+                    energy_form=ENERGY_EVOLUTION, moore_current=current)
+    ic = lattice_mod.random_phase_ic(p, 31, True)
+    res = {}
+    for name, prec, var in (("f64", 0, 0), ("f32", F32, 0), ("f32_onepass", F32, 1)):
+        q = p.copy()
+        q.precision = prec
+        q.kernel_variant = var
+        lat = lattice_mod.Lattice(q)
+        lat.set_state(ic, ic, 0)
+        d = lat.advance(12, diag_every=4)
+        res[name] = (lat.get_slots(), d)
+        lat.close()
+    s64 = res["f64"][0]
+    for name in ("f32", "f32_onepass"):
+        s, d = res[name]
+        mx, l2 = normwise(s, s64)
+        assert l2 < 3e-6 and mx < 3e-5, (name, mx, l2)
+        np.testing.assert_allclose([x[1] for x in d], [x[1] for x in res["f64"][1]], rtol=1e-5)
+        np.testing.assert_allclose([x[2] for x in d], [x[2] for x in res["f64"][1]], rtol=1e-4)
