@@ -38,21 +38,44 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-BYTES_PER_SITE = {"f64": 120, "f64_fast": 120, "f32": 60}  # 5 values x (read now, read past, write new)
 DIAG_EVERY = 20
+# Workloads: "ah" (AH 512^3, the headline) and "moore" (Moore 768^3 FP32 with FP64 reductions).
+MODEL = {"name": "ah"}
+# algorithmic bytes per site-update: each field value read at levels n and n-1, written at n+1
+BYTES = {"ah": {"f64": 120, "f64_fast": 120, "f32": 60}, "moore": {"f64": 168, "f64_fast": 168, "f32": 84}}
 KERNEL_NAME = {"f64": "ah_links_kernel + ah_update_kernel (strict FP64 two-pass step)",
                "f64_fast": "ah_links_kernel + ah_update_kernel (fast FP64 two-pass step)",
-               "f32": "ah_tiled_kernel<float> (FP32 fused tiled step)"}
+               "f32": "tiled_step_kernel<float, 1> (FP32 fused tiled step)"}
+KERNEL_NAME_MOORE = {"f64": "moore_step_kernel<double> (one-pass FP64 step)",
+                     "f64_fast": "moore_step_kernel<double> (one-pass FP64 step)",
+                     "f32": "tiled_step_kernel<float, 2> (FP32 fused tiled step, two scalars)"}
+
+
+def bytes_per_site(precision: str) -> int:
+    return BYTES[MODEL["name"]][precision]
+
+
+def kernel_name(precision: str) -> str:
+    return (KERNEL_NAME_MOORE if MODEL["name"] == "moore" else KERNEL_NAME)[precision]
 
 
 def workload_params(n: int, precision: str):
-    from axions_gb300.params import ENERGY_EVOLUTION, F32, F64, F64_FAST, make_params
+    from axions_gb300.params import ENERGY_EVOLUTION, F32, F64, F64_FAST, MODEL_MOORE, make_params
     prec = {"f64": F64, "f64_fast": F64_FAST, "f32": F32}[precision]
+    if MODEL["name"] == "moore":
+        # two scalars with charges 1 and 2, equal vevs, lambda1 = lambda2 = 2, e = 1, radiation era
+        return make_params(MODEL_MOORE, n=n, d=0.5, dt=0.1, lam=2.0, lambda2=2.0, lambda12=0.0, eta=1.0, eta2=1.0,
+                           q1=1.0, q2=2.0, g=1.0, damped_nt=0, dampFac=0.0, alpha=3.0, scaling=1.0, tau0=1.0,
+                           energy_form=ENERGY_EVOLUTION, precision=prec)
     return make_params(0, n=n, d=0.5, dt=0.1, lam=2.0, eta=1.0, g=1.0, damped_nt=0, dampFac=0.0, alpha=3.0,
                        scaling=1.0, tau0=1.0, energy_form=ENERGY_EVOLUTION, precision=prec)
 
 
 def workload_name(n: int) -> str:
+    if MODEL["name"] == "moore":
+        return (f"Moore model {n}^3 periodic, phi1/phi2 charges 1/2, eta=1, lambda1=lambda2=2, e=1, dx=0.5, "
+                f"dt=0.1, PRS friction alpha=3 (a~tau, tau0=1), independent phases, energy+Gauss every "
+                f"{DIAG_EVERY} steps")
     return (f"Abelian-Higgs {n}^3 periodic, lambda=2, e=1, eta=1, dx=0.5, dt=0.1, PRS friction alpha=3 "
             f"(a~tau, tau0=1), energy+Gauss every {DIAG_EVERY} steps")
 
@@ -196,7 +219,7 @@ def measure_gpu(n: int, precision: str, steps: int, warmup: int, ws: int, local:
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     p = workload_params(n, precision)
-    ic = lattice.random_phase_ic(p, 42 + local)
+    ic = lattice.random_phase_ic(p, 42 + local, independent=MODEL["name"] == "moore")
     lat = lattice.Lattice(p)
     lat.set_stream(stream.cuda_stream)
     lat.set_state(ic, ic, 0)
@@ -274,7 +297,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--n", type=int, default=512, help="lattice side (workload: 512)")
+    ap.add_argument("--model", choices=["ah", "moore"], default="ah",
+                    help="ah: Abelian-Higgs 512^3 (headline); moore: Moore model 768^3")
+    ap.add_argument("--n", type=int, default=None, help="lattice side (default 512 for ah, 768 for moore)")
     ap.add_argument("--cpu-n", type=int, default=256, help="side of the CPU sample lattice")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--precision", choices=["f64", "f64_fast", "f32"], default="f64",
@@ -283,7 +308,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     ws, rank, local = dist_env()
-    steps, warmup, n = args.steps, max(args.warmup, 0), args.n
+    MODEL["name"] = args.model
+    n = args.n if args.n else (768 if args.model == "moore" else 512)
+    steps, warmup = args.steps, max(args.warmup, 0)
 
     if args.impl == "reference":
         if rank != 0:
@@ -335,7 +362,7 @@ def main():
     for form in ([] if args.no_fp32 else [f for f in ("f64", "f64_fast", "f32") if f != head]):
         r2 = measure_gpu(n, form, steps, warmup, ws, local, peaks)
         t2 = dist_max(ws, r2["total_ms"], dev)
-        ach2 = BYTES_PER_SITE[form] * r2["sites"] / (r2["kern_ms"] * 1e-3) / 1e9
+        ach2 = bytes_per_site(form) * r2["sites"] / (r2["kern_ms"] * 1e-3) / 1e9
         forms[form] = {"value": units / (t2 * 1e-3), "ms_per_step": t2 / steps,
                        "dtype": "f32" if form == "f32" else "f64", "kernel_ms": r2["kern_ms"],
                        "roofline": {"bound": "hbm", "achieved": ach2, "peak": hbm, "unit": "GB/s",
@@ -343,19 +370,21 @@ def main():
                        "speedup_vs_f64": res["total_ms"] / r2["total_ms"]}
     if rank != 0:
         return
-    achieved = BYTES_PER_SITE[head] * res["sites"] / (res["kern_ms"] * 1e-3) / 1e9
+    achieved = bytes_per_site(head) * res["sites"] / (res["kern_ms"] * 1e-3) / 1e9
     line = {
         "metric": "site-updates/s", "value": units / (t_max * 1e-3), "unit": "site-updates/s", "n_gpus": ws,
         "steps": steps, "warmup": warmup, "ms_per_step": t_max / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if head == "f32" else "f64",
         "data": "synthetic: seeded uniform-phase IC (mt19937, mpi_evolution.cpp:287-312)",
-        "config": {"workload": workload_name(n), "model": "abelian-higgs", "lattice": n, "precision": head,
-                   "diag_every": DIAG_EVERY, "l2": f"inputs larger than L2 ({2 * 5 * 8 * n ** 3 / 1e9:.1f} GB state)",
+        "config": {"workload": workload_name(n), "model": "moore" if args.model == "moore" else "abelian-higgs",
+                   "lattice": n, "precision": head,
+                   "diag_every": DIAG_EVERY,
+                   "l2": f"inputs larger than L2 ({2 * bytes_per_site(head) / 3 * n ** 3 / 1e9:.1f} GB state)",
                    "parallelism": "replicas" if ws > 1 else "single"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": load_traffic(head, n), "peak_source": peak_src,
-                     "kernel": KERNEL_NAME[head], "kernel_ms": res["kern_ms"],
-                     "bytes_per_site": BYTES_PER_SITE[head]},
+                     "kernel": kernel_name(head), "kernel_ms": res["kern_ms"],
+                     "bytes_per_site": bytes_per_site(head)},
         "cpu_baseline": cpu,
         "e2e": {"value": units / (e2e_max * 1e-3), "unit": "site-updates/s",
                 "h2d_bytes_per_step": res["e2e_h2d"], "d2h_bytes_per_step": res["e2e_d2h"]},
