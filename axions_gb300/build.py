@@ -38,6 +38,7 @@ UNITS = {
     "moore_f32.cu": [],
     "misc.cu": [],
     "lattice_api.cu": [],
+    "batch.cu": [],
     "host_ic.cpp": [],
 }
 

@@ -24,3 +24,13 @@ cudaError_t launch_divergence_f32(const Geom& g, const float* tx, const float* t
 }
 
 }  // namespace lat
+
+namespace lat {
+
+int tiled_blocks(const Geom& g, int chunk)
+{
+    const dim3 t = tiled_grid(g, chunk);
+    return (int)(t.x * t.y * t.z);
+}
+
+}  // namespace lat

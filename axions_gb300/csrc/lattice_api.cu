@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "lattice_handle.hpp"
 #include "lattice_internal.cuh"
 
 namespace lat {
@@ -94,41 +95,6 @@ StepCoef make_coef(const lat_params& p, int64_t n)
 
 using namespace lat;
 
-struct lat_handle {
-    lat_params p;
-    int ncomp = 0;
-    int64_t N = 0;
-    size_t elem = 8;
-    Geom geom;
-    int device = 0;
-    cudaStream_t own = nullptr;
-    cudaStream_t stream = nullptr;
-    int64_t n = 0;             // TimeStep of the "now" level
-    bool div_valid = false;    // divbuf holds the divergence of the past level
-    // device memory
-    void* fields = nullptr;    // [ncomp][2][N]
-    void* divbuf = nullptr;    // [N]
-    double* links = nullptr;   // two-pass FP64 link data [ah_link_slots()][N]
-    size_t links_bytes = 0;
-    bool recip = false;        // every spacing is a power of two: exact reciprocals
-    int chunk = 32;            // x-planes per CTA of the tiled FP32 kernel
-    double* partials = nullptr;
-    int nblocks = 0;
-    double* diag_dev = nullptr;
-    int64_t diag_cap = 0;
-    double* staging = nullptr;  // [N] doubles (FP32 handles)
-    long long* det_blocks = nullptr;
-    long long* det_total = nullptr;
-    int det_nb = 0;
-    double* det_xyz = nullptr;
-    int64_t det_cap = 0;
-    int8_t* wind = nullptr;
-    unsigned long long* wind_sum = nullptr;
-    int64_t bytes = 0;
-    int64_t launches = 0;      // kernels launched by this handle
-
-    char* slot(int comp, int t) const { return (char*)fields + ((size_t)comp * 2 + (size_t)t) * (size_t)N * elem; }
-};
 
 #define LAT_CK(call)                                                                             \
     do {                                                                                         \
@@ -461,7 +427,12 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
             else LAT_CKL(launch_moore_step_f32(h->geom, f, cf, d, diag, h->stream));
         }
     }
-    if (diag) LAT_CKL(launch_finalize(h->partials, h->nblocks, diag_dst, h->stream));
+    if (diag) {
+        // partials written by the step: one per CTA of the kernel that ran
+        const bool tiled = h->elem == 4 && p.kernel_variant == 0;
+        const int used = tiled ? tiled_blocks(h->geom, h->chunk) : h->nblocks;
+        LAT_CKL(launch_finalize(h->partials, used, diag_dst, h->stream));
+    }
     if (write) {
         h->n += 1;
         h->div_valid = store_div;

@@ -110,6 +110,8 @@ cudaError_t launch_ah_twopass_strict(const Geom&, const Fields<double, 5>&, doub
                                      bool diag, bool recip, cudaStream_t);
 cudaError_t launch_ah_twopass_fast(const Geom&, const Fields<double, 5>&, double* L, const StepCoef&, const DiagOut&,
                                    bool diag, bool recip, cudaStream_t);
+// number of CTAs (and diagnostic partials) of the tiled FP32 step
+int tiled_blocks(const Geom&, int chunk);
 // tiled, x-marching FP32 Abelian-Higgs step; `chunk` x-planes per CTA
 cudaError_t launch_ah_tiled_f32(const Geom&, const Fields<float, 5>&, const StepCoef&, const DiagOut&, bool diag,
                                 int chunk, cudaStream_t);

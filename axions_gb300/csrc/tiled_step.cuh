@@ -118,21 +118,22 @@ __device__ __forceinline__ void stage_plane(TiledSmem<T, NS>& sm, int b, const F
     __pipeline_commit();
 }
 
+// One tile: columns (bx*TZ.., by*TY..) of the evolved region, x-planes
+// [bz*chunk, bz*chunk + chunk).  Called by every thread of the CTA.  With DIAG
+// the CTA's energy and |G| sums are written to part[0], part[1].
 template <class T, int NS, bool DIAG>
-__global__ void __launch_bounds__(TT_THREADS, 2)
-tiled_step_kernel(const Geom g, const Fields<T, 2 * NS + 3> f, const StepCoefT<T> c, const Charges<T> ch,
-                  const DiagOut d, const int chunk)
+__device__ __forceinline__ void tiled_tile(TiledSmem<T, NS>& sm, const Geom& g, const Fields<T, 2 * NS + 3>& f,
+                                           const StepCoefT<T>& c, const Charges<T>& ch, const DiagOut& d, int bx,
+                                           int by, int bz, int chunk, double* part)
 {
     using TR = Trig<T>;
     using LI = LinkIdx<NS>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TiledSmem<T, NS>& sm = *reinterpret_cast<TiledSmem<T, NS>*>(smem_raw);
     constexpr int TH0 = 2 * NS;  // first theta component
 
     const int tz = threadIdx.x, ty = threadIdx.y;
-    const int k0 = g.lo + (int)blockIdx.x * TT_Z;
-    const int j0 = g.lo + (int)blockIdx.y * TT_Y;
-    const int ib = g.lo + (int)blockIdx.z * chunk;
+    const int k0 = g.lo + bx * TT_Z;
+    const int j0 = g.lo + by * TT_Y;
+    const int ib = g.lo + bz * chunk;
     const int ie = min(ib + chunk, g.hix);
     const int k = k0 + tz, j = j0 + ty;
     const bool active = (k < g.hiz) && (j < g.hiy);
@@ -407,11 +408,23 @@ tiled_step_kernel(const Geom g, const Fields<T, 2 * NS + 3> f, const StepCoefT<T
                 a += sm.red[0][w];
                 b += sm.red[1][w];
             }
-            const int blk = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-            d.partials[2 * blk] = a;
-            d.partials[2 * blk + 1] = b;
+            part[0] = a;
+            part[1] = b;
         }
+        __syncthreads();  // sm.red is reused by the CTA's next tile
     }
+}
+
+template <class T, int NS, bool DIAG>
+__global__ void __launch_bounds__(TT_THREADS, 2)
+tiled_step_kernel(const Geom g, const Fields<T, 2 * NS + 3> f, const StepCoefT<T> c, const Charges<T> ch,
+                  const DiagOut d, const int chunk)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TiledSmem<T, NS>& sm = *reinterpret_cast<TiledSmem<T, NS>*>(smem_raw);
+    const int blk = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    tiled_tile<T, NS, DIAG>(sm, g, f, c, ch, d, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, chunk,
+                            DIAG ? d.partials + 2 * blk : nullptr);
 }
 
 inline dim3 tiled_grid(const Geom& g, int chunk)

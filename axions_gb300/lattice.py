@@ -28,6 +28,8 @@ EXPORTS = [
     "lat_kernel_launches",
     "lat_set_state", "lat_get_state", "lat_step", "lat_step_diag", "lat_advance", "lat_diagnostics",
     "lat_detect_crossings", "lat_winding", "lat_ah_step_f64_noalloc",
+    "lat_batch_create", "lat_batch_destroy", "lat_batch_add", "lat_batch_remove", "lat_batch_size",
+    "lat_batch_kernel_launches", "lat_batch_advance", "lat_batch_take_diags",
 ]
 
 
@@ -82,6 +84,15 @@ def load_library(path: Path | None = None):
     L.lat_detect_crossings.argtypes = [vp, ctypes.c_int32, dp, ctypes.c_int64, P(ctypes.c_int64)]
     L.lat_winding.argtypes = [vp, ctypes.c_int32, P(ctypes.c_int8), P(ctypes.c_int64)]
     L.lat_ah_step_f64_noalloc.argtypes = [P(LatParams), vp, ctypes.c_int64, ctypes.c_int32, vp]
+    L.lat_batch_create.argtypes = [ctypes.c_int32, P(vp)]
+    L.lat_batch_destroy.argtypes = [vp]
+    L.lat_batch_add.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_int64]
+    L.lat_batch_remove.argtypes = [vp, vp]
+    L.lat_batch_size.argtypes = [vp]
+    L.lat_batch_kernel_launches.argtypes = [vp]
+    L.lat_batch_kernel_launches.restype = ctypes.c_int64
+    L.lat_batch_advance.argtypes = [vp, ctypes.c_int32]
+    L.lat_batch_take_diags.argtypes = [vp, vp, P(LatDiag), ctypes.c_int64, P(ctypes.c_int64)]
     if path is None:
         _lib = L
     return L
@@ -226,3 +237,70 @@ class Lattice:
         ptr = out.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)) if want_array else None
         _check("lat_winding", self.L.lat_winding(self.h, int(field), ptr, ctypes.byref(tot)))
         return out, int(tot.value)
+
+
+class Batch:
+    """Many FP32 lattices advanced together (lat_batch_* of the C ABI).
+
+    Every lattice of the batch steps in the same kernel launches; a call
+    advancing K steps is one CUDA graph.  Results per lattice are bitwise the
+    same as stepping it alone.
+    """
+
+    def __init__(self, max_jobs: int = 64):
+        self.L = load_library()
+        b = ctypes.c_void_p()
+        _check("lat_batch_create", self.L.lat_batch_create(int(max_jobs), ctypes.byref(b)))
+        self.b = b
+        self.members = []
+
+    def add(self, lat: "Lattice", diag_every: int = 0, stop_step: int | None = None) -> int:
+        stop = (1 << 62) if stop_step is None else int(stop_step)
+        rc = self.L.lat_batch_add(self.b, lat.h, int(diag_every), stop)
+        if rc < 0:
+            _check("lat_batch_add", rc)
+        self.members.append(lat)
+        return rc
+
+    def remove(self, lat: "Lattice"):
+        _check("lat_batch_remove", self.L.lat_batch_remove(self.b, lat.h))
+        self.members.remove(lat)
+
+    def advance(self, nsteps: int) -> int:
+        rc = self.L.lat_batch_advance(self.b, int(nsteps))
+        if rc < 0:
+            _check("lat_batch_advance", rc)
+        return rc
+
+    def take_diags(self, lat: "Lattice"):
+        cnt = ctypes.c_int64(0)
+        _check("lat_batch_take_diags", self.L.lat_batch_take_diags(self.b, lat.h, None, 0, ctypes.byref(cnt)))
+        n = cnt.value
+        buf = (LatDiag * max(n, 1))()
+        _check("lat_batch_take_diags", self.L.lat_batch_take_diags(self.b, lat.h, buf, n, ctypes.byref(cnt)))
+        return [(buf[q].time_step, buf[q].energy, buf[q].gauss_abs_sum) for q in range(n)]
+
+    @property
+    def size(self) -> int:
+        return int(self.L.lat_batch_size(self.b))
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.L.lat_batch_kernel_launches(self.b))
+
+    def close(self):
+        if getattr(self, "b", None) is not None and self.b.value:
+            self.L.lat_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

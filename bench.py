@@ -291,6 +291,91 @@ def measure_gpu(n: int, precision: str, steps: int, warmup: int, ws: int, local:
     }
 
 
+def ensemble_jobs(njobs: int, n: int):
+    """The batched-ensemble workload: AH n^3 lattices, FP32 fields, each with
+    its own seed, lambda ~ U[0.5, 4] and e ~ U[0.5, 2] from a fixed meta-seed."""
+    import numpy as np
+
+    from axions_gb300.params import ENERGY_EVOLUTION, F32, make_params
+    rng = np.random.default_rng(20260)
+    jobs = []
+    for q in range(njobs):
+        lam = float(rng.uniform(0.5, 4.0))
+        e = float(rng.uniform(0.5, 2.0))
+        p = make_params(0, n=n, d=0.5, dt=0.1, lam=lam, eta=1.0, g=e, damped_nt=0, dampFac=0.0, alpha=0.0,
+                        energy_form=ENERGY_EVOLUTION, precision=F32)
+        jobs.append((p, q))
+    return jobs
+
+
+def measure_ensemble(njobs: int, n: int, steps: int, diag_every: int, tick: int):
+    """Runs/hour of an ensemble: batched (all lattices in the same launches,
+    one CUDA graph per tick) against the same jobs run one after another
+    through the single-lattice path.  Both are timed twice: stepping only
+    (state resident) and end to end (host IC generation, upload, stepping,
+    diagnostics, download of the final fields)."""
+    import numpy as np
+    import torch
+
+    from axions_gb300 import lattice
+    jobs = ensemble_jobs(njobs, n)
+    out = {"jobs": njobs, "lattice": n, "steps": steps, "diag_every": diag_every, "tick_steps": tick}
+
+    def run_sequential():
+        t_step = 0.0
+        t0 = time.perf_counter()
+        for p, seed in jobs:
+            lat = lattice.Lattice(p)
+            ic = lattice.random_phase_ic(p, seed)
+            lat.set_state(ic, ic, 0)
+            torch.cuda.synchronize()
+            s0 = time.perf_counter()
+            lat.advance(steps, diag_every)
+            t_step += time.perf_counter() - s0
+            lat.get_state()
+            lat.close()
+        return time.perf_counter() - t0, t_step
+
+    def run_batched():
+        t0 = time.perf_counter()
+        lats = []
+        for p, seed in jobs:
+            lat = lattice.Lattice(p)
+            ic = lattice.random_phase_ic(p, seed)
+            lat.set_state(ic, ic, 0)
+            lats.append(lat)
+        torch.cuda.synchronize()
+        with lattice.Batch(max(njobs, 1)) as b:
+            for lat in lats:
+                b.add(lat, diag_every=diag_every, stop_step=steps)
+            s0 = time.perf_counter()
+            while b.advance(tick) > 0:
+                pass
+            t_step = time.perf_counter() - s0
+            launches = b.kernel_launches
+            for lat in lats:
+                b.take_diags(lat)
+        for lat in lats:
+            lat.get_state()
+            lat.close()
+        return time.perf_counter() - t0, t_step, launches
+
+    run_batched()      # warm-up: graph capture, module loading
+    seq_total, seq_step = run_sequential()
+    bat_total, bat_step, launches = run_batched()
+    su = njobs * n ** 3 * steps
+    out.update({
+        "batched": {"runs_per_hour": njobs / bat_step * 3600, "runs_per_hour_e2e": njobs / bat_total * 3600,
+                    "site_updates_per_s": su / bat_step, "kernel_launches": launches},
+        "sequential": {"runs_per_hour": njobs / seq_step * 3600, "runs_per_hour_e2e": njobs / seq_total * 3600,
+                       "site_updates_per_s": su / seq_step},
+    })
+    out["speedup"] = out["batched"]["runs_per_hour"] / out["sequential"]["runs_per_hour"]
+    out["speedup_e2e"] = out["batched"]["runs_per_hour_e2e"] / out["sequential"]["runs_per_hour_e2e"]
+    del np
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -306,6 +391,10 @@ def main():
                     help="form of the headline number (the workload's plain path is f64)")
     ap.add_argument("--no-fp32", action="store_true", help="measure only the headline form")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--ensemble-jobs", type=int, default=64)
+    ap.add_argument("--ensemble-n", type=int, default=128)
+    ap.add_argument("--ensemble-steps", type=int, default=500)
     args = ap.parse_args()
     ws, rank, local = dist_env()
     MODEL["name"] = args.model
@@ -368,6 +457,9 @@ def main():
                        "roofline": {"bound": "hbm", "achieved": ach2, "peak": hbm, "unit": "GB/s",
                                     "frac": ach2 / hbm, "traffic": load_traffic(form, n)},
                        "speedup_vs_f64": res["total_ms"] / r2["total_ms"]}
+    ensemble = None
+    if not args.no_ensemble:
+        ensemble = measure_ensemble(args.ensemble_jobs, args.ensemble_n, args.ensemble_steps, DIAG_EVERY, 50)
     if rank != 0:
         return
     achieved = bytes_per_site(head) * res["sites"] / (res["kern_ms"] * 1e-3) / 1e9
@@ -393,6 +485,7 @@ def main():
         "fp32": forms.get("f32"),
         "f64_fast": forms.get("f64_fast"),
         "f64": forms.get("f64"),
+        "ensemble": ensemble,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:

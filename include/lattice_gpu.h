@@ -216,6 +216,30 @@ int lat_detect_crossings(lat_handle* h, int32_t field, double* xyz, int64_t cap,
  * the lattice are 0. */
 int lat_winding(lat_handle* h, int32_t field, int8_t* out, int64_t* abs_sum);
 
+/* ---- batches: many lattices advanced by the same launches ----------------------
+ * The reference runs one lattice per program invocation; an ensemble of
+ * independent lattices (different seeds, couplings, sizes, models) is a loop of
+ * runs.  A batch advances all its lattices together: each step is one
+ * persistent kernel over the tiles of every lattice, and nsteps of them are one
+ * CUDA graph.  Lattices are ordinary FP32 handles (LAT_F32): state transfer,
+ * detection and winding keep working on each handle between batch calls.  A
+ * lattice's results are bitwise the same alone, in any mix and through
+ * lat_step/lat_advance on its own handle. */
+typedef struct lat_batch lat_batch;
+int lat_batch_create(int32_t max_jobs, lat_batch** out);          /* max_jobs <= 256 */
+int lat_batch_destroy(lat_batch* b);                               /* handles are not freed */
+/* Add a lattice; it advances until its TimeStep reaches stop_step and records
+ * a lat_diag every diag_every steps (0: none).  Returns its slot (>= 0). */
+int lat_batch_add(lat_batch* b, lat_handle* h, int32_t diag_every, int64_t stop_step);
+int lat_batch_remove(lat_batch* b, lat_handle* h);
+int lat_batch_size(const lat_batch* b);
+int64_t lat_batch_kernel_launches(const lat_batch* b);
+/* Advance every lattice by up to nsteps (not past its stop_step).  Returns the
+ * number of lattices that have not reached their stop_step. */
+int lat_batch_advance(lat_batch* b, int32_t nsteps);
+/* Move the diagnostics recorded for h so far into out (oldest first). */
+int lat_batch_take_diags(lat_batch* b, lat_handle* h, lat_diag* out, int64_t cap, int64_t* count);
+
 /* ---- stepping without allocation ---------------------------------------------- */
 /* Largest lattice (sites) lat_ah_step_f64_noalloc accepts: 64^3. */
 #define LAT_NOALLOC_MAX_SITES 262144
