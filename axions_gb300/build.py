@@ -39,6 +39,9 @@ UNITS = {
     "misc.cu": [],
     "lattice_api.cu": [],
     "batch.cu": [],
+    "device_ic.cu": [],
+    "tune.cu": [],
+    "server.cpp": [],
     "host_ic.cpp": [],
 }
 

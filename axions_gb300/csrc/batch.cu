@@ -66,7 +66,7 @@ __device__ __forceinline__ void run_item(unsigned char* smem_raw, const BatchJob
 // the work items of all of them.  One kernel per model keeps each kernel's
 // register use to that model's tile.
 template <int NS>
-__global__ void __launch_bounds__(TT_THREADS, NS == 1 ? 3 : 2) batch_step_kernel(const BatchStep* __restrict__ tab)
+__global__ void __launch_bounds__(TT_THREADS, NS == 1 ? 4 : 2) batch_step_kernel(const BatchStep* __restrict__ tab)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ BatchJob sj;
@@ -391,8 +391,12 @@ int lat_batch_advance(lat_batch* b, int32_t nsteps)
             J.d.charge_current = J.ch.charge_current;
             J.d.write = 1;
             J.diag = diag ? 1 : 0;
-            J.chunk = h->chunk;
-            const dim3 tg = tiled_grid(h->geom, h->chunk);
+            // In a batch the other lattices supply the parallelism, so each
+            // lattice marches long x-ranges (one prologue per 128 planes).  The
+            // value depends on the lattice's own shape only, never on its
+            // company, so results do not depend on the mix.
+            J.chunk = std::min(h->geom.hix - h->geom.lo, 128);
+            const dim3 tg = tiled_grid(h->geom, J.chunk);
             J.tiles_z = (int)tg.x;
             J.tiles_y = (int)tg.y;
             J.items = (int)(tg.x * tg.y * tg.z);

@@ -202,6 +202,27 @@ static int validate(const lat_params* p)
     return LAT_OK;
 }
 
+// Device bytes lat_create allocates for `p` (the same terms as below).
+static int64_t footprint(const lat_params& p)
+{
+    const int64_t N = p.nx * p.ny * p.nz;
+    const int64_t elem = p.precision == LAT_F32 ? 4 : 8;
+    const int64_t ncomp = p.model == LAT_MODEL_MOORE ? 7 : 5;
+    int64_t b = ncomp * 2 * N * elem + N * elem;  // fields, divbuf
+    if (p.model == LAT_MODEL_AH && elem == 8 && p.kernel_variant == 0) b += 8 * (int64_t)ah_link_slots() * N;
+    const dim3 gr = site_grid(make_geom(p));
+    b += 16 * (int64_t)gr.x * gr.y * gr.z;        // partials
+    b += (int64_t)sizeof(long long) + (int64_t)sizeof(unsigned long long);
+    return b;
+}
+
+int64_t lat_footprint_bytes(const lat_params* p)
+{
+    int rc = validate(p);
+    if (rc) return rc;
+    return footprint(*p);
+}
+
 int lat_create(const lat_params* p, lat_handle** out)
 {
     int rc = validate(p);
@@ -225,6 +246,7 @@ int lat_create(const lat_params* p, lat_handle** out)
     };
     h->recip = pow2(p->dx) && pow2(p->dy) && pow2(p->dz);
     h->geom = make_geom(*p);
+    h->chunk = default_chunk(*p);
     cudaGetDevice(&h->device);
     auto fail = [&](int code) {
         lat_destroy(h);
@@ -255,6 +277,37 @@ int lat_create(const lat_params* p, lat_handle** out)
     *out = h;
     return LAT_OK;
 }
+
+}  // extern "C"
+
+namespace lat {
+
+// Give an existing lattice new parameters of the same shape (model,
+// precision, boundaries, sides, kernels): the serving loop reuses idle
+// lattices this way instead of freeing and allocating device memory.  The
+// state is left as is; TimeStep restarts at 0.
+int reconfigure_handle(lat_handle* h, const lat_params* p)
+{
+    int rc = validate(p);
+    if (rc) return rc;
+    LAT_REQUIRE(h, "reconfigure: null handle");
+    LAT_REQUIRE(p->model == h->p.model && p->precision == h->p.precision && p->bc == h->p.bc && p->nx == h->p.nx &&
+                    p->ny == h->p.ny && p->nz == h->p.nz && p->kernel_variant == h->p.kernel_variant,
+                "reconfigure: different shape");
+    h->p = *p;
+    h->n = 0;
+    h->div_valid = false;
+    auto pow2 = [](double v) {
+        int e;
+        return std::frexp(v, &e) == 0.5;
+    };
+    h->recip = pow2(p->dx) && pow2(p->dy) && pow2(p->dz);
+    return LAT_OK;
+}
+
+}  // namespace lat
+
+extern "C" {
 
 int lat_destroy(lat_handle* h)
 {

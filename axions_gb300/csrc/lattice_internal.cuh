@@ -110,6 +110,9 @@ cudaError_t launch_ah_twopass_strict(const Geom&, const Fields<double, 5>&, doub
                                      bool diag, bool recip, cudaStream_t);
 cudaError_t launch_ah_twopass_fast(const Geom&, const Fields<double, 5>&, double* L, const StepCoef&, const DiagOut&,
                                    bool diag, bool recip, cudaStream_t);
+// x-planes per CTA of the tiled FP32 step for a new handle (tuned value of the
+// shape if known in this process, else a heuristic); tune.cu
+int default_chunk(const lat_params& p);
 // number of CTAs (and diagnostic partials) of the tiled FP32 step
 int tiled_blocks(const Geom&, int chunk);
 // tiled, x-marching FP32 Abelian-Higgs step; `chunk` x-planes per CTA

@@ -30,7 +30,15 @@ EXPORTS = [
     "lat_detect_crossings", "lat_winding", "lat_ah_step_f64_noalloc",
     "lat_batch_create", "lat_batch_destroy", "lat_batch_add", "lat_batch_remove", "lat_batch_size",
     "lat_batch_kernel_launches", "lat_batch_advance", "lat_batch_take_diags",
+    "lat_random_phase_ic_device", "lat_philox4x32_10", "lat_autotune", "lat_get_tuning", "lat_set_tuning",
+    "lat_tune_cache_save", "lat_tune_cache_load", "lat_footprint_bytes",
+    "lat_server_create", "lat_server_submit", "lat_server_poll", "lat_server_wait", "lat_server_diags",
+    "lat_server_get_stats", "lat_server_destroy",
 ]
+
+
+class LatTuning(ctypes.Structure):
+    _fields_ = [("chunk", ctypes.c_int32), ("candidates", ctypes.c_int32), ("ms_per_step", ctypes.c_double)]
 
 
 class LatDiag(ctypes.Structure):
@@ -93,6 +101,23 @@ def load_library(path: Path | None = None):
     L.lat_batch_kernel_launches.restype = ctypes.c_int64
     L.lat_batch_advance.argtypes = [vp, ctypes.c_int32]
     L.lat_batch_take_diags.argtypes = [vp, vp, P(LatDiag), ctypes.c_int64, P(ctypes.c_int64)]
+    u32p = P(ctypes.c_uint32)
+    L.lat_random_phase_ic_device.argtypes = [vp, ctypes.c_uint64, ctypes.c_int32]
+    L.lat_philox4x32_10.argtypes = [u32p, u32p, u32p]
+    L.lat_autotune.argtypes = [vp, ctypes.c_int32, P(LatTuning)]
+    L.lat_get_tuning.argtypes = [vp, P(LatTuning)]
+    L.lat_set_tuning.argtypes = [vp, P(LatTuning)]
+    L.lat_tune_cache_save.argtypes = [ctypes.c_char_p]
+    L.lat_tune_cache_load.argtypes = [ctypes.c_char_p]
+    L.lat_footprint_bytes.argtypes = [P(LatParams)]
+    L.lat_footprint_bytes.restype = ctypes.c_int64
+    L.lat_server_create.argtypes = [vp, P(vp)]
+    L.lat_server_submit.argtypes = [vp, vp, P(ctypes.c_int64)]
+    L.lat_server_poll.argtypes = [vp, ctypes.c_int64, vp]
+    L.lat_server_wait.argtypes = [vp, ctypes.c_int64, ctypes.c_double, vp]
+    L.lat_server_diags.argtypes = [vp, ctypes.c_int64, P(LatDiag), ctypes.c_int64, P(ctypes.c_int64)]
+    L.lat_server_get_stats.argtypes = [vp, vp]
+    L.lat_server_destroy.argtypes = [vp]
     if path is None:
         _lib = L
     return L
@@ -121,6 +146,26 @@ def random_phase_ic(p: LatParams, seed: int, independent: bool = False) -> np.nd
     _check("lat_random_phase_ic",
            load_library().lat_random_phase_ic(ctypes.byref(p), ctypes.c_uint32(seed), int(bool(independent)), _dp(out)))
     return out
+
+
+def philox4x32_10(counter, key):
+    """Philox-4x32-10 (the generator of Lattice.random_phase_ic_device) on the host."""
+    c = (ctypes.c_uint32 * 4)(*counter)
+    k = (ctypes.c_uint32 * 2)(*key)
+    out = (ctypes.c_uint32 * 4)()
+    _check("lat_philox4x32_10", load_library().lat_philox4x32_10(c, k, out))
+    return list(out)
+
+
+def tune_cache_save(path) -> None:
+    _check("lat_tune_cache_save", load_library().lat_tune_cache_save(str(path).encode()))
+
+
+def tune_cache_load(path) -> int:
+    rc = load_library().lat_tune_cache_load(str(path).encode())
+    if rc < 0:
+        _check("lat_tune_cache_load", rc)
+    return rc
 
 
 class Lattice:
@@ -165,6 +210,27 @@ class Lattice:
     @property
     def device_bytes(self) -> int:
         return int(self.L.lat_device_bytes(self.h))
+
+    def random_phase_ic_device(self, seed: int, independent: bool = False):
+        """Random-phase IC drawn on the GPU (Philox-4x32-10); state at TimeStep 0."""
+        _check("lat_random_phase_ic_device",
+               self.L.lat_random_phase_ic_device(self.h, ctypes.c_uint64(seed), int(bool(independent))))
+
+    def autotune(self, trial_steps: int = 3) -> LatTuning:
+        t = LatTuning()
+        _check("lat_autotune", self.L.lat_autotune(self.h, int(trial_steps), ctypes.byref(t)))
+        return t
+
+    @property
+    def tuning(self) -> LatTuning:
+        t = LatTuning()
+        _check("lat_get_tuning", self.L.lat_get_tuning(self.h, ctypes.byref(t)))
+        return t
+
+    def set_chunk(self, chunk: int):
+        t = LatTuning()
+        t.chunk = int(chunk)
+        _check("lat_set_tuning", self.L.lat_set_tuning(self.h, ctypes.byref(t)))
 
     def set_stream(self, stream_handle: int | None):
         _check("lat_set_stream", self.L.lat_set_stream(self.h, ctypes.c_void_p(stream_handle or 0)))
@@ -292,6 +358,96 @@ class Batch:
         if getattr(self, "b", None) is not None and self.b.value:
             self.L.lat_batch_destroy(self.b)
             self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("tick_steps", ctypes.c_int32), ("max_running", ctypes.c_int32)]
+
+
+class JobSpec(ctypes.Structure):
+    _fields_ = [("params", LatParams), ("seed", ctypes.c_uint64), ("nsteps", ctypes.c_int32),
+                ("diag_every", ctypes.c_int32), ("independent", ctypes.c_int32), ("winding_at_end", ctypes.c_int32)]
+
+
+class JobResult(ctypes.Structure):
+    _fields_ = [("job_id", ctypes.c_int64), ("status", ctypes.c_int32), ("ndiag", ctypes.c_int32),
+                ("submit_s", ctypes.c_double), ("start_s", ctypes.c_double), ("end_s", ctypes.c_double),
+                ("final_energy", ctypes.c_double), ("final_gauss", ctypes.c_double),
+                ("winding_abs", ctypes.c_int64), ("site_updates", ctypes.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in ("submitted", "queued", "running", "done", "failed", "site_updates",
+                                              "ticks", "running_bytes", "pooled_bytes", "peak_bytes")] + \
+               [("busy_s", ctypes.c_double), ("wall_s", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+def footprint_bytes(p: LatParams) -> int:
+    """Device bytes a lattice with these parameters holds (lat_footprint_bytes)."""
+    return int(load_library().lat_footprint_bytes(ctypes.byref(p)))
+
+
+class Server:
+    """Job queue with continuous batching on the current device (lat_server_*)."""
+
+    def __init__(self, hbm_budget_bytes: int, tick_steps: int = 25, max_running: int = 128):
+        self.L = load_library()
+        cfg = ServerConfig(int(hbm_budget_bytes), int(tick_steps), int(max_running))
+        s = ctypes.c_void_p()
+        _check("lat_server_create", self.L.lat_server_create(ctypes.byref(cfg), ctypes.byref(s)))
+        self.s = s
+
+    def submit(self, params: LatParams, seed: int, nsteps: int, diag_every: int = 0, independent: bool = False,
+               winding_at_end: bool = True) -> int:
+        spec = JobSpec(params, int(seed), int(nsteps), int(diag_every), int(bool(independent)), int(bool(winding_at_end)))
+        jid = ctypes.c_int64()
+        _check("lat_server_submit", self.L.lat_server_submit(self.s, ctypes.byref(spec), ctypes.byref(jid)))
+        return jid.value
+
+    def poll(self, job_id: int) -> JobResult:
+        r = JobResult()
+        _check("lat_server_poll", self.L.lat_server_poll(self.s, int(job_id), ctypes.byref(r)))
+        return r
+
+    def wait(self, job_id: int, timeout_s: float = 600.0) -> JobResult:
+        r = JobResult()
+        _check("lat_server_wait", self.L.lat_server_wait(self.s, int(job_id), float(timeout_s), ctypes.byref(r)))
+        return r
+
+    def diags(self, job_id: int):
+        cnt = ctypes.c_int64()
+        _check("lat_server_diags", self.L.lat_server_diags(self.s, int(job_id), None, 0, ctypes.byref(cnt)))
+        buf = (LatDiag * max(cnt.value, 1))()
+        _check("lat_server_diags", self.L.lat_server_diags(self.s, int(job_id), buf, cnt.value, ctypes.byref(cnt)))
+        return [(buf[q].time_step, buf[q].energy, buf[q].gauss_abs_sum) for q in range(cnt.value)]
+
+    def stats(self) -> ServerStats:
+        st = ServerStats()
+        _check("lat_server_get_stats", self.L.lat_server_get_stats(self.s, ctypes.byref(st)))
+        return st
+
+    def close(self):
+        if getattr(self, "s", None) is not None and self.s.value:
+            self.L.lat_server_destroy(self.s)
+            self.s = None
 
     def __del__(self):
         try:

@@ -319,15 +319,18 @@ def measure_ensemble(njobs: int, n: int, steps: int, diag_every: int, tick: int)
 
     from axions_gb300 import lattice
     jobs = ensemble_jobs(njobs, n)
-    out = {"jobs": njobs, "lattice": n, "steps": steps, "diag_every": diag_every, "tick_steps": tick}
+    out = {"jobs": njobs, "lattice": n, "steps": steps, "diag_every": diag_every, "tick_steps": tick,
+           "ic": "device Philox-4x32-10 random phases (lat_random_phase_ic_device)"}
+    with lattice.Lattice(jobs[0][0]) as tl:   # tune the shape once; new handles start tuned
+        tuning = tl.autotune(3)
+    out["tuned_chunk"] = tuning.chunk
 
     def run_sequential():
         t_step = 0.0
         t0 = time.perf_counter()
         for p, seed in jobs:
             lat = lattice.Lattice(p)
-            ic = lattice.random_phase_ic(p, seed)
-            lat.set_state(ic, ic, 0)
+            lat.random_phase_ic_device(seed)
             torch.cuda.synchronize()
             s0 = time.perf_counter()
             lat.advance(steps, diag_every)
@@ -341,8 +344,7 @@ def measure_ensemble(njobs: int, n: int, steps: int, diag_every: int, tick: int)
         lats = []
         for p, seed in jobs:
             lat = lattice.Lattice(p)
-            ic = lattice.random_phase_ic(p, seed)
-            lat.set_state(ic, ic, 0)
+            lat.random_phase_ic_device(seed)
             lats.append(lat)
         torch.cuda.synchronize()
         with lattice.Batch(max(njobs, 1)) as b:
@@ -376,6 +378,54 @@ def measure_ensemble(njobs: int, n: int, steps: int, diag_every: int, tick: int)
     return out
 
 
+def measure_serving(njobs: int, rate: float, budget_gb: float, tick: int, seed: int = 4242):
+    """Serving loop under a Poisson stream of jobs: 70 % Abelian-Higgs, 30 %
+    Moore, sides from {64, 96, 128, 192, 256}, 200-1000 steps, lambda in
+    [0.5, 4], e in [0.5, 2], FP32 fields with FP64 diagnostics every 20 steps,
+    device random-phase ICs.  Reports p50/p99 job latency (completion minus
+    submission) and the aggregate site-updates/s over the whole run."""
+    import threading
+
+    import numpy as np
+
+    from axions_gb300 import lattice
+    from axions_gb300.params import ENERGY_EVOLUTION, F32, MODEL_MOORE, make_params
+    rng = np.random.default_rng(seed)
+    specs = []
+    for k in range(njobs):
+        n = int(rng.choice([64, 96, 128, 192, 256]))
+        steps = int(rng.integers(200, 1001))
+        lam, e = float(rng.uniform(0.5, 4.0)), float(rng.uniform(0.5, 2.0))
+        if rng.random() < 0.7:
+            p = make_params(0, n=n, d=0.5, dt=0.1, lam=lam, eta=1.0, g=e, damped_nt=0, alpha=0.0,
+                            energy_form=ENERGY_EVOLUTION, precision=F32)
+        else:
+            p = make_params(MODEL_MOORE, n=n, d=0.5, dt=0.1, lam=lam, lambda2=lam, eta=1.0, eta2=1.0, q1=1.0, q2=2.0,
+                            g=e, damped_nt=0, alpha=0.0, energy_form=ENERGY_EVOLUTION, precision=F32)
+        specs.append((p, k, steps, float(rng.exponential(1.0 / rate))))
+    ids = []
+    with lattice.Server(int(budget_gb * (1 << 30)), tick_steps=tick, max_running=128) as srv:
+        def client():
+            for p, k, steps, gap in specs:
+                time.sleep(gap)
+                ids.append(srv.submit(p, seed=k, nsteps=steps, diag_every=20, independent=True))
+        th = threading.Thread(target=client)
+        th.start()
+        th.join()
+        res = [srv.wait(i, 3600) for i in ids]
+        st = srv.stats()
+    ok = [r for r in res if r.status == 2]
+    lat_s = np.array([r.end_s - r.submit_s for r in ok])
+    span = max(r.end_s for r in ok) - min(r.submit_s for r in res)
+    su = sum(r.site_updates for r in ok)
+    return {"jobs": njobs, "done": len(ok), "rate_jobs_per_s": rate, "mix": "70% AH / 30% Moore",
+            "sides": [64, 96, 128, 192, 256], "steps": "200-1000", "precision": "f32 fields, f64 diagnostics",
+            "tick_steps": tick, "hbm_budget_gb": budget_gb,
+            "latency_p50_s": float(np.percentile(lat_s, 50)), "latency_p99_s": float(np.percentile(lat_s, 99)),
+            "latency_max_s": float(lat_s.max()), "site_updates_per_s": su / span, "makespan_s": span,
+            "gpu_busy_frac": st.busy_s / st.wall_s, "peak_hbm_gb": st.peak_bytes / (1 << 30)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -395,6 +445,9 @@ def main():
     ap.add_argument("--ensemble-jobs", type=int, default=64)
     ap.add_argument("--ensemble-n", type=int, default=128)
     ap.add_argument("--ensemble-steps", type=int, default=500)
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
+    ap.add_argument("--serving-jobs", type=int, default=120, help="jobs in the Poisson stream (workload: 2000)")
+    ap.add_argument("--serving-rate", type=float, default=4.0, help="mean arrivals per second")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     MODEL["name"] = args.model
@@ -460,6 +513,9 @@ def main():
     ensemble = None
     if not args.no_ensemble:
         ensemble = measure_ensemble(args.ensemble_jobs, args.ensemble_n, args.ensemble_steps, DIAG_EVERY, 50)
+    serving = None
+    if not args.no_serving:
+        serving = measure_serving(args.serving_jobs, args.serving_rate, 96.0, 25)
     if rank != 0:
         return
     achieved = bytes_per_site(head) * res["sites"] / (res["kern_ms"] * 1e-3) / 1e9
@@ -486,6 +542,7 @@ def main():
         "f64_fast": forms.get("f64_fast"),
         "f64": forms.get("f64"),
         "ensemble": ensemble,
+        "serving": serving,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:

@@ -216,6 +216,41 @@ int lat_detect_crossings(lat_handle* h, int32_t field, double* xyz, int64_t cap,
  * the lattice are 0. */
 int lat_winding(lat_handle* h, int32_t field, int8_t* out, int64_t* abs_sum);
 
+/* ---- device-side random-phase IC ------------------------------------------------
+ * The physics of lat_random_phase_ic (phi = eta*e^{i phase}, phase uniform in
+ * [0, 2 pi), both levels equal, theta = 0, TimeStep 0) drawn on the GPU with
+ * the counter-based generator Philox-4x32-10: site s uses counter (s, 0, 0, 0)
+ * and key (seed & 0xffffffff, seed >> 32); its phase is 2 pi times the 53-bit
+ * uniform of outputs 0 and 1 (for Moore with independent != 0, phi2's phase
+ * comes from outputs 2 and 3).  Not the reference's mt19937 sequence: for
+ * ensembles and served jobs, where reproducing it is not needed.  No
+ * counterpart in the reference. */
+int lat_random_phase_ic_device(lat_handle* h, uint64_t seed, int32_t independent);
+/* The generator on the host (checks, reproduction of device ICs). */
+int lat_philox4x32_10(const uint32_t counter[4], const uint32_t key[2], uint32_t out[4]);
+
+/* ---- tuning of the tiled FP32 step ------------------------------------------------
+ * chunk = x-planes each CTA of the tiled FP32 step marches through.  New
+ * handles start with the value tuned for their shape in this process (or
+ * loaded from a cache file), else with a heuristic.  lat_autotune times the
+ * candidates on a scratch lattice of the same shape (the handle's state is
+ * untouched), applies the fastest and remembers it.  No counterpart in the
+ * reference. */
+typedef struct lat_tuning {
+    int32_t chunk;
+    int32_t candidates;    /* candidates timed by lat_autotune (0: not tuned) */
+    double ms_per_step;    /* measured time of the chosen candidate */
+} lat_tuning;
+int lat_autotune(lat_handle* h, int32_t trial_steps, lat_tuning* out);
+int lat_get_tuning(const lat_handle* h, lat_tuning* out);
+int lat_set_tuning(lat_handle* h, const lat_tuning* t);
+int lat_tune_cache_save(const char* path);
+int lat_tune_cache_load(const char* path);   /* returns the number of entries loaded */
+
+/* Device bytes lat_create would allocate for p (negative status if p is invalid);
+ * used for admission by HBM footprint.  No counterpart in the reference. */
+int64_t lat_footprint_bytes(const lat_params* p);
+
 /* ---- batches: many lattices advanced by the same launches ----------------------
  * The reference runs one lattice per program invocation; an ensemble of
  * independent lattices (different seeds, couplings, sizes, models) is a loop of
@@ -239,6 +274,55 @@ int64_t lat_batch_kernel_launches(const lat_batch* b);
 int lat_batch_advance(lat_batch* b, int32_t nsteps);
 /* Move the diagnostics recorded for h so far into out (oldest first). */
 int lat_batch_take_diags(lat_batch* b, lat_handle* h, lat_diag* out, int64_t cap, int64_t* count);
+
+/* ---- serving: a job queue with continuous batching ------------------------------
+ * The reference runs one job per program invocation (run_mpi_evol.sh,
+ * submit_job.sh).  A server owns a worker thread and one batch.  Jobs are
+ * admitted in arrival order while their device footprint (lat_footprint_bytes)
+ * fits hbm_budget_bytes, get a device random-phase IC
+ * (lat_random_phase_ic_device) and join the batch; the batch advances
+ * tick_steps steps at a time, jobs arriving meanwhile join at the next tick and
+ * finished jobs leave.  Fields stay on the device for a job's whole life.  A
+ * job's results are the same whatever else runs beside it.  Served jobs run
+ * the FP32 path.  No counterpart in the reference. */
+typedef struct lat_server lat_server;
+typedef struct lat_server_config {
+    int64_t hbm_budget_bytes;   /* device memory the running (and pooled) lattices may hold */
+    int32_t tick_steps;         /* steps per batch call (one CUDA graph)                   */
+    int32_t max_running;        /* jobs on the device at once, <= 256                      */
+} lat_server_config;
+typedef struct lat_job_spec {
+    lat_params params;          /* precision LAT_F32                                       */
+    uint64_t seed;              /* device IC seed                                          */
+    int32_t nsteps;             /* steps to run from TimeStep 0                           */
+    int32_t diag_every;         /* record energy/Gauss every diag_every steps (0: none)    */
+    int32_t independent;        /* Moore: independent phases for phi2                      */
+    int32_t winding_at_end;     /* compute sum |winding| of phi (phi1) at the end          */
+} lat_job_spec;
+typedef struct lat_job_result {
+    int64_t job_id;
+    int32_t status;             /* 0 queued, 1 running, 2 done, < 0 failed (LAT_ERR_*)     */
+    int32_t ndiag;              /* diagnostics recorded (lat_server_diags)                 */
+    double submit_s, start_s, end_s;  /* seconds since the server started                   */
+    double final_energy;        /* diagnostics of the final level                          */
+    double final_gauss;
+    int64_t winding_abs;        /* sum |winding| of the final level, if requested          */
+    int64_t site_updates;       /* nx*ny*nz*nsteps                                         */
+} lat_job_result;
+typedef struct lat_server_stats {
+    int64_t submitted, queued, running, done, failed;
+    int64_t site_updates, ticks;
+    int64_t running_bytes, pooled_bytes, peak_bytes;
+    double busy_s, wall_s;
+} lat_server_stats;
+int lat_server_create(const lat_server_config* cfg, lat_server** out);
+int lat_server_submit(lat_server* s, const lat_job_spec* spec, int64_t* job_id);
+int lat_server_poll(lat_server* s, int64_t job_id, lat_job_result* out);
+int lat_server_wait(lat_server* s, int64_t job_id, double timeout_s, lat_job_result* out);
+int lat_server_diags(lat_server* s, int64_t job_id, lat_diag* out, int64_t cap, int64_t* count);
+int lat_server_get_stats(lat_server* s, lat_server_stats* out);
+/* Drops queued jobs, lets running ones finish, frees everything. */
+int lat_server_destroy(lat_server* s);
 
 /* ---- stepping without allocation ---------------------------------------------- */
 /* Largest lattice (sites) lat_ah_step_f64_noalloc accepts: 64^3. */
