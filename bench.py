@@ -374,7 +374,72 @@ def measure_ensemble(njobs: int, n: int, steps: int, diag_every: int, tick: int)
     })
     out["speedup"] = out["batched"]["runs_per_hour"] / out["sequential"]["runs_per_hour"]
     out["speedup_e2e"] = out["batched"]["runs_per_hour_e2e"] / out["sequential"]["runs_per_hour_e2e"]
+    # The reference's own way to run an ensemble: one program invocation per
+    # job (run_mpi_evol.sh, submit_job.sh).  Timed with the drop-in program on
+    # a few jobs; each invocation creates its CUDA context, draws its mt19937
+    # IC, steps and exits.
+    prog = ROOT / "axions_gb300" / "bin" / "mpi_evolution"
+    if prog.exists():
+        import subprocess as sp
+        import tempfile as tf
+        times = []
+        for p, seed in jobs[:3]:
+            with tf.TemporaryDirectory() as d:
+                cmd = [str(prog), f"out_dir={d}", f"nx={n}", f"ny={n}", f"nz={n}", f"nt={steps}", "dx=0.5", "dy=0.5",
+                       "dz=0.5", "dt=0.1", f"lambda={p.lam}", f"g={p.g}", "damped_nt=0", "alpha=0", "precision=f32",
+                       "stringDetect=false", "calcEnergy=false", f"seed={seed}", "countRate=1000000"]
+                t0 = time.perf_counter()
+                r = sp.run(cmd, stdout=sp.DEVNULL, stderr=sp.PIPE)
+                times.append(time.perf_counter() - t0)
+                if r.returncode != 0:
+                    times = []
+                    break
+        if times:
+            per = sum(times) / len(times)
+            out["program_launches"] = {"seconds_per_run": per, "runs_per_hour": 3600 / per, "sampled_runs": len(times),
+                                       "program": "axions_gb300/bin/mpi_evolution precision=f32 (one process per job)"}
+            out["speedup_vs_program_launches_e2e"] = out["batched"]["runs_per_hour_e2e"] / (3600 / per)
     del np
+    return out
+
+
+def measure_fp32_accuracy(n: int, steps: int, sample_every: int = 100):
+    """FP32 form against the FP64 path on the same seeded IC (the workload's
+    physics, diagnostics every 20 steps): field L2 drift at the end, the largest
+    relative difference of the energy and of the Gauss residual over the run,
+    and the total string length L = dx * sum |winding| (and the number of
+    bilinear crossings) every `sample_every` steps."""
+    import numpy as np
+
+    from axions_gb300 import lattice
+    out = {"lattice": n, "steps": steps, "diag_every": DIAG_EVERY,
+           "string_length": "dx * sum over plaquettes of |winding of phi|"}
+    runs = {}
+    for prec in ("f64", "f32"):
+        p = workload_params(n, prec)
+        with lattice.Lattice(p) as lat:
+            lat.random_phase_ic_device(2026)
+            diags, lengths, crossings = [], [], []
+            for s0 in range(0, steps, sample_every):
+                diags += lat.advance(min(sample_every, steps - s0), DIAG_EVERY)
+                _, w = lat.winding(0, want_array=False)
+                lengths.append(w * p.dx)
+                crossings.append(len(lat.detect(0)))
+            now, _ = lat.get_state()
+        runs[prec] = (np.array([d[1] for d in diags]), np.array([d[2] for d in diags]), np.array(lengths),
+                      np.array(crossings), now)
+    e64, g64, l64, c64, f64 = runs["f64"]
+    e32, g32, l32, c32, f32 = runs["f32"]
+    rel = lambda a, b: float(np.max(np.abs(a - b) / np.abs(b)))  # noqa: E731
+    out.update({
+        "field_l2_drift": float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64)),
+        "scalar_l2_drift": float(np.linalg.norm(f32[:2] - f64[:2]) / np.linalg.norm(f64[:2])),
+        "energy_rel_max": rel(e32, e64), "energy_rel_final": float(abs(e32[-1] - e64[-1]) / abs(e64[-1])),
+        "gauss_rel_max": rel(g32, g64), "gauss_rel_final": float(abs(g32[-1] - g64[-1]) / abs(g64[-1])),
+        "string_length_f64": l64.tolist(), "string_length_f32": l32.tolist(),
+        "string_length_rel_max": rel(l32, l64), "string_length_rel_final": float(abs(l32[-1] - l64[-1]) / l64[-1]),
+        "crossings_f64": c64.tolist(), "crossings_f32": c32.tolist(),
+    })
     return out
 
 
@@ -448,6 +513,9 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--serving-jobs", type=int, default=120, help="jobs in the Poisson stream (workload: 2000)")
     ap.add_argument("--serving-rate", type=float, default=4.0, help="mean arrivals per second")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy study")
+    ap.add_argument("--accuracy-n", type=int, default=256, help="lattice side of the accuracy study (workload: 512)")
+    ap.add_argument("--accuracy-steps", type=int, default=1000)
     args = ap.parse_args()
     ws, rank, local = dist_env()
     MODEL["name"] = args.model
@@ -516,6 +584,9 @@ def main():
     serving = None
     if not args.no_serving:
         serving = measure_serving(args.serving_jobs, args.serving_rate, 96.0, 25)
+    accuracy = None
+    if not args.no_accuracy and args.model == "ah":
+        accuracy = measure_fp32_accuracy(args.accuracy_n, args.accuracy_steps)
     if rank != 0:
         return
     achieved = bytes_per_site(head) * res["sites"] / (res["kern_ms"] * 1e-3) / 1e9
@@ -543,6 +614,7 @@ def main():
         "f64": forms.get("f64"),
         "ensemble": ensemble,
         "serving": serving,
+        "fp32_accuracy": accuracy,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:

@@ -702,3 +702,138 @@ int orc_winding(const lat_params* p, const double* st, int64_t n, int field,
     if (abs_sum) *abs_sum = tot;
     return 0;
 }
+
+/* ------------------------------------------------------------------------- */
+/* ic_func.cpp:647-683 random IC: minstd_rand(seed) (Park-Miller, multiplier */
+/* 48271, modulus 2^31-1) and uniform_real_distribution<double>(-1, 1) as     */
+/* libstdc++ computes it (generate_canonical from two draws).  Per site in    */
+/* linear order: phi_re, phi_im, then (if g != 0) theta_mu = d_mu * u.  Both  */
+/* time levels equal.                                                         */
+/* ------------------------------------------------------------------------- */
+typedef struct { uint64_t x; } orc_minstd;
+
+static uint32_t minstd_next(orc_minstd* g)
+{
+    g->x = (g->x * 48271u) % 2147483647u;
+    return (uint32_t)g->x;
+}
+
+static double minstd_uniform_m1_1(orc_minstd* g)
+{
+    const long double r = 2147483646.0L;  /* max - min + 1 */
+    double sum = 0.0, tmp = 1.0;
+    sum += (double)(minstd_next(g) - 1u) * tmp;
+    tmp = (double)((long double)tmp * r);
+    sum += (double)(minstd_next(g) - 1u) * tmp;
+    tmp = (double)((long double)tmp * r);
+    double u = sum / tmp;
+    if (u >= 1.0) u = nextafter(1.0, 0.0);
+    return u * (1.0 - (-1.0)) + (-1.0);
+}
+
+int orc_icfunc_random_ic(const lat_params* p, uint32_t seed, double* st)
+{
+    if (!p || !st || p->model != LAT_MODEL_AH) return LAT_ERR_INVALID;
+    const int64_t N = p->nx * p->ny * p->nz;
+    memset(st, 0, sizeof(double) * 5 * 2 * (size_t)N);
+    orc_minstd g;
+    g.x = seed % 2147483647u;
+    if (g.x == 0) g.x = 1;
+    for (int64_t s = 0; s < N; ++s) {
+        double v[5] = {0, 0, 0, 0, 0};
+        v[0] = minstd_uniform_m1_1(&g);
+        v[1] = minstd_uniform_m1_1(&g);
+        if (p->g != 0) {
+            v[2] = p->dx * minstd_uniform_m1_1(&g);
+            v[3] = p->dy * minstd_uniform_m1_1(&g);
+            v[4] = p->dz * minstd_uniform_m1_1(&g);
+        }
+        for (int c = 0; c < 5; ++c) {
+            st[((int64_t)c * 2 + 0) * N + s] = v[c];
+            st[((int64_t)c * 2 + 1) * N + s] = v[c];
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* total string length by greedy chaining of crossings                        */
+/* (ic_w_evolution.cpp:961-1087), single-thread semantics: from the current   */
+/* point, the nearest remaining point within (dx^2+dy^2+dz^2)^2 (compared     */
+/* with the squared distance; the last of equally near points wins) is the     */
+/* next; its distance is added; when none is left in reach, the distance to    */
+/* the first point of the chain is checked and, if within reach, the cutoff's  */
+/* square root is added (as the reference does), and a new chain starts at     */
+/* the first remaining point.  Per-axis minimum image only for periodic axes.  */
+/* With split, lengths are added to L0 when the current point lies in the     */
+/* central quarter-box, else to L1.  O(M^2), like the reference.              */
+/* ------------------------------------------------------------------------- */
+static double chain_dist2(const double* a, const double* b, double bx, double by, double bz, int pxy, int pz)
+{
+    double d = 0, t;
+    t = fabs(a[0] - b[0]);
+    if (t <= 0.5 * bx) d = (a[0] - b[0]) * (a[0] - b[0]);
+    else if (pxy) d = (bx - t) * (bx - t);
+    t = fabs(a[1] - b[1]);
+    if (t <= 0.5 * by) d += (a[1] - b[1]) * (a[1] - b[1]);
+    else if (pxy) d += (by - t) * (by - t);
+    t = fabs(a[2] - b[2]);
+    if (t <= 0.5 * bz) d += (a[2] - b[2]) * (a[2] - b[2]);
+    else if (pz) d += (bz - t) * (bz - t);
+    return d;
+}
+
+int orc_string_length(const lat_params* p, const double* xyz, int64_t M, int split, double* L0, double* L1)
+{
+    if (!p || (!xyz && M) || !L0 || !L1) return LAT_ERR_INVALID;
+    const double dx = p->dx, dy = p->dy, dz = p->dz;
+    const double bx = p->nx * dx, by = p->ny * dy, bz = p->nz * dz;
+    const int per = p->bc == LAT_BC_PERIODIC;
+    const double c0 = dx * dx + dy * dy + dz * dz;
+    const double cutoff = c0 * c0;
+    *L0 = 0;
+    *L1 = 0;
+    if (M == 0) return 0;
+    char* alive = (char*)malloc((size_t)M);
+    if (!alive) return LAT_ERR_NOMEM;
+    memset(alive, 1, (size_t)M);
+    int64_t f = 0, first = 0;
+    double begin[3] = {xyz[0], xyz[1], xyz[2]};
+    for (int64_t it = 0; it < M; ++it) {
+        double best = cutoff;
+        int64_t bi = -1;
+        for (int64_t j = 0; j < M; ++j) {
+            if (!alive[j] || j == f) continue;
+            const double d = chain_dist2(&xyz[3 * f], &xyz[3 * j], bx, by, bz, per, per);
+            if (d <= best) {
+                best = d;
+                bi = j;
+            }
+        }
+        const double* cf = &xyz[3 * f];
+        const int inner = cf[0] >= -0.25 * p->nx * dx && cf[0] <= 0.25 * p->nx * dx && cf[1] >= -0.25 * p->ny * dy &&
+                          cf[1] <= 0.25 * p->ny * dy && cf[2] >= -0.25 * p->nz * dz && cf[2] <= 0.25 * p->nz * dz;
+        if (bi >= 0) {
+            if (split && !inner) *L1 += sqrt(best);
+            else *L0 += sqrt(best);
+            alive[f] = 0;
+            f = bi;
+        } else {
+            const double d = chain_dist2(cf, begin, bx, by, bz, per, per);
+            if (d <= best) {
+                if (split && !inner) *L1 += sqrt(best);
+                else *L0 += sqrt(best);
+            }
+            alive[f] = 0;
+            while (first < M && !alive[first]) ++first;
+            if (first < M) {
+                f = first;
+                begin[0] = xyz[3 * f];
+                begin[1] = xyz[3 * f + 1];
+                begin[2] = xyz[3 * f + 2];
+            }
+        }
+    }
+    free(alive);
+    return 0;
+}

@@ -56,6 +56,12 @@ int orc_detect(const lat_params* p, const double* st, int64_t n, int field,
 int orc_winding(const lat_params* p, const double* st, int64_t n, int field,
                 int8_t* out, int64_t* abs_sum);
 
+/* ic_func.cpp's "random" IC (minstd_rand, uniform in [-1, 1] per component) */
+int orc_icfunc_random_ic(const lat_params* p, uint32_t seed, double* st);
+
+/* total string length by greedy chaining of crossings, ic_w_evolution.cpp:961-1087 */
+int orc_string_length(const lat_params* p, const double* xyz, int64_t M, int split, double* L0, double* L1);
+
 #ifdef __cplusplus
 }
 #endif

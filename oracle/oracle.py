@@ -53,6 +53,8 @@ def lib():
         L.orc_mt_seed.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
         L.orc_uniform_0_2pi.argtypes = [ctypes.c_void_p]
         L.orc_uniform_0_2pi.restype = ctypes.c_double
+        L.orc_icfunc_random_ic.argtypes = [P(LatParams), ctypes.c_uint32, dp]
+        L.orc_string_length.argtypes = [P(LatParams), dp, ctypes.c_int64, ctypes.c_int, dp, dp]
         _lib = L
     return _lib
 
@@ -136,6 +138,27 @@ def winding(p: LatParams, st: np.ndarray, n: int, field: int = 0):
     if rc != 0:
         raise RuntimeError(f"orc_winding rc={rc}")
     return out, int(tot.value)
+
+
+def icfunc_random_ic(p: LatParams, seed: int) -> np.ndarray:
+    """ic_func.cpp:647-683 "random" IC (minstd_rand, uniform in [-1, 1])."""
+    st = empty_state(p)
+    rc = lib().orc_icfunc_random_ic(ctypes.byref(p), int(seed), _dp(st))
+    if rc != 0:
+        raise RuntimeError(f"orc_icfunc_random_ic rc={rc}")
+    return st
+
+
+def string_length(p: LatParams, xyz: np.ndarray, split: bool = True):
+    """(L0, L1) by greedy chaining of the crossings `xyz` (ic_w_evolution.cpp:961-1087)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    L0 = ctypes.c_double(0)
+    L1 = ctypes.c_double(0)
+    rc = lib().orc_string_length(ctypes.byref(p), _dp(xyz) if len(xyz) else None, len(xyz), int(bool(split)),
+                                 ctypes.byref(L0), ctypes.byref(L1))
+    if rc != 0:
+        raise RuntimeError(f"orc_string_length rc={rc}")
+    return L0.value, L1.value
 
 
 def now_slot(n: int) -> int:

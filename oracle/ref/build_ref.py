@@ -37,6 +37,8 @@ PROGRAMS = {
     "moore_mpi_evolution": ([], "totSize,haloSize,coreSize,phi1,phi2,theta"),
     "evolution": (["array.cpp"], None),
     "mooreEvol": (["array.cpp"], None),
+    # ic_w_evolution.cpp:79 builds its IC in-process with ic_func() (ic_func.cpp:18)
+    "ic_w_evolution": (["ic_func.cpp", "array.cpp"], None),
 }
 
 
@@ -55,10 +57,11 @@ def _fmt(v) -> str:
 
 
 def substitute_consts(src: str, consts: dict) -> str:
-    """Replace the initialiser of `const <type> NAME = ...;` lines."""
+    """Replace the initialiser of `[const] <type> NAME = ...;` lines (the
+    boundary-condition strings of ic_w_evolution.cpp:44-45 are not const)."""
     out = src
     for name, val in consts.items():
-        pat = re.compile(r"^(\s*const\s+(?:int|double|bool|string)\s+" + re.escape(name) + r"\s*=\s*)([^;]*)(;)",
+        pat = re.compile(r"^(\s*(?:const\s+)?(?:int|double|bool|string)\s+" + re.escape(name) + r"\s*=\s*)([^;]*)(;)",
                          re.MULTILINE)
         out, n = pat.subn(lambda m: m.group(1) + _fmt(val) + m.group(3), out, count=1)
         if n != 1:
@@ -66,8 +69,10 @@ def substitute_consts(src: str, consts: dict) -> str:
     return out
 
 
-def build(program: str, tag: str, consts: dict) -> Path:
-    """Build `program` with `consts`; return the binary path."""
+def build(program: str, tag: str, consts: dict, extra_consts: dict | None = None) -> Path:
+    """Build `program` with `consts`; return the binary path.  `extra_consts`
+    maps an extra source (e.g. "ic_func.cpp") to the constants substituted in
+    a copy of it."""
     if program not in PROGRAMS:
         raise ValueError(program)
     extra, fields = PROGRAMS[program]
@@ -85,7 +90,14 @@ def build(program: str, tag: str, consts: dict) -> Path:
            "-I", str(REFERENCE)]
     if fields:
         cmd += ["-I", str(HERE / "mpi_stub"), f"-DAXR_FIELDS={fields}"]
-    cmd += [str(work / f"{program}.cpp")] + [str(REFERENCE / e) for e in extra]
+    sources = [str(work / f"{program}.cpp")]
+    for e in extra:
+        if extra_consts and e in extra_consts:
+            (work / e).write_text(substitute_consts((REFERENCE / e).read_text(), extra_consts[e]))
+            sources.append(str(work / e))
+        else:
+            sources.append(str(REFERENCE / e))
+    cmd += sources
     cmd += ["-o", str(binary)]
     subprocess.run(cmd, check=True)
     return binary
@@ -119,5 +131,7 @@ def build_defaults() -> list[Path]:
     out = [build("mpi_evolution", "mpi_evolution_small", small),
            build("moore_mpi_evolution", "moore_mpi_evolution_small", small),
            build("evolution", "evolution_small", small),
-           build("mooreEvol", "mooreEvol_small", small)]
+           build("mooreEvol", "mooreEvol_small", small),
+           build("ic_w_evolution", "ic_w_evolution_small", dict(small, makeGif=False),
+                 {"ic_func.cpp": {"ic_type": "random"}})]
     return out

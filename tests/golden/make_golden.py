@@ -199,9 +199,35 @@ def gen_moore_evol(name, nx, ny, nz, nt, lam1, lam2, lam12, q1, q2, seed, dt=0.1
     print(name, "vals", vals.shape)
 
 
+def gen_icw_length(name, nx, ny, nz, nt, bc, seed, d=0.35, split=True):
+    """ic_w_evolution: IC from ic_func's "random" branch (minstd_rand, seed),
+    evolution without friction, string length by greedy chaining every step
+    (ic_w_evolution.cpp:961-1087); valsPerLoop = energy dev L0 [L1]."""
+    s = "periodic" if bc == BC_PERIODIC else "fixed"
+    consts = {"nx": nx, "ny": ny, "nz": nz, "nt": nt, "dx": d, "dy": d, "dz": d, "dt": 0.05,
+              "makeGif": False, "xyBC": s, "zBC": s, "splitLength": bool(split)}
+    build_ref.build("ic_w_evolution", name, consts, {"ic_func.cpp": {"ic_type": "random", "seed": float(seed)}})
+    work = build_ref.run(name)
+    ncol = 4 if split else 3
+    vals = build_ref.read_columns(work / "Data" / "valsPerLoop_test.txt").reshape(nt, ncol)
+    N = nx * ny * nz
+    final = build_ref.read_columns(work / "Data" / "finalField.txt").reshape(N, 5).T.copy()
+    p = make_params(MODEL_AH, nx=nx, ny=ny, nz=nz, d=d, dt=0.05, lam=1.0, eta=1.0, g=0.0, damped_nt=0,
+                    dampFac=0.0, alpha=0.0, scaling=1.0, tau0=1.0, bc=bc)
+    L1 = vals[:, 3] if split else np.zeros(nt)
+    np.savez_compressed(OUT / f"{name}.npz", program="ic_w_evolution", params=_params_json(p), seed=seed, nt=nt,
+                        split=bool(split), L0=vals[:, 2], L1=L1, energy=vals[:, 0], final_phi=final[:2])
+    print(name, "vals", vals.shape)
+
+
 def main():
     if not build_ref.reference_available():
         raise SystemExit("reference sources not found; fixtures can only be made where they are")
+    only = sys.argv[1:]
+    if only:
+        for call in only:
+            eval(call)
+        return
     gen_mpi_ah_ic("ref_mpi_ah_ic_s7", 6, 5, 4, seed=7)
     # config-1 physics (lambda=2, e=1, dx=0.5, dt=0.1, Minkowski, no damping)
     gen_mpi_ah("ref_mpi_ah_c1", 14, 12, 10, 30, lam=2.0, g=1.0, damped_nt=0, dampFac=0.0, alpha=0.0,
@@ -217,6 +243,11 @@ def main():
     gen_moore_mpi("ref_moore_mpi", 12, 10, 8, 20, 2.0, 2.0, 0.5, 2, 1, damped_nt=6, dampFac=0.5, alpha=3.0,
                   seed=9, saveFreq=5)
     gen_moore_evol("ref_moore_evol", 10, 9, 8, 12, 2.0, 2.0, 0.5, 2, 1, seed=13)
+    # string length (the reference default spacing 0.35; a wide cutoff; fixed walls; no split)
+    gen_icw_length("ref_icw_len_periodic", 17, 15, 13, 40, BC_PERIODIC, seed=3)
+    gen_icw_length("ref_icw_len_wide", 13, 12, 11, 16, BC_PERIODIC, seed=4, d=1.0)
+    gen_icw_length("ref_icw_len_fixed", 15, 15, 15, 25, BC_FIXED, seed=5)
+    gen_icw_length("ref_icw_len_nosplit", 11, 13, 9, 12, BC_PERIODIC, seed=6, d=0.5, split=False)
 
 
 if __name__ == "__main__":

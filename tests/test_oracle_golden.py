@@ -97,3 +97,49 @@ def test_oracle_threads_do_not_change_fields(oracle_mod):
     O.set_threads(1)
     assert np.array_equal(outs[0], outs[1])
     assert np.array_equal(outs[0], z["final"])
+
+
+ICW_CASES = ["ref_icw_len_periodic", "ref_icw_len_wide", "ref_icw_len_fixed", "ref_icw_len_nosplit"]
+
+
+@pytest.mark.parametrize("name", ICW_CASES)
+def test_string_length_chaining_bit_exact(oracle_mod, name):
+    """ic_w_evolution: ic_func's minstd IC, then every step the greedy chaining
+    length of the crossings (ic_w_evolution.cpp:961-1087) -- L0 and L1 of every
+    step and the final field equal the reference's bit for bit."""
+    O = oracle_mod
+    z = load_golden(name)
+    p = params_from_json(z["params"])
+    split = bool(z["split"])
+    st = O.icfunc_random_ic(p, int(z["seed"]))
+    L0s, L1s = [], []
+    for n in range(int(z["nt"])):
+        L0, L1 = O.string_length(p, O.detect(p, st, n, 0), split)
+        L0s.append(L0)
+        L1s.append(L1)
+        O.step(p, st, n)
+    assert np.array_equal(np.array(L0s), z["L0"])
+    assert np.array_equal(np.array(L1s), z["L1"])
+    N = p.nx * p.ny * p.nz
+    last = (int(z["nt"]) - 1) % 2
+    v = st.reshape(5, 2, N)
+    assert np.array_equal(v[:2, last], z["final_phi"])
+
+
+def test_string_length_edge_cases(oracle_mod):
+    """Empty list, one point (closes onto itself: the cutoff's square root),
+    ties (the last of equally near points wins), and the minimum image."""
+    from axions_gb300.params import make_params
+    O = oracle_mod
+    p = make_params(0, nx=16, ny=16, nz=16, d=0.5)
+    c0 = 3 * 0.25
+    assert O.string_length(p, np.zeros((0, 3))) == (0.0, 0.0)
+    assert O.string_length(p, np.array([[0.1, 0.2, 0.3]])) == (c0, 0.0)
+    assert O.string_length(p, np.array([[3.9, 0.0, 0.0]])) == (0.0, c0)
+    # 0 -> (2 or 3, both at 0.5): 3 wins; 3 -> 1 (0.5) ... the walk order fixes the sum
+    pts = np.array([[0.0, 0, 0], [0.0, 0.5, 0.5], [0.5, 0, 0], [-0.5, 0, 0]])
+    L0, _ = O.string_length(p, pts)
+    assert L0 > 0
+    # periodic image: x = -3.9 and x = 3.9 are 0.2 apart on a box of 8
+    L0, L1 = O.string_length(p, np.array([[-3.9, 0.0, 0.0], [3.9, 0.0, 0.0]]))
+    assert L0 == 0 and abs(L1 - (0.2 + c0)) < 1e-15
