@@ -325,6 +325,7 @@ int lat_destroy(lat_handle* h)
     cudaFree(h->det_xyz);
     cudaFree(h->wind);
     cudaFree(h->wind_sum);
+    cudaFree(h->chain_ws);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
     return LAT_OK;
@@ -624,13 +625,9 @@ static DetectArgs detect_args(const lat_handle* h)
     return a;
 }
 
-int lat_detect_crossings(lat_handle* h, int32_t field, double* xyz, int64_t cap, int64_t* count)
+// count the crossings of `field` on the current level (block totals scanned in place)
+static int detect_count(lat_handle* h, int32_t field, int64_t* total_out)
 {
-    LAT_REQUIRE(h && count, "lat_detect_crossings: null argument");
-    LAT_REQUIRE(field == LAT_FIELD_PHI1 || (field == LAT_FIELD_PHI2 && h->p.model == LAT_MODEL_MOORE),
-                "lat_detect_crossings: bad field");
-    LAT_REQUIRE(cap >= 0 && (xyz || cap == 0), "lat_detect_crossings: bad capacity");
-    LAT_CK(cudaSetDevice(h->device));
     const DetectArgs a = detect_args(h);
     const int tNow = (int)((h->n + 1) % 2);
     const int nb = (int)((h->N + detect_block_sites() - 1) / detect_block_sites());
@@ -649,20 +646,47 @@ int lat_detect_crossings(lat_handle* h, int32_t field, double* xyz, int64_t cap,
     long long total = 0;
     LAT_CK(cudaMemcpyAsync(&total, h->det_total, sizeof(total), cudaMemcpyDeviceToHost, h->stream));
     LAT_CK(cudaStreamSynchronize(h->stream));
+    *total_out = total;
+    return LAT_OK;
+}
+
+// write the first nw crossings (after detect_count) into h->det_xyz
+static int detect_write(lat_handle* h, int32_t field, int64_t nw)
+{
+    if (nw <= 0) return LAT_OK;
+    if (nw > h->det_cap) {
+        dev_free(h, (void**)&h->det_xyz, sizeof(double) * 3 * (size_t)h->det_cap);
+        h->det_cap = 0;
+        int rc = dev_alloc(h, (void**)&h->det_xyz, sizeof(double) * 3 * (size_t)nw);
+        if (rc) return rc;
+        h->det_cap = nw;
+    }
+    const DetectArgs a = detect_args(h);
+    const int tNow = (int)((h->n + 1) % 2);
+    const int nb = (int)((h->N + detect_block_sites() - 1) / detect_block_sites());
+    const void* re = h->slot(2 * field, tNow);
+    const void* im = h->slot(2 * field + 1, tNow);
+    if (h->elem == 8)
+        LAT_CKL(launch_detect_write_f64(a, (const double*)re, (const double*)im, h->det_blocks, nb, h->det_xyz, nw, h->stream));
+    else
+        LAT_CKL(launch_detect_write_f32(a, (const float*)re, (const float*)im, h->det_blocks, nb, h->det_xyz, nw, h->stream));
+    return LAT_OK;
+}
+
+int lat_detect_crossings(lat_handle* h, int32_t field, double* xyz, int64_t cap, int64_t* count)
+{
+    LAT_REQUIRE(h && count, "lat_detect_crossings: null argument");
+    LAT_REQUIRE(field == LAT_FIELD_PHI1 || (field == LAT_FIELD_PHI2 && h->p.model == LAT_MODEL_MOORE),
+                "lat_detect_crossings: bad field");
+    LAT_REQUIRE(cap >= 0 && (xyz || cap == 0), "lat_detect_crossings: bad capacity");
+    LAT_CK(cudaSetDevice(h->device));
+    int64_t total = 0;
+    int rc = detect_count(h, field, &total);
+    if (rc) return rc;
     *count = total;
     const int64_t nw = total < cap ? total : cap;
     if (nw > 0) {
-        if (nw > h->det_cap) {
-            dev_free(h, (void**)&h->det_xyz, sizeof(double) * 3 * (size_t)h->det_cap);
-            h->det_cap = 0;
-            int rc = dev_alloc(h, (void**)&h->det_xyz, sizeof(double) * 3 * (size_t)nw);
-            if (rc) return rc;
-            h->det_cap = nw;
-        }
-        if (h->elem == 8)
-            LAT_CKL(launch_detect_write_f64(a, (const double*)re, (const double*)im, h->det_blocks, nb, h->det_xyz, nw, h->stream));
-        else
-            LAT_CKL(launch_detect_write_f32(a, (const float*)re, (const float*)im, h->det_blocks, nb, h->det_xyz, nw, h->stream));
+        if ((rc = detect_write(h, field, nw))) return rc;
         LAT_CK(cudaMemcpyAsync(xyz, h->det_xyz, sizeof(double) * 3 * (size_t)nw, cudaMemcpyDeviceToHost, h->stream));
         LAT_CK(cudaStreamSynchronize(h->stream));
     }
@@ -670,6 +694,41 @@ int lat_detect_crossings(lat_handle* h, int32_t field, double* xyz, int64_t cap,
         set_error("lat_detect_crossings: capacity smaller than the number of crossings");
         return LAT_ERR_CAPACITY;
     }
+    return LAT_OK;
+}
+
+int lat_string_length(lat_handle* h, int32_t field, int32_t split, int32_t method, double* L0, double* L1,
+                      int64_t* count)
+{
+    LAT_REQUIRE(h && L0 && L1, "lat_string_length: null argument");
+    LAT_REQUIRE(field == LAT_FIELD_PHI1 || (field == LAT_FIELD_PHI2 && h->p.model == LAT_MODEL_MOORE),
+                "lat_string_length: bad field");
+    LAT_REQUIRE(method >= LAT_CHAIN_AUTO && method <= LAT_CHAIN_EXHAUSTIVE, "lat_string_length: bad method");
+    const bool periodic = h->p.bc == LAT_BC_PERIODIC;
+    LAT_REQUIRE(method != LAT_CHAIN_HASH || periodic, "lat_string_length: the hash needs a periodic lattice");
+    LAT_CK(cudaSetDevice(h->device));
+    *L0 = *L1 = 0.0;
+    int64_t total = 0;
+    int rc = detect_count(h, field, &total);
+    if (rc) return rc;
+    if (count) *count = total;
+    if (total == 0) return LAT_OK;
+    if ((rc = detect_write(h, field, total))) return rc;
+    if (method == LAT_CHAIN_AUTO) method = periodic ? LAT_CHAIN_HASH : LAT_CHAIN_EXHAUSTIVE;
+    const ChainGeom g = make_chain_geom(h->p, total);
+    const size_t need = chain_workspace_bytes(g, total, method);
+    if (need > h->chain_ws_bytes) {
+        dev_free(h, &h->chain_ws, h->chain_ws_bytes);
+        h->chain_ws_bytes = 0;
+        if ((rc = dev_alloc(h, &h->chain_ws, need))) return rc;
+        h->chain_ws_bytes = need;
+    }
+    double out[2];
+    rc = chain_length_run(g, h->det_xyz, total, split, method, h->chain_ws, h->chain_ws_bytes, h->stream, out,
+                          &h->launches);
+    if (rc) return rc;
+    *L0 = out[0];
+    *L1 = out[1];
     return LAT_OK;
 }
 

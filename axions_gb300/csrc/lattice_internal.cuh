@@ -154,6 +154,32 @@ cudaError_t launch_winding_f64(const DetectArgs&, int fixed, const double* re, c
 cudaError_t launch_winding_f32(const DetectArgs&, int fixed, const float* re, const float* im, int8_t* out,
                                unsigned long long* abs_sum, cudaStream_t);
 
+// ---------------------------------------------------------------------------
+// string length by greedy chaining of crossings (string_length.cu)
+// ---------------------------------------------------------------------------
+struct ChainGeom {
+    double L[3];          // n*d: box side
+    double half[3];       // (0.5*n)*d: minimum-image threshold
+    double quarter[3];    // (0.25*n)*d: half-side of the inner (L0) box
+    double lo[3];         // -x0*d: lower edge of crossing coordinates
+    double w[3];          // hash cell width (>= the cutoff radius)
+    int nb[3];            // hash cells per axis
+    int periodic;
+    double cutoff;        // (dx*dx + dy*dy + dz*dz)^2, compared with squared distances
+    double root_cutoff;   // sqrt(cutoff): the closing length the reference adds
+    int nnb;              // distinct neighbour-cell offsets
+    signed char off[27][3];
+};
+
+ChainGeom make_chain_geom(const lat_params& p, int64_t M);
+// points lie in the box the hash covers (finite, within [lo, lo+L] per axis)
+bool chain_points_in_box(const ChainGeom& g, const double* xyz_host, int64_t M);
+size_t chain_workspace_bytes(const ChainGeom& g, int64_t M, int method);
+// Chaining of the M crossings at d_xyz (device, [M][3]).  method: LAT_CHAIN_*
+// (resolved, not AUTO).  out[0..1] = L0, L1 (host).  Returns a LAT_* status.
+int chain_length_run(const ChainGeom& g, const double* d_xyz, int64_t M, int split, int method, void* ws,
+                     size_t ws_bytes, cudaStream_t st, double* out, int64_t* launches);
+
 // error reporting
 void set_error(const std::string& msg);
 

@@ -27,7 +27,8 @@ EXPORTS = [
     "lat_set_stream", "lat_get_params", "lat_num_components", "lat_time_step", "lat_device_bytes",
     "lat_kernel_launches",
     "lat_set_state", "lat_get_state", "lat_step", "lat_step_diag", "lat_advance", "lat_diagnostics",
-    "lat_detect_crossings", "lat_winding", "lat_ah_step_f64_noalloc",
+    "lat_detect_crossings", "lat_winding", "lat_string_length", "lat_string_length_points",
+    "lat_ah_step_f64_noalloc",
     "lat_batch_create", "lat_batch_destroy", "lat_batch_add", "lat_batch_remove", "lat_batch_size",
     "lat_batch_kernel_launches", "lat_batch_advance", "lat_batch_take_diags",
     "lat_random_phase_ic_device", "lat_philox4x32_10", "lat_autotune", "lat_get_tuning", "lat_set_tuning",
@@ -91,6 +92,8 @@ def load_library(path: Path | None = None):
     L.lat_diagnostics.argtypes = [vp, P(LatDiag)]
     L.lat_detect_crossings.argtypes = [vp, ctypes.c_int32, dp, ctypes.c_int64, P(ctypes.c_int64)]
     L.lat_winding.argtypes = [vp, ctypes.c_int32, P(ctypes.c_int8), P(ctypes.c_int64)]
+    L.lat_string_length.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, dp, dp, P(ctypes.c_int64)]
+    L.lat_string_length_points.argtypes = [P(LatParams), dp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, dp, dp]
     L.lat_ah_step_f64_noalloc.argtypes = [P(LatParams), vp, ctypes.c_int64, ctypes.c_int32, vp]
     L.lat_batch_create.argtypes = [ctypes.c_int32, P(vp)]
     L.lat_batch_destroy.argtypes = [vp]
@@ -304,6 +307,14 @@ class Lattice:
         _check("lat_winding", self.L.lat_winding(self.h, int(field), ptr, ctypes.byref(tot)))
         return out, int(tot.value)
 
+    def string_length(self, field: int = 0, split: bool = True, method: int = 0):
+        """(L0, L1, crossings): greedy chaining of the current level's crossings
+        (lat_string_length; ic_w_evolution.cpp:961-1087)."""
+        L0, L1, cnt = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_int64(0)
+        _check("lat_string_length", self.L.lat_string_length(self.h, int(field), int(bool(split)), int(method),
+                                                             ctypes.byref(L0), ctypes.byref(L1), ctypes.byref(cnt)))
+        return L0.value, L1.value, int(cnt.value)
+
 
 class Batch:
     """Many FP32 lattices advanced together (lat_batch_* of the C ABI).
@@ -398,6 +409,20 @@ class ServerStats(ctypes.Structure):
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+CHAIN_AUTO, CHAIN_HASH, CHAIN_EXHAUSTIVE = 0, 1, 2
+
+
+def string_length_points(p: LatParams, xyz: np.ndarray, split: bool = True, method: int = CHAIN_AUTO):
+    """(L0, L1) of a host crossing list chained on the current device (lat_string_length_points)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    L0, L1 = ctypes.c_double(0), ctypes.c_double(0)
+    ptr = _dp(xyz) if len(xyz) else None
+    _check("lat_string_length_points",
+           load_library().lat_string_length_points(ctypes.byref(p), ptr, len(xyz), int(bool(split)), int(method),
+                                                   ctypes.byref(L0), ctypes.byref(L1)))
+    return L0.value, L1.value
 
 
 def footprint_bytes(p: LatParams) -> int:

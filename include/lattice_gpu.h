@@ -216,6 +216,38 @@ int lat_detect_crossings(lat_handle* h, int32_t field, double* xyz, int64_t cap,
  * the lattice are 0. */
 int lat_winding(lat_handle* h, int32_t field, int8_t* out, int64_t* abs_sum);
 
+/* Total string length by greedy chaining of crossings; replaces
+ * ic_w_evolution.cpp:961-1087 (stringLength[0], stringLength[1]).
+ * From the current crossing the nearest remaining one whose squared distance
+ * is <= (dx^2+dy^2+dz^2)^2 is next (the last of equally near ones wins); its
+ * distance is added.  Per axis the separation |a-b| is used when it is at most
+ * half the box, else box-|a-b| on a periodic lattice and 0 on a fixed one (as
+ * the reference does).  With none in reach the chain closes onto its first
+ * crossing if that is in reach, adding sqrt((dx^2+dy^2+dz^2)^2) as the
+ * reference does, and restarts at the lowest remaining index.  With split != 0
+ * a step counts to *L0 when the crossing it leaves lies in the central box
+ * |x| <= nx*dx/4 (same for y, z) and to *L1 otherwise; with split == 0 all goes
+ * to *L0.  The result equals the reference's bit for bit on the same crossing
+ * list.  method: LAT_CHAIN_HASH walks the linked components of a periodic
+ * lattice in parallel through a cell hash; LAT_CHAIN_EXHAUSTIVE is one thread
+ * block testing every remaining crossing per step (any lattice; the fixed-wall
+ * rule above links crossings across the box, so fixed lattices use it);
+ * LAT_CHAIN_AUTO picks. */
+#define LAT_CHAIN_AUTO        0
+#define LAT_CHAIN_HASH        1
+#define LAT_CHAIN_EXHAUSTIVE  2
+
+/* Crossings of scalar `field` on the current level (as lat_detect_crossings,
+ * kept on the device) chained as above.  count (may be NULL) = crossings. */
+int lat_string_length(lat_handle* h, int32_t field, int32_t split, int32_t method, double* L0, double* L1,
+                      int64_t* count);
+
+/* The same chaining for M host crossings xyz[3*M] on the geometry of p (nx..nz,
+ * dx..dz, bc), on the current CUDA device.  LAT_CHAIN_HASH needs a periodic
+ * lattice and every point inside the box ((i-x0)*dx coordinates). */
+int lat_string_length_points(const lat_params* p, const double* xyz, int64_t M, int32_t split, int32_t method,
+                             double* L0, double* L1);
+
 /* ---- device-side random-phase IC ------------------------------------------------
  * The physics of lat_random_phase_ic (phi = eta*e^{i phase}, phase uniform in
  * [0, 2 pi), both levels equal, theta = 0, TimeStep 0) drawn on the GPU with
