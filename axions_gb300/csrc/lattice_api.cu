@@ -325,7 +325,7 @@ int lat_destroy(lat_handle* h)
     cudaFree(h->det_xyz);
     cudaFree(h->wind);
     cudaFree(h->wind_sum);
-    cudaFree(h->chain_ws);
+    chain_buffers_release(h->chain, nullptr);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
     return LAT_OK;
@@ -716,16 +716,8 @@ int lat_string_length(lat_handle* h, int32_t field, int32_t split, int32_t metho
     if ((rc = detect_write(h, field, total))) return rc;
     if (method == LAT_CHAIN_AUTO) method = periodic ? LAT_CHAIN_HASH : LAT_CHAIN_EXHAUSTIVE;
     const ChainGeom g = make_chain_geom(h->p, total);
-    const size_t need = chain_workspace_bytes(g, total, method);
-    if (need > h->chain_ws_bytes) {
-        dev_free(h, &h->chain_ws, h->chain_ws_bytes);
-        h->chain_ws_bytes = 0;
-        if ((rc = dev_alloc(h, &h->chain_ws, need))) return rc;
-        h->chain_ws_bytes = need;
-    }
     double out[2];
-    rc = chain_length_run(g, h->det_xyz, total, split, method, h->chain_ws, h->chain_ws_bytes, h->stream, out,
-                          &h->launches);
+    rc = chain_length_run(g, h->det_xyz, total, split, method, h->chain, &h->bytes, h->stream, out, &h->launches);
     if (rc) return rc;
     *L0 = out[0];
     *L1 = out[1];

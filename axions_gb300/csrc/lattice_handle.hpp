@@ -37,8 +37,7 @@ struct lat_handle {
     int64_t det_cap = 0;
     int8_t* wind = nullptr;
     unsigned long long* wind_sum = nullptr;
-    void* chain_ws = nullptr;  // string-length workspace
-    size_t chain_ws_bytes = 0;
+    lat::ChainBuffers chain;   // string-length buffers
     int64_t bytes = 0;
     int64_t launches = 0;      // kernels launched by this handle
 

@@ -174,11 +174,19 @@ struct ChainGeom {
 ChainGeom make_chain_geom(const lat_params& p, int64_t M);
 // points lie in the box the hash covers (finite, within [lo, lo+L] per axis)
 bool chain_points_in_box(const ChainGeom& g, const double* xyz_host, int64_t M);
-size_t chain_workspace_bytes(const ChainGeom& g, int64_t M, int method);
-// Chaining of the M crossings at d_xyz (device, [M][3]).  method: LAT_CHAIN_*
-// (resolved, not AUTO).  out[0..1] = L0, L1 (host).  Returns a LAT_* status.
-int chain_length_run(const ChainGeom& g, const double* d_xyz, int64_t M, int split, int method, void* ws,
-                     size_t ws_bytes, cudaStream_t st, double* out, int64_t* launches);
+// device buffers of the chaining, kept between calls (grown as needed)
+struct ChainBuffers {
+    void* ws = nullptr;
+    size_t ws_bytes = 0;
+    void* edges = nullptr;  // links between crossings
+    size_t edge_bytes = 0;
+};
+void chain_buffers_release(ChainBuffers& b, int64_t* held);
+// Chaining of the M crossings at d_xyz (device, [M][3]).  method: LAT_CHAIN_HASH
+// or LAT_CHAIN_EXHAUSTIVE.  Buffers grow as needed (`held`, may be NULL, counts
+// their bytes).  out[0..1] = L0, L1 (host).  Returns a LAT_* status.
+int chain_length_run(const ChainGeom& g, const double* d_xyz, int64_t M, int split, int method, ChainBuffers& buf,
+                     int64_t* held, cudaStream_t st, double* out, int64_t* launches);
 
 // error reporting
 void set_error(const std::string& msg);

@@ -9,20 +9,30 @@
 // restarts at the lowest remaining index.
 //
 // GPU form, exact on the same crossing list:
-//   * Crossings within the cutoff of each other are linked.  A chain never
-//     leaves a connected component of that graph, and a restart takes the
-//     lowest remaining index, which is also its component's lowest remaining
-//     index.  So each component's walk is independent of the others: one warp
-//     walks one component, finding neighbours through a cell hash whose cells
-//     are at least the cutoff radius wide (periodic lattices).
+//   * Periodic lattice.  Crossings within the cutoff of each other are linked;
+//     a chain never leaves a connected component of that graph, and a restart
+//     takes the lowest remaining index, which is also its component's lowest
+//     remaining index, so components are walked independently.  The links are
+//     built once, in parallel, through a cell hash whose cells are at least the
+//     cutoff radius wide: per crossing a list of (neighbour, squared distance,
+//     the neighbour's own list, the slot of the reverse link).  One warp walks
+//     one component over these lists.  A step reads the current crossing's list
+//     and the dead marks of its entries in one memory round trip, picks the
+//     nearest live neighbour by comparing the squared distances' bit patterns
+//     (non-negative doubles order like their bits), and marks dead the reverse
+//     links of the crossing it leaves.  No floating point is done in the walk.
 //   * The reference visits chains in increasing order of their first index.
 //     Each visit is recorded with its chain's first index and its place in the
 //     chain; a scan of the chain lengths places every visit in the reference's
-//     order and one warp adds the lengths in that order, so L0 and L1 are the
-//     reference's doubles bit for bit.
-//   * On a fixed lattice a separation above half the box counts as 0 on that
-//     axis, which links crossings across the box; there one CTA walks all
-//     crossings, testing every remaining one per step.
+//     order, square roots are taken there in parallel, and one warp adds the
+//     lengths in that order, so L0 and L1 are the reference's doubles bit for
+//     bit.
+//   * Any lattice (on a fixed lattice a separation above half the box counts as
+//     0 on that axis, which links crossings across the box): a cooperative grid
+//     follows the reference's loop directly.  Each CTA owns a slice of the
+//     crossings; per step it publishes its slice's nearest live candidate and
+//     lowest live index, and after one grid barrier (a bounded wait) every CTA
+//     reduces the same winner.
 // Compiled with -fmad=false: distances use the reference's unfused products.
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -41,49 +51,71 @@ constexpr int SCAN_T = 1024;            // threads of a scan block
 constexpr int SCAN_I = 4;               // items per scan thread
 constexpr int SCAN_CHUNK = SCAN_T * SCAN_I;
 constexpr int WALK_WARPS = 4;           // warps per walk block
-constexpr int EX_T = 1024;              // threads of the exhaustive walk
+constexpr int EX_T = 512;               // threads per CTA of the cooperative walk
+constexpr int UNROLL = 4;
 constexpr unsigned FULL = 0xffffffffu;
 
 struct ChainPt {
     double x, y, z;
     int idx;
-    int pad;
+    int bin;  // hash cell
+};
+
+// a link i -> j of the crossing graph
+struct AdjEdge {
+    unsigned long long d2;  // bits of the squared distance (a non-negative double)
+    long long start;        // first link of j
+    long long rev;          // slot of the link j -> i
+    int j;
+    int meta;               // number of links of j | inner(j) << 31
 };
 
 // error codes left in counters[2]
 constexpr int CHAIN_ERR_UNION = 1;     // union-find retry bound reached
 constexpr int CHAIN_ERR_RESTART = 2;   // no remaining member where one must be
-constexpr int CHAIN_ERR_LINK = 3;      // a component's last member found a neighbour
+constexpr int CHAIN_ERR_LINK = 3;      // the link graph is not symmetric, or a walk outran its component
+constexpr int CHAIN_ERR_BARRIER = 4;   // a grid barrier wait gave up
 
 struct ChainDev {
     ChainGeom g;
-    const double* xyz;      // [M][3]
+    const double* xyz;        // [M][3]
     int M;
     int split;
     int nbins;
-    int* bin_of;            // [M]
-    int* bin_cnt;           // [nbins] counts, then fill cursors
-    long long* bin_start;   // [nbins + 1]
-    ChainPt* sp;            // [M] crossings sorted by cell
-    int* spos;              // [M] sorted position of each crossing
-    int* parent;            // [M] union-find forest
-    int* comp;              // [M] the component's lowest index
-    int* csize;             // [M] component sizes (at the component's lowest index)
-    int* roots;             // [M]
-    unsigned char* alive_o; // [M] by index
-    unsigned char* alive_s; // [M] by sorted position
-    double* rec_val;        // [M] length added when leaving crossing i
-    unsigned char* rec_cls; // [M] 0: L0, 1: L1, 2: nothing
-    int* rec_start;         // [M] first index of i's chain
-    int* rec_pos;           // [M] place of i in its chain
-    int* chain_len;         // [M] chain lengths at their first index, else 0
-    long long* chain_off;   // [M] exclusive scan of chain_len
-    double* ord_val;        // [M] visits in the reference's order
-    unsigned char* ord_cls; // [M]
-    long long* scan_tot;    // [scan blocks]
-    long long* scan_sum;    // [1]
-    int* counters;          // [0] roots, [1] queue head, [2] error
-    double* out;            // [2] L0, L1
+    // cell hash and links
+    int* bin_of;              // [M]
+    int* bin_cnt;             // [nbins] counts, then fill cursors
+    long long* bin_start;     // [nbins + 1]
+    ChainPt* sp;              // [M] crossings sorted by cell
+    unsigned char* inner;     // [M] inside the central quarter box
+    int* deg;                 // [M] links per crossing
+    long long* adj_start;     // [M + 1]
+    AdjEdge* adj;             // [E]
+    unsigned char* edge_dead; // [E] the link's far end has been left
+    // components
+    int* parent;              // [M] union-find forest
+    int* comp;                // [M] the component's lowest index
+    int* csize;               // [M] component sizes (at the component's lowest index)
+    int* roots;               // [M]
+    unsigned char* alive_o;   // [M]
+    // visits
+    double* rec_d2;           // [M] squared length added when leaving crossing i
+    unsigned char* rec_cls;   // [M] 0: L0, 1: L1, 2: nothing
+    int* rec_start;           // [M] first index of i's chain
+    int* rec_pos;             // [M] place of i in its chain
+    int* chain_len;           // [M] chain lengths at their first index, else 0
+    long long* chain_off;     // [M] exclusive scan of chain_len
+    double* ord_val;          // [M] visits in the reference's order
+    unsigned char* ord_cls;   // [M]
+    long long* scan_tot;      // [scan blocks]
+    long long* scan_sum;      // [1]
+    // cooperative walk
+    double* slot_d2;          // [2][grid]
+    int* slot_j;              // [2][grid]
+    int* slot_min;            // [2][grid]
+    unsigned* bar;            // [2] arrivals, generation
+    int* counters;            // [0] roots, [1] queue head, [2] error
+    double* out;              // [2] L0, L1
 };
 
 // ---------------------------------------------------------------------------
@@ -247,6 +279,7 @@ __global__ void bin_count_kernel(const ChainDev c)
     const int b = (ix * c.g.nb[1] + iy) * c.g.nb[2] + iz;
     c.bin_of[i] = b;
     atomicAdd(&c.bin_cnt[b], 1);
+    c.inner[i] = chain_inner(c.g, p[0], p[1], p[2]) ? 1 : 0;
     c.parent[i] = i;
     c.csize[i] = 0;
     c.chain_len[i] = 0;
@@ -266,10 +299,41 @@ __global__ void bin_scatter_kernel(const ChainDev c)
     s.y = p[1];
     s.z = p[2];
     s.idx = i;
-    s.pad = 0;
+    s.bin = b;
     c.sp[q] = s;
-    c.spos[i] = (int)q;
-    c.alive_s[q] = 1;
+}
+
+// fn(j, d2) for every crossing j != i within the cutoff of crossing i
+template <class F>
+__device__ __forceinline__ void for_links(const ChainDev& c, int i, F&& fn)
+{
+    const double* p = c.xyz + 3 * (size_t)i;
+    const double x = p[0], y = p[1], z = p[2];
+    const int b = c.bin_of[i];
+    const int iz = b % c.g.nb[2], t = b / c.g.nb[2];
+    const int iy = t % c.g.nb[1], ix = t / c.g.nb[1];
+    for (int k = 0; k < c.g.nnb; ++k) {
+        const int jx = wrap_cell(ix + c.g.off[k][0], c.g.nb[0]);
+        const int jy = wrap_cell(iy + c.g.off[k][1], c.g.nb[1]);
+        const int jz = wrap_cell(iz + c.g.off[k][2], c.g.nb[2]);
+        const int nb = (jx * c.g.nb[1] + jy) * c.g.nb[2] + jz;
+        const long long q1 = c.bin_start[nb + 1];
+        for (long long q = c.bin_start[nb]; q < q1; ++q) {
+            const ChainPt s = c.sp[q];
+            if (s.idx == i) continue;
+            const double d = chain_d2(c.g, x, y, z, s.x, s.y, s.z);
+            if (d <= c.g.cutoff) fn(s.idx, d);
+        }
+    }
+}
+
+__global__ void adj_count_kernel(const ChainDev c)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.M) return;
+    int n = 0;
+    for_links(c, i, [&](int, double) { ++n; });
+    c.deg[i] = n;
 }
 
 // ---------------------------------------------------------------------------
@@ -305,26 +369,45 @@ __device__ void unite(int* parent, int a, int b, int* err)
     atomicExch(err, CHAIN_ERR_UNION);
 }
 
-__global__ void union_kernel(const ChainDev c)
+// the links of i, in the order adj_count_kernel counted them; joins the sets
+__global__ void adj_fill_kernel(const ChainDev c)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.M) return;
-    const double* p = c.xyz + 3 * (size_t)i;
-    const double x = p[0], y = p[1], z = p[2];
-    const int b = c.bin_of[i];
-    const int iz = b % c.g.nb[2], t = b / c.g.nb[2];
-    const int iy = t % c.g.nb[1], ix = t / c.g.nb[1];
-    for (int k = 0; k < c.g.nnb; ++k) {
-        const int jx = wrap_cell(ix + c.g.off[k][0], c.g.nb[0]);
-        const int jy = wrap_cell(iy + c.g.off[k][1], c.g.nb[1]);
-        const int jz = wrap_cell(iz + c.g.off[k][2], c.g.nb[2]);
-        const int nb = (jx * c.g.nb[1] + jy) * c.g.nb[2] + jz;
-        const long long q1 = c.bin_start[nb + 1];
-        for (long long q = c.bin_start[nb]; q < q1; ++q) {
-            const ChainPt s = c.sp[q];
-            if (s.idx <= i) continue;
-            if (chain_d2(c.g, x, y, z, s.x, s.y, s.z) <= c.g.cutoff) unite(c.parent, i, s.idx, &c.counters[2]);
-        }
+    long long pos = c.adj_start[i];
+    for_links(c, i, [&](int j, double d) {
+        AdjEdge e;
+        e.d2 = (unsigned long long)__double_as_longlong(d);
+        e.start = 0;
+        e.rev = -1;
+        e.j = j;
+        e.meta = 0;
+        c.adj[pos] = e;
+        c.edge_dead[pos] = 0;
+        ++pos;
+        if (j > i) unite(c.parent, i, j, &c.counters[2]);
+    });
+}
+
+// where each link's far end keeps its own links, and the reverse link
+__global__ void adj_link_kernel(const ChainDev c)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.M) return;
+    const long long k1 = c.adj_start[i + 1];
+    for (long long k = c.adj_start[i]; k < k1; ++k) {
+        const int j = c.adj[k].j;
+        const long long s = c.adj_start[j], n = c.deg[j];
+        long long rev = -1;
+        for (long long q = s; q < s + n; ++q)
+            if (c.adj[q].j == i) {
+                rev = q;
+                break;
+            }
+        if (rev < 0) atomicExch(&c.counters[2], CHAIN_ERR_LINK);
+        c.adj[k].start = s;
+        c.adj[k].rev = rev < 0 ? k : rev;
+        c.adj[k].meta = (int)((unsigned)n | ((unsigned)c.inner[j] << 31));
     }
 }
 
@@ -339,14 +422,15 @@ __global__ void flatten_kernel(const ChainDev c)
 }
 
 // ---------------------------------------------------------------------------
-// one warp walks one component; visits are recorded, not summed
+// one warp walks one component over the links; visits are recorded, not
+// summed.  Dead marks are read through L2 (ld.global.cg): the lanes of this
+// warp set them, __syncwarp orders the steps.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(32 * WALK_WARPS) walk_kernel(const ChainDev c)
 {
     const int lane = threadIdx.x & 31;
-    volatile unsigned char* alive_o = c.alive_o;
-    volatile unsigned char* alive_s = c.alive_s;
     const int nroots = c.counters[0];
+    const unsigned long long cut = (unsigned long long)__double_as_longlong(c.g.cutoff);
     for (;;) {
         int qi = 0;
         if (lane == 0) qi = atomicAdd(&c.counters[1], 1);
@@ -355,64 +439,85 @@ __global__ void __launch_bounds__(32 * WALK_WARPS) walk_kernel(const ChainDev c)
         const int r = c.roots[qi];
         const int S = c.csize[r];
         int f = r, start = r, pos = 0;
+        long long s0 = c.adj_start[r];
+        int n0 = c.deg[r];
+        int inner_f = c.inner[r];
         double bx = c.xyz[3 * (size_t)r], by = c.xyz[3 * (size_t)r + 1], bz = c.xyz[3 * (size_t)r + 2];
         bool found = false;
         for (int it = 0; it < S; ++it) {
-            const double fx = c.xyz[3 * (size_t)f], fy = c.xyz[3 * (size_t)f + 1], fz = c.xyz[3 * (size_t)f + 2];
-            double best = c.g.cutoff;
+            unsigned long long best = cut;
             int bj = -1;
-            if (lane < c.g.nnb) {
-                const int b = c.bin_of[f];
-                const int iz = b % c.g.nb[2], t = b / c.g.nb[2];
-                const int iy = t % c.g.nb[1], ix = t / c.g.nb[1];
-                const int jx = wrap_cell(ix + c.g.off[lane][0], c.g.nb[0]);
-                const int jy = wrap_cell(iy + c.g.off[lane][1], c.g.nb[1]);
-                const int jz = wrap_cell(iz + c.g.off[lane][2], c.g.nb[2]);
-                const int nb = (jx * c.g.nb[1] + jy) * c.g.nb[2] + jz;
-                const long long q1 = c.bin_start[nb + 1];
-                for (long long q = c.bin_start[nb]; q < q1; ++q) {
-                    if (!alive_s[q]) continue;
-                    const ChainPt s = c.sp[q];
-                    if (s.idx == f) continue;
-                    better(best, bj, chain_d2(c.g, fx, fy, fz, s.x, s.y, s.z), s.idx);
+            long long wstart = 0;
+            int wmeta = 0;
+            for (int k = lane; k < n0; k += 32) {
+                const AdjEdge e = c.adj[s0 + k];
+                const unsigned char dead = __ldcg(c.edge_dead + s0 + k);
+                c.edge_dead[e.rev] = 1;  // f is left: the link back to it dies
+                if (dead) continue;
+                if (e.d2 < best || (e.d2 == best && e.j > bj)) {
+                    best = e.d2;
+                    bj = e.j;
+                    wstart = e.start;
+                    wmeta = e.meta;
                 }
             }
-            warp_best(best, bj);
+            const int my_bj = bj;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                const unsigned long long ob = __shfl_xor_sync(FULL, best, o);
+                const int oj = __shfl_xor_sync(FULL, bj, o);
+                if (ob < best || (ob == best && oj > bj)) {
+                    best = ob;
+                    bj = oj;
+                }
+            }
             found = bj >= 0;
+            long long ns0 = 0;
+            int nmeta = 0;
+            if (found) {
+                const int src = __ffs(__ballot_sync(FULL, my_bj == bj)) - 1;
+                ns0 = __shfl_sync(FULL, wstart, src);
+                nmeta = __shfl_sync(FULL, wmeta, src);
+            }
             if (lane == 0) {
-                const unsigned char side = (c.split && !chain_inner(c.g, fx, fy, fz)) ? 1 : 0;
-                double v = 0.0;
+                const unsigned char side = (c.split && !inner_f) ? 1 : 0;
+                double d2 = 0.0;
                 unsigned char cls = 2;
                 if (found) {
-                    v = sqrt(best);
+                    d2 = __longlong_as_double((long long)best);
                     cls = side;
-                } else if (chain_d2(c.g, fx, fy, fz, bx, by, bz) <= c.g.cutoff) {
-                    v = c.g.root_cutoff;
-                    cls = side;
+                } else {
+                    const double* pf = c.xyz + 3 * (size_t)f;
+                    if (chain_d2(c.g, pf[0], pf[1], pf[2], bx, by, bz) <= c.g.cutoff) {
+                        d2 = c.g.cutoff;
+                        cls = side;
+                    }
                 }
-                c.rec_val[f] = v;
+                c.rec_d2[f] = d2;
                 c.rec_cls[f] = cls;
                 c.rec_start[f] = start;
                 c.rec_pos[f] = pos;
-                alive_o[f] = 0;
-                alive_s[c.spos[f]] = 0;
+                c.alive_o[f] = 0;
                 if (!found) c.chain_len[start] = pos + 1;
             }
             __syncwarp();
             if (found) {
                 f = bj;
+                s0 = ns0;
+                n0 = nmeta & 0x7fffffff;
+                inner_f = (int)((unsigned)nmeta >> 31);
                 ++pos;
                 continue;
             }
             if (it + 1 >= S) break;
             // restart at the component's lowest remaining index (above start)
             int nf = -1;
-            for (int cur = start + 1; cur < c.M; cur += 32) {
-                const int i = cur + lane;
-                const bool ok = i < c.M && c.comp[i] == r && alive_o[i];
+            for (int cu = start + 1; cu < c.M; cu += 32) {
+                const int i = cu + lane;
+                const bool ok = i < c.M && c.comp[i] == r && __ldcg(c.alive_o + i);
                 const unsigned m = __ballot_sync(FULL, ok);
                 if (m) {
-                    nf = cur + __ffs(m) - 1;
+                    nf = cu + __ffs(m) - 1;
                     break;
                 }
             }
@@ -422,6 +527,9 @@ __global__ void __launch_bounds__(32 * WALK_WARPS) walk_kernel(const ChainDev c)
             }
             f = start = nf;
             pos = 0;
+            s0 = c.adj_start[f];
+            n0 = c.deg[f];
+            inner_f = c.inner[f];
             bx = c.xyz[3 * (size_t)f];
             by = c.xyz[3 * (size_t)f + 1];
             bz = c.xyz[3 * (size_t)f + 2];
@@ -430,15 +538,16 @@ __global__ void __launch_bounds__(32 * WALK_WARPS) walk_kernel(const ChainDev c)
     }
 }
 
-// every visit's place in the reference's order: chains by first index, then
-// by place in the chain
+// every visit's place in the reference's order (chains by first index, then by
+// place in the chain) and its length
 __global__ void order_kernel(const ChainDev c)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.M) return;
     const long long o = c.chain_off[c.rec_start[i]] + c.rec_pos[i];
-    c.ord_val[o] = c.rec_val[i];
-    c.ord_cls[o] = c.rec_cls[i];
+    const unsigned char cls = c.rec_cls[i];
+    c.ord_val[o] = cls == 2 ? 0.0 : sqrt(c.rec_d2[i]);
+    c.ord_cls[o] = cls;
 }
 
 // the sums in the reference's order (one warp; every lane keeps the same sums)
@@ -469,83 +578,145 @@ __global__ void __launch_bounds__(32) sum_kernel(const ChainDev c)
 }
 
 // ---------------------------------------------------------------------------
-// exhaustive walk: one CTA follows the reference's loop directly, testing all
-// remaining crossings per step (any lattice)
+// cooperative walk over all crossings (any lattice)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(EX_T) walk_exhaustive_kernel(const ChainDev c)
+// Grid barrier for a cooperative launch (all CTAs resident).  The wait is
+// bounded: after about a second it records CHAIN_ERR_BARRIER and every CTA
+// leaves at its next barrier.  Returns false once an error is recorded.
+__device__ bool grid_barrier(unsigned* bar, int* err)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* vgen = bar + 1;
+        const unsigned gen = *vgen;
+        __threadfence();
+        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long spins = 0;
+            while (*vgen == gen) {
+                if (++spins > (1LL << 24)) {
+                    atomicExch(err, CHAIN_ERR_BARRIER);
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int*)err == 0;
+}
+
+__global__ void __launch_bounds__(EX_T) walk_coop_kernel(const ChainDev c)
 {
     __shared__ double s_best[EX_T / 32];
     __shared__ int s_bj[EX_T / 32];
-    __shared__ int s_next;
+    __shared__ unsigned s_min[EX_T / 32];
+    __shared__ int r_bj, r_min;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    volatile unsigned char* alive = c.alive_o;
-    for (int i = tid; i < c.M; i += EX_T) alive[i] = 1;
-    __syncthreads();
-    int f = 0, start = 0;
+    const int G = gridDim.x, b = blockIdx.x;
+    const int lo = (int)((long long)c.M * b / G), hi = (int)((long long)c.M * (b + 1) / G);
+    for (int i = lo + tid; i < hi; i += EX_T) c.alive_o[i] = 1;
+    int f = 0;
     double bx = c.xyz[0], by = c.xyz[1], bz = c.xyz[2];
-    double L0 = 0.0, L1 = 0.0;  // kept by thread 0
+    double L0 = 0.0, L1 = 0.0;  // kept by thread 0 of CTA 0
+    __syncthreads();
     for (int it = 0; it < c.M; ++it) {
         const double fx = c.xyz[3 * (size_t)f], fy = c.xyz[3 * (size_t)f + 1], fz = c.xyz[3 * (size_t)f + 2];
         double best = c.g.cutoff;
         int bj = -1;
-        for (int j = tid; j < c.M; j += EX_T) {
-            if (j == f || !alive[j]) continue;
-            better(best, bj,
-                   chain_d2(c.g, fx, fy, fz, c.xyz[3 * (size_t)j], c.xyz[3 * (size_t)j + 1], c.xyz[3 * (size_t)j + 2]),
-                   j);
+        unsigned mn = (unsigned)INT_MAX;  // lowest live index other than f
+        for (int j0 = lo + tid; j0 < hi; j0 += EX_T * UNROLL) {
+            unsigned char al[UNROLL];
+            double px[UNROLL], py[UNROLL], pz[UNROLL];
+#pragma unroll
+            for (int u = 0; u < UNROLL; ++u) {
+                const int j = j0 + u * EX_T;
+                al[u] = 0;
+                if (j < hi) {
+                    al[u] = c.alive_o[j];
+                    px[u] = c.xyz[3 * (size_t)j];
+                    py[u] = c.xyz[3 * (size_t)j + 1];
+                    pz[u] = c.xyz[3 * (size_t)j + 2];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < UNROLL; ++u) {
+                const int j = j0 + u * EX_T;
+                if (!al[u] || j == f) continue;
+                mn = min(mn, (unsigned)j);
+                better(best, bj, chain_d2(c.g, fx, fy, fz, px[u], py[u], pz[u]), j);
+            }
         }
         warp_best(best, bj);
+        mn = __reduce_min_sync(FULL, mn);
         if (lane == 0) {
             s_best[wid] = best;
             s_bj[wid] = bj;
+            s_min[wid] = mn;
         }
         __syncthreads();
         if (wid == 0) {
-            best = s_best[lane];
-            bj = s_bj[lane];
+            best = lane < EX_T / 32 ? s_best[lane] : c.g.cutoff;
+            bj = lane < EX_T / 32 ? s_bj[lane] : -1;
+            mn = lane < EX_T / 32 ? s_min[lane] : (unsigned)INT_MAX;
             warp_best(best, bj);
+            mn = __reduce_min_sync(FULL, mn);
             if (lane == 0) {
-                const bool outer = c.split && !chain_inner(c.g, fx, fy, fz);
-                if (bj >= 0) {
-                    if (outer) L1 += sqrt(best);
-                    else L0 += sqrt(best);
-                } else if (chain_d2(c.g, fx, fy, fz, bx, by, bz) <= c.g.cutoff) {
-                    if (outer) L1 += c.g.root_cutoff;
-                    else L0 += c.g.root_cutoff;
+                const int sl = (it & 1) * G + b;
+                c.slot_d2[sl] = best;
+                c.slot_j[sl] = bj;
+                c.slot_min[sl] = (int)mn;
+            }
+        }
+        if (!grid_barrier(c.bar, &c.counters[2])) return;
+        if (wid == 0) {
+            best = c.g.cutoff;
+            bj = -1;
+            mn = (unsigned)INT_MAX;
+            for (int k = lane; k < G; k += 32) {
+                const int sl = (it & 1) * G + k;
+                better(best, bj, __ldcg(c.slot_d2 + sl), __ldcg(c.slot_j + sl));
+                mn = min(mn, (unsigned)__ldcg(c.slot_min + sl));
+            }
+            warp_best(best, bj);
+            mn = __reduce_min_sync(FULL, mn);
+            if (lane == 0) {
+                r_bj = bj;
+                r_min = (int)mn;
+                if (f >= lo && f < hi) c.alive_o[f] = 0;  // f's owner retires it
+                if (b == 0) {
+                    const bool outer = c.split && !chain_inner(c.g, fx, fy, fz);
+                    if (bj >= 0) {
+                        if (outer) L1 += sqrt(best);
+                        else L0 += sqrt(best);
+                    } else if (chain_d2(c.g, fx, fy, fz, bx, by, bz) <= c.g.cutoff) {
+                        if (outer) L1 += c.g.root_cutoff;
+                        else L0 += c.g.root_cutoff;
+                    }
                 }
-                alive[f] = 0;
-                s_next = bj;
             }
         }
         __syncthreads();
-        const int nf = s_next;
-        __syncthreads();  // every thread has read s_next before it is reused
-        if (nf >= 0) {
-            f = nf;
+        const int nbj = r_bj, nmin = r_min;
+        if (nbj >= 0) {
+            f = nbj;
             continue;
         }
         if (it + 1 >= c.M) break;
-        if (tid == 0) s_next = INT_MAX;
-        __syncthreads();
-        int m = INT_MAX;
-        for (int base = start + 1; base < c.M; base += EX_T) {
-            const int i = base + tid;
-            if (i < c.M && alive[i]) atomicMin(&s_next, i);
-            __syncthreads();
-            m = s_next;
-            __syncthreads();
-            if (m != INT_MAX) break;
+        if (nmin == INT_MAX) {
+            if (tid == 0) atomicExch(&c.counters[2], CHAIN_ERR_RESTART);
+            return;
         }
-        if (m == INT_MAX) {
-            if (tid == 0) c.counters[2] = CHAIN_ERR_RESTART;
-            break;
-        }
-        f = start = m;
+        f = nmin;
         bx = c.xyz[3 * (size_t)f];
         by = c.xyz[3 * (size_t)f + 1];
         bz = c.xyz[3 * (size_t)f + 2];
     }
-    if (tid == 0) {
+    if (b == 0 && tid == 0) {
         c.out[0] = L0;
         c.out[1] = L1;
     }
@@ -569,7 +740,8 @@ struct Carver {
 
 long long chain_bins(const ChainGeom& g) { return (long long)g.nb[0] * g.nb[1] * g.nb[2]; }
 
-ChainDev carve(void* ws, const ChainGeom& g, int64_t M, int method, size_t* bytes)
+// everything but the links (sized once their number is known)
+ChainDev carve(void* ws, const ChainGeom& g, int64_t M, int method, int grid, size_t* bytes)
 {
     ChainDev c{};
     Carver k{(char*)ws};
@@ -577,20 +749,26 @@ ChainDev carve(void* ws, const ChainGeom& g, int64_t M, int method, size_t* byte
     c.counters = k.take<int>(4);
     c.out = k.take<double>(2);
     c.alive_o = k.take<unsigned char>(M);
-    if (method == LAT_CHAIN_HASH) {
+    if (method == LAT_CHAIN_EXHAUSTIVE) {
+        c.slot_d2 = k.take<double>(2 * (size_t)grid);
+        c.slot_j = k.take<int>(2 * (size_t)grid);
+        c.slot_min = k.take<int>(2 * (size_t)grid);
+        c.bar = k.take<unsigned>(2);
+    } else {
         const long long nbins = chain_bins(g);
         c.nbins = (int)nbins;
         c.bin_of = k.take<int>(M);
         c.bin_cnt = k.take<int>(nbins);
         c.bin_start = k.take<long long>(nbins + 1);
         c.sp = k.take<ChainPt>(M);
-        c.spos = k.take<int>(M);
+        c.inner = k.take<unsigned char>(M);
+        c.deg = k.take<int>(M);
+        c.adj_start = k.take<long long>(M + 1);
         c.parent = k.take<int>(M);
         c.comp = k.take<int>(M);
         c.csize = k.take<int>(M);
         c.roots = k.take<int>(M);
-        c.alive_s = k.take<unsigned char>(M);
-        c.rec_val = k.take<double>(M);
+        c.rec_d2 = k.take<double>(M);
         c.rec_cls = k.take<unsigned char>(M);
         c.rec_start = k.take<int>(M);
         c.rec_pos = k.take<int>(M);
@@ -598,11 +776,51 @@ ChainDev carve(void* ws, const ChainGeom& g, int64_t M, int method, size_t* byte
         c.chain_off = k.take<long long>(M);
         c.ord_val = k.take<double>(M);
         c.ord_cls = k.take<unsigned char>(M);
-        c.scan_tot = k.take<long long>(std::max(scan_blocks(nbins), scan_blocks(M)));
+        c.scan_tot = k.take<long long>(std::max(scan_blocks(nbins), scan_blocks(M + 1)));
         c.scan_sum = k.take<long long>(1);
     }
     *bytes = k.off;
     return c;
+}
+
+// grow a device buffer to `need` bytes; `held` tracks the bytes held
+int grow(void** p, size_t* have, size_t need, int64_t* held)
+{
+    if (need <= *have && *p) return LAT_OK;
+    if (*p) {
+        cudaFree(*p);
+        if (held) *held -= (int64_t)*have;
+        *p = nullptr;
+        *have = 0;
+    }
+    const size_t want = need ? need : 256;
+    const cudaError_t e = cudaMalloc(p, want);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        set_error(std::string("string length: cudaMalloc: ") + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? LAT_ERR_NOMEM : LAT_ERR_CUDA;
+    }
+    *have = want;
+    if (held) *held += (int64_t)want;
+    return LAT_OK;
+}
+
+// CTAs of the cooperative walk: all resident at once (at most one per SM), at
+// most one per EX_T crossings
+int coop_grid(int64_t M, int* grid)
+{
+    int dev = 0, sms = 0, coop = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, walk_coop_kernel, EX_T, 0);
+    if (e != cudaSuccess || !coop || per_sm < 1) {
+        set_error("string length: the device cannot run the cooperative walk");
+        return LAT_ERR_CUDA;
+    }
+    const int64_t want = std::max<int64_t>(1, (M + EX_T - 1) / EX_T);
+    *grid = (int)std::min<int64_t>(want, (int64_t)sms);
+    return LAT_OK;
 }
 
 }  // namespace
@@ -684,11 +902,13 @@ bool chain_points_in_box(const ChainGeom& g, const double* xyz, int64_t M)
     return true;
 }
 
-size_t chain_workspace_bytes(const ChainGeom& g, int64_t M, int method)
+
+void chain_buffers_release(ChainBuffers& b, int64_t* held)
 {
-    size_t bytes = 0;
-    carve(nullptr, g, M, method, &bytes);
-    return bytes;
+    cudaFree(b.ws);
+    cudaFree(b.edges);
+    if (held) *held -= (int64_t)(b.ws_bytes + b.edge_bytes);
+    b = ChainBuffers{};
 }
 
 #define CH_CK(call)                                                                          \
@@ -700,8 +920,8 @@ size_t chain_workspace_bytes(const ChainGeom& g, int64_t M, int method)
         }                                                                                    \
     } while (0)
 
-int chain_length_run(const ChainGeom& g, const double* d_xyz, int64_t M, int split, int method, void* ws,
-                     size_t ws_bytes, cudaStream_t st, double* out, int64_t* launches)
+int chain_length_run(const ChainGeom& g, const double* d_xyz, int64_t M, int split, int method, ChainBuffers& buf,
+                     int64_t* held, cudaStream_t st, double* out, int64_t* launches)
 {
     out[0] = out[1] = 0.0;
     if (M <= 0) return LAT_OK;
@@ -713,37 +933,49 @@ int chain_length_run(const ChainGeom& g, const double* d_xyz, int64_t M, int spl
         set_error("string length: method must be resolved");
         return LAT_ERR_INVALID;
     }
+    int grid = 1, rc;
+    if (method == LAT_CHAIN_EXHAUSTIVE && (rc = coop_grid(M, &grid))) return rc;
     size_t need = 0;
-    ChainDev c = carve(ws, g, M, method, &need);
-    if (!ws || need > ws_bytes) {
-        set_error("string length: workspace too small");
-        return LAT_ERR_INVALID;
-    }
+    carve(nullptr, g, M, method, grid, &need);
+    if ((rc = grow(&buf.ws, &buf.ws_bytes, need, held))) return rc;
+    ChainDev c = carve(buf.ws, g, M, method, grid, &need);
     c.xyz = d_xyz;
     c.M = (int)M;
     c.split = split ? 1 : 0;
     int64_t nl = 0;
     CH_CK(cudaMemsetAsync(c.counters, 0, 4 * sizeof(int), st));
     if (method == LAT_CHAIN_EXHAUSTIVE) {
-        walk_exhaustive_kernel<<<1, EX_T, 0, st>>>(c);
+        CH_CK(cudaMemsetAsync(c.bar, 0, 2 * sizeof(unsigned), st));
+        void* args[] = {(void*)&c};
+        CH_CK(cudaLaunchCooperativeKernel((const void*)walk_coop_kernel, dim3(grid), dim3(EX_T), args, 0, st));
         ++nl;
     } else {
         const int tb = 256;
-        const int grid = (int)((M + tb - 1) / tb);
+        const int blocks = (int)((M + tb - 1) / tb);
         const size_t cnt_bytes = sizeof(int) * (size_t)c.nbins;
         CH_CK(cudaMemsetAsync(c.bin_cnt, 0, cnt_bytes, st));
-        bin_count_kernel<<<grid, tb, 0, st>>>(c);
+        bin_count_kernel<<<blocks, tb, 0, st>>>(c);
         CH_CK(exclusive_scan(c.bin_cnt, c.nbins, c.bin_start, 1, c.scan_tot, c.scan_sum, st, &nl));
         CH_CK(cudaMemsetAsync(c.bin_cnt, 0, cnt_bytes, st));
-        bin_scatter_kernel<<<grid, tb, 0, st>>>(c);
-        union_kernel<<<grid, tb, 0, st>>>(c);
-        flatten_kernel<<<grid, tb, 0, st>>>(c);
+        bin_scatter_kernel<<<blocks, tb, 0, st>>>(c);
+        adj_count_kernel<<<blocks, tb, 0, st>>>(c);
+        CH_CK(exclusive_scan(c.deg, M, c.adj_start, 1, c.scan_tot, c.scan_sum, st, &nl));
+        long long E = 0;
+        CH_CK(cudaMemcpyAsync(&E, c.adj_start + M, sizeof(E), cudaMemcpyDeviceToHost, st));
+        CH_CK(cudaStreamSynchronize(st));
+        const size_t ebytes = sizeof(AdjEdge) * (size_t)E + 256 + (size_t)E;
+        if ((rc = grow(&buf.edges, &buf.edge_bytes, ebytes, held))) return rc;
+        c.adj = (AdjEdge*)buf.edges;
+        c.edge_dead = (unsigned char*)buf.edges + ((sizeof(AdjEdge) * (size_t)E + 255) & ~(size_t)255);
+        adj_fill_kernel<<<blocks, tb, 0, st>>>(c);
+        adj_link_kernel<<<blocks, tb, 0, st>>>(c);
+        flatten_kernel<<<blocks, tb, 0, st>>>(c);
         const int wgrid = (int)std::min<int64_t>(152 * 8, (M + WALK_WARPS - 1) / WALK_WARPS);
         walk_kernel<<<wgrid, 32 * WALK_WARPS, 0, st>>>(c);
         CH_CK(exclusive_scan(c.chain_len, M, c.chain_off, 0, c.scan_tot, c.scan_sum, st, &nl));
-        order_kernel<<<grid, tb, 0, st>>>(c);
+        order_kernel<<<blocks, tb, 0, st>>>(c);
         sum_kernel<<<1, 32, 0, st>>>(c);
-        nl += 7;
+        nl += 10;
     }
     CH_CK(cudaGetLastError());
     int err = 0;
@@ -753,9 +985,10 @@ int chain_length_run(const ChainGeom& g, const double* d_xyz, int64_t M, int spl
     if (launches) *launches += nl;
     if (err) {
         out[0] = out[1] = 0.0;
-        set_error(err == CHAIN_ERR_UNION ? "string length: union-find retry bound reached"
-                                         : "string length: inconsistent component walk");
-        return err == CHAIN_ERR_UNION ? LAT_ERR_TIMEOUT : LAT_ERR_STATE;
+        set_error(err == CHAIN_ERR_UNION     ? "string length: union-find retry bound reached"
+                  : err == CHAIN_ERR_BARRIER ? "string length: a grid barrier wait timed out"
+                                             : "string length: inconsistent component walk");
+        return (err == CHAIN_ERR_UNION || err == CHAIN_ERR_BARRIER) ? LAT_ERR_TIMEOUT : LAT_ERR_STATE;
     }
     return LAT_OK;
 }
@@ -780,25 +1013,23 @@ extern "C" int lat_string_length_points(const lat_params* p, const double* xyz, 
         return LAT_ERR_INVALID;
     }
     if (method == LAT_CHAIN_AUTO) method = hashable ? LAT_CHAIN_HASH : LAT_CHAIN_EXHAUSTIVE;
-    const size_t ws_bytes = chain_workspace_bytes(g, M, method);
     cudaStream_t st = nullptr;
     double* d_xyz = nullptr;
-    void* ws = nullptr;
+    ChainBuffers buf;
     int rc = LAT_OK;
     double out[2] = {0.0, 0.0};
     cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&d_xyz, sizeof(double) * 3 * (size_t)M);
-    if (e == cudaSuccess) e = cudaMalloc(&ws, ws_bytes);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_xyz, xyz, sizeof(double) * 3 * (size_t)M, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) {
         set_error(std::string("lat_string_length_points: ") + cudaGetErrorString(e));
         rc = e == cudaErrorMemoryAllocation ? LAT_ERR_NOMEM : LAT_ERR_CUDA;
     } else {
-        rc = chain_length_run(g, d_xyz, M, split, method, ws, ws_bytes, st, out, nullptr);
+        rc = chain_length_run(g, d_xyz, M, split, method, buf, nullptr, st, out, nullptr);
     }
     if (st) cudaStreamSynchronize(st);
-    cudaFree(ws);
+    chain_buffers_release(buf, nullptr);
     cudaFree(d_xyz);
     if (st) cudaStreamDestroy(st);
     if (rc == LAT_OK) {
