@@ -71,6 +71,16 @@ def workload_params(n: int, precision: str):
                        scaling=1.0, tau0=1.0, energy_form=ENERGY_EVOLUTION, precision=prec)
 
 
+def global_string_params(n: int, precision: str):
+    """The physics of the reference's string-length program (ic_w_evolution.cpp:
+    23-45): global strings (e = 0), lambda = 1, eta = 1, dx = 0.35, dt = 0.05, no
+    friction, periodic."""
+    from axions_gb300.params import ENERGY_EVOLUTION, F32, F64, make_params
+    prec = {"f64": F64, "f32": F32}[precision]
+    return make_params(0, n=n, d=0.35, dt=0.05, lam=1.0, eta=1.0, g=0.0, damped_nt=0, dampFac=0.0, alpha=0.0,
+                       scaling=1.0, tau0=1.0, energy_form=ENERGY_EVOLUTION, precision=prec)
+
+
 def workload_name(n: int) -> str:
     if MODEL["name"] == "moore":
         return (f"Moore model {n}^3 periodic, phi1/phi2 charges 1/2, eta=1, lambda1=lambda2=2, e=1, dx=0.5, "
@@ -404,43 +414,95 @@ def measure_ensemble(njobs: int, n: int, steps: int, diag_every: int, tick: int)
 
 
 def measure_fp32_accuracy(n: int, steps: int, sample_every: int = 100):
-    """FP32 form against the FP64 path on the same seeded IC (the workload's
-    physics, diagnostics every 20 steps): field L2 drift at the end, the largest
-    relative difference of the energy and of the Gauss residual over the run,
-    and the total string length L = dx * sum |winding| (and the number of
-    bilinear crossings) every `sample_every` steps."""
+    """FP32 form against the FP64 path on the same seeded IC.  The workload's
+    physics (diagnostics every 20 steps): field L2 drift at the end and the
+    largest relative difference of the energy and of the Gauss residual over the
+    run.  The string-length program's physics (global strings, 1000 steps):
+    every 200 steps the total string length by greedy chaining of the crossings
+    (L0 + L1, ic_w_evolution.cpp:961-1087) and the number of crossings.  (With
+    e != 0 the gauge links drift and the reference's detection, which reads phi
+    alone, finds crossings at almost every site after a few hundred steps, so
+    lengths are compared on global strings, as the reference measures them.)"""
     import numpy as np
 
     from axions_gb300 import lattice
-    out = {"lattice": n, "steps": steps, "diag_every": DIAG_EVERY,
-           "string_length": "dx * sum over plaquettes of |winding of phi|"}
+    out = {"lattice": n, "steps": steps, "diag_every": DIAG_EVERY}
     runs = {}
     for prec in ("f64", "f32"):
         p = workload_params(n, prec)
         with lattice.Lattice(p) as lat:
             lat.random_phase_ic_device(2026)
-            diags, lengths, crossings = [], [], []
-            for s0 in range(0, steps, sample_every):
-                diags += lat.advance(min(sample_every, steps - s0), DIAG_EVERY)
-                _, w = lat.winding(0, want_array=False)
-                lengths.append(w * p.dx)
-                crossings.append(len(lat.detect(0)))
+            diags = lat.advance(steps, DIAG_EVERY)
             now, _ = lat.get_state()
-        runs[prec] = (np.array([d[1] for d in diags]), np.array([d[2] for d in diags]), np.array(lengths),
-                      np.array(crossings), now)
-    e64, g64, l64, c64, f64 = runs["f64"]
-    e32, g32, l32, c32, f32 = runs["f32"]
+        runs[prec] = (np.array([d[1] for d in diags]), np.array([d[2] for d in diags]), now)
+    e64, g64, f64 = runs["f64"]
+    e32, g32, f32 = runs["f32"]
     rel = lambda a, b: float(np.max(np.abs(a - b) / np.abs(b)))  # noqa: E731
     out.update({
         "field_l2_drift": float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64)),
         "scalar_l2_drift": float(np.linalg.norm(f32[:2] - f64[:2]) / np.linalg.norm(f64[:2])),
         "energy_rel_max": rel(e32, e64), "energy_rel_final": float(abs(e32[-1] - e64[-1]) / abs(e64[-1])),
         "gauss_rel_max": rel(g32, g64), "gauss_rel_final": float(abs(g32[-1] - g64[-1]) / abs(g64[-1])),
-        "string_length_f64": l64.tolist(), "string_length_f32": l32.tolist(),
-        "string_length_rel_max": rel(l32, l64), "string_length_rel_final": float(abs(l32[-1] - l64[-1]) / l64[-1]),
-        "crossings_f64": c64.tolist(), "crossings_f32": c32.tolist(),
     })
+    gsteps, gevery = 1000, 200
+    lens = {}
+    for prec in ("f64", "f32"):
+        p = global_string_params(n, prec)
+        with lattice.Lattice(p) as lat:
+            lat.random_phase_ic_device(2026)
+            L, M = [], []
+            for s0 in range(0, gsteps, gevery):
+                lat.advance(gevery)
+                L0, L1, m = lat.string_length(0, True)
+                L.append(L0 + L1)
+                M.append(m)
+        lens[prec] = (np.array(L), np.array(M))
+    l64, c64 = lens["f64"]
+    l32, c32 = lens["f32"]
+    out["global_strings"] = {
+        "physics": "e=0, lambda=1, eta=1, dx=0.35, dt=0.05, no friction", "steps": gsteps, "every": gevery,
+        "string_length_f64": l64.tolist(), "string_length_f32": l32.tolist(),
+        "string_length_rel_max": rel(l32, l64), "crossings_f64": c64.tolist(), "crossings_f32": c32.tolist()}
     return out
+
+
+def measure_string_length(n: int, steps: int, cpu_sample: int):
+    """Total string length by greedy chaining (ic_w_evolution.cpp:961-1087) of
+    the crossings of an n^3 lattice of the string-length program's physics after
+    `steps` FP32 steps from a random-phase IC.  GPU: wall time of
+    lat_string_length (detection and chaining on the device, link-graph
+    component walks).  CPU: the O(M^2) restatement of the reference's loop (one
+    thread) timed on the first `cpu_sample` crossings of the same list and
+    scaled by (M / sample)^2 to the full list; the GPU chaining of that sample
+    is checked against it bit for bit."""
+    from axions_gb300 import lattice
+    from oracle import oracle as O
+    p = global_string_params(n, "f32")
+    with lattice.Lattice(p) as lat:
+        lat.random_phase_ic_device(2027)
+        lat.advance(steps)
+        lat.string_length(0, True)  # buffers
+        times = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            L0, L1, M = lat.string_length(0, True)
+            times.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        xyz = lat.detect(0)
+        t_detect = time.perf_counter() - t0
+    sample = xyz[:cpu_sample]
+    t0 = time.perf_counter()
+    c = O.string_length(p, sample, True)
+    t_cpu = time.perf_counter() - t0
+    g = lattice.string_length_points(p, sample, True)
+    t_gpu = min(times)
+    t_ref = t_cpu * (M / max(len(sample), 1)) ** 2
+    return {"lattice": n, "steps": steps, "physics": "e=0, lambda=1, eta=1, dx=0.35, dt=0.05, no friction",
+            "crossings": M, "L0": L0, "L1": L1, "method": "link-graph component walks",
+            "gpu_s": t_gpu, "gpu_crossings_per_s": M / t_gpu, "detect_to_host_s": t_detect,
+            "cpu_sample_crossings": len(sample), "cpu_sample_s": t_cpu, "cpu_kind": "port", "cpu_cores": 1,
+            "cpu_full_s_extrapolated": t_ref, "speedup_vs_cpu_extrapolated": t_ref / t_gpu,
+            "sample_bit_exact": g == c}
 
 
 def measure_serving(njobs: int, rate: float, budget_gb: float, tick: int, seed: int = 4242):
@@ -516,6 +578,10 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy study")
     ap.add_argument("--accuracy-n", type=int, default=256, help="lattice side of the accuracy study (workload: 512)")
     ap.add_argument("--accuracy-steps", type=int, default=1000)
+    ap.add_argument("--no-length", action="store_true", help="skip the string-length measurement")
+    ap.add_argument("--length-n", type=int, default=512)
+    ap.add_argument("--length-steps", type=int, default=600)
+    ap.add_argument("--length-cpu-sample", type=int, default=20000)
     args = ap.parse_args()
     ws, rank, local = dist_env()
     MODEL["name"] = args.model
@@ -587,6 +653,9 @@ def main():
     accuracy = None
     if not args.no_accuracy and args.model == "ah":
         accuracy = measure_fp32_accuracy(args.accuracy_n, args.accuracy_steps)
+    slen = None
+    if not args.no_length and args.model == "ah" and rank == 0:
+        slen = measure_string_length(args.length_n, args.length_steps, args.length_cpu_sample)
     if rank != 0:
         return
     achieved = bytes_per_site(head) * res["sites"] / (res["kern_ms"] * 1e-3) / 1e9
@@ -615,6 +684,7 @@ def main():
         "ensemble": ensemble,
         "serving": serving,
         "fp32_accuracy": accuracy,
+        "string_length": slen,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:
