@@ -617,6 +617,7 @@ def main():
         cpu = {"value": r, "unit": "site-updates/s", "cores": cores, "kind": "port",
                "sample": f"{args.cpu_n}^3 lattice of the same physics, {ns} steps in {el:.1f} s"}
 
+    t_start = time.perf_counter()
     import torch
     torch.cuda.set_device(local)
     dist_init(ws, "nccl")
@@ -644,18 +645,30 @@ def main():
                        "roofline": {"bound": "hbm", "achieved": ach2, "peak": hbm, "unit": "GB/s",
                                     "frac": ach2 / hbm, "traffic": load_traffic(form, n)},
                        "speedup_vs_f64": res["total_ms"] / r2["total_ms"]}
+    def note(leg, t0):
+        print(f"bench: {leg} done in {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
+
+    note("headline and forms", t_start)
+    t_leg = time.perf_counter()
     ensemble = None
     if not args.no_ensemble:
         ensemble = measure_ensemble(args.ensemble_jobs, args.ensemble_n, args.ensemble_steps, DIAG_EVERY, 50)
+    note("ensemble", t_leg)
+    t_leg = time.perf_counter()
     serving = None
     if not args.no_serving:
         serving = measure_serving(args.serving_jobs, args.serving_rate, 96.0, 25)
+    note("serving", t_leg)
+    t_leg = time.perf_counter()
     accuracy = None
     if not args.no_accuracy and args.model == "ah":
         accuracy = measure_fp32_accuracy(args.accuracy_n, args.accuracy_steps)
+    note("accuracy", t_leg)
+    t_leg = time.perf_counter()
     slen = None
     if not args.no_length and args.model == "ah" and rank == 0:
         slen = measure_string_length(args.length_n, args.length_steps, args.length_cpu_sample)
+    note("string length", t_leg)
     if rank != 0:
         return
     achieved = bytes_per_site(head) * res["sites"] / (res["kern_ms"] * 1e-3) / 1e9
