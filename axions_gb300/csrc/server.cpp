@@ -191,6 +191,9 @@ void worker_main(lat_server* s)
             j.res.start_s = s->now();
             s->running.push_back(id);
         }
+        // jobs refused at admission (too large for the budget, no memory) are
+        // finished: wake their waiters before sleeping on new work
+        s->cv_done.notify_all();
         if (s->running.empty()) {
             if (s->stop) break;
             s->cv_work.wait(lock);

@@ -300,6 +300,12 @@ class Lattice:
                    self.L.lat_detect_crossings(self.h, int(field), _dp(xyz), n, ctypes.byref(cnt)))
         return xyz[:n]
 
+    def count_crossings(self, field: int = 0) -> int:
+        """Number of bilinear crossings on the current level (nothing copied)."""
+        cnt = ctypes.c_int64(0)
+        _check("lat_detect_crossings", self.L.lat_detect_crossings(self.h, int(field), None, 0, ctypes.byref(cnt)))
+        return int(cnt.value)
+
     def winding(self, field: int = 0, want_array: bool = True):
         tot = ctypes.c_int64(0)
         out = np.zeros((3, self.N), dtype=np.int8) if want_array else None
