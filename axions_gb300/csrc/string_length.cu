@@ -454,6 +454,9 @@ __global__ void __launch_bounds__(32 * WALK_WARPS) walk_kernel(const ChainDev c)
                 const unsigned char dead = __ldcg(c.edge_dead + s0 + k);
                 c.edge_dead[e.rev] = 1;  // f is left: the link back to it dies
                 if (dead) continue;
+                // a live neighbour may be the next crossing: start fetching its links
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(c.adj + e.start));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(c.edge_dead + e.start));
                 if (e.d2 < best || (e.d2 == best && e.j > bj)) {
                     best = e.d2;
                     bj = e.j;
@@ -550,31 +553,38 @@ __global__ void order_kernel(const ChainDev c)
     c.ord_cls[o] = cls;
 }
 
-// the sums in the reference's order (one warp; every lane keeps the same sums)
+// the sums in the reference's order, by one thread.  Every visit adds to both
+// sums, 0.0 to the one it does not count to (x + 0.0 == x for the non-negative
+// partial sums), so the two dependent chains interleave and the loads of a
+// batch are issued together.
 __global__ void __launch_bounds__(32) sum_kernel(const ChainDev c)
 {
-    const int lane = threadIdx.x & 31;
+    if (threadIdx.x != 0) return;
+    constexpr int B = 16;
     double L0 = 0.0, L1 = 0.0;
-    for (int base = 0; base < c.M; base += 32) {
-        const int i = base + lane;
-        double v = 0.0;
-        int cls = 2;
-        if (i < c.M) {
-            v = c.ord_val[i];
-            cls = c.ord_cls[i];
+    int base = 0;
+    for (; base + B <= c.M; base += B) {
+        double v[B];
+        unsigned char k[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            v[u] = c.ord_val[base + u];
+            k[u] = c.ord_cls[base + u];
         }
-        const int n = min(32, c.M - base);
-        for (int k = 0; k < n; ++k) {
-            const double vk = __shfl_sync(FULL, v, k);
-            const int ck = __shfl_sync(FULL, cls, k);
-            if (ck == 0) L0 += vk;
-            else if (ck == 1) L1 += vk;
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            L0 += k[u] == 0 ? v[u] : 0.0;
+            L1 += k[u] == 1 ? v[u] : 0.0;
         }
     }
-    if (lane == 0) {
-        c.out[0] = L0;
-        c.out[1] = L1;
+    for (; base < c.M; ++base) {
+        const double v = c.ord_val[base];
+        const unsigned char k = c.ord_cls[base];
+        L0 += k == 0 ? v : 0.0;
+        L1 += k == 1 ? v : 0.0;
     }
+    c.out[0] = L0;
+    c.out[1] = L1;
 }
 
 // ---------------------------------------------------------------------------

@@ -72,13 +72,18 @@ def workload_params(n: int, precision: str):
 
 
 def global_string_params(n: int, precision: str):
-    """The physics of the reference's string-length program (ic_w_evolution.cpp:
-    23-45): global strings (e = 0), lambda = 1, eta = 1, dx = 0.35, dt = 0.05, no
-    friction, periodic."""
+    """The reference's default physics (mpi_evolution.cpp:15-60): global strings
+    (e = 0), lambda = 1, eta = 1, dx = 0.25, dt = 0.05, a damping phase of 200
+    steps (0.5), then radiation-era friction (alpha = 3, a ~ tau, tau0 = 1),
+    periodic.  (Without damping or friction a random-phase start in a periodic
+    box keeps its gradient energy and no network forms.)"""
     from axions_gb300.params import ENERGY_EVOLUTION, F32, F64, make_params
     prec = {"f64": F64, "f32": F32}[precision]
-    return make_params(0, n=n, d=0.35, dt=0.05, lam=1.0, eta=1.0, g=0.0, damped_nt=0, dampFac=0.0, alpha=0.0,
+    return make_params(0, n=n, d=0.25, dt=0.05, lam=1.0, eta=1.0, g=0.0, damped_nt=200, dampFac=0.5, alpha=3.0,
                        scaling=1.0, tau0=1.0, energy_form=ENERGY_EVOLUTION, precision=prec)
+
+
+GLOBAL_STRINGS = "e=0, lambda=1, eta=1, dx=0.25, dt=0.05, damped 200 steps (0.5), then alpha=3 friction"
 
 
 def workload_name(n: int) -> str:
@@ -417,8 +422,8 @@ def measure_fp32_accuracy(n: int, steps: int, sample_every: int = 100):
     """FP32 form against the FP64 path on the same seeded IC.  The workload's
     physics (diagnostics every 20 steps): field L2 drift at the end and the
     largest relative difference of the energy and of the Gauss residual over the
-    run.  The string-length program's physics (global strings on 128^3, 2000
-    steps): every 500 steps the total string length by greedy chaining of the crossings
+    run.  Global strings (the reference's default physics, 128^3, 1000 steps):
+    every 250 steps the total string length by greedy chaining of the crossings
     (L0 + L1, ic_w_evolution.cpp:961-1087) and the number of crossings.  (With
     e != 0 the gauge links drift and the reference's detection, which reads phi
     alone, finds crossings at almost every site after a few hundred steps, so
@@ -450,7 +455,7 @@ def measure_fp32_accuracy(n: int, steps: int, sample_every: int = 100):
         "energy_rel_max": rel(e32, e64), "energy_rel_final": float(abs(e32[-1] - e64[-1]) / abs(e64[-1])),
         "gauss_rel_max": rel(g32, g64), "gauss_rel_final": float(abs(g32[-1] - g64[-1]) / abs(g64[-1])),
     })
-    gn, gsteps, gevery = 128, 2000, 500
+    gn, gsteps, gevery = 128, 1000, 250
     lens = {}
     for prec in ("f64", "f32"):
         p = global_string_params(gn, prec)
@@ -466,7 +471,7 @@ def measure_fp32_accuracy(n: int, steps: int, sample_every: int = 100):
     l64, c64 = lens["f64"]
     l32, c32 = lens["f32"]
     out["global_strings"] = {
-        "physics": "e=0, lambda=1, eta=1, dx=0.35, dt=0.05, no friction", "lattice": gn, "steps": gsteps,
+        "physics": GLOBAL_STRINGS, "lattice": gn, "steps": gsteps,
         "every": gevery,
         "string_length_f64": l64.tolist(), "string_length_f32": l32.tolist(),
         "string_length_rel_max": rel(l32, l64), "crossings_f64": c64.tolist(), "crossings_f32": c32.tolist()}
@@ -475,7 +480,8 @@ def measure_fp32_accuracy(n: int, steps: int, sample_every: int = 100):
 
 def measure_string_length(n: int, max_steps: int, max_crossings: int, cpu_sample: int):
     """Total string length by greedy chaining (ic_w_evolution.cpp:961-1087) of
-    the crossings of an n^3 lattice of the string-length program's physics,
+    the crossings of an n^3 lattice of global strings (the reference's default
+    physics),
     evolved in FP32 from a random-phase IC in blocks of 250 steps until at most
     `max_crossings` crossings remain (the network has formed; early fields are
     noise whose crossings form one percolating cluster that the greedy rule can
@@ -512,7 +518,7 @@ def measure_string_length(n: int, max_steps: int, max_crossings: int, cpu_sample
     g = lattice.string_length_points(p, sample, True)
     t_gpu = min(times)
     t_ref = t_cpu * (M / max(len(sample), 1)) ** 2
-    return {"lattice": n, "steps": steps, "physics": "e=0, lambda=1, eta=1, dx=0.35, dt=0.05, no friction",
+    return {"lattice": n, "steps": steps, "physics": GLOBAL_STRINGS,
             "crossings": M, "L0": L0, "L1": L1, "method": "link-graph component walks",
             "gpu_s": t_gpu, "gpu_crossings_per_s": M / t_gpu, "detect_to_host_s": t_detect,
             "cpu_sample_crossings": len(sample), "cpu_sample_s": t_cpu, "cpu_kind": "port", "cpu_cores": 1,
