@@ -217,7 +217,7 @@ def load_traffic(precision: str, n: int):
         return None
     try:
         d = json.loads(f.read_text())
-        e = d.get(f"ah_step_{precision}")
+        e = d.get(f"{'moore' if MODEL['name'] == 'moore' else 'ah'}_step_{precision}")
         if not e:
             return None
         return e["bytes_per_site"] * n ** 3
