@@ -9,6 +9,7 @@
 #include <cstdlib>
 #include <fstream>
 #include <iostream>
+#include <random>
 #include <sstream>
 #include <stdexcept>
 #include <string>
@@ -151,6 +152,29 @@ Params::Params(Program prog)
         v["saveFreq"] = "10";
         v["xyBC"] = "fixed";
         break;
+    case Program::IcwEvolution:
+        // ic_w_evolution.cpp:23-50 and the ic_func.cpp:25-58 constants it uses
+        v["nx"] = v["ny"] = v["nz"] = "201";
+        v["nt"] = "2001";
+        v["dx"] = v["dy"] = v["dz"] = "0.35";
+        v["dt"] = "0.05";
+        v["lambda"] = "1";
+        v["eta"] = "1";
+        v["g"] = "0";
+        v["damped_nt"] = "0";
+        v["dampFac"] = "0";
+        v["makeGif"] = "true";
+        v["saveFreq"] = "10";
+        v["xyBC"] = "periodic";
+        v["zBC"] = "periodic";
+        v["stringPos"] = "false";
+        v["stringDetect"] = "true";
+        v["splitLength"] = "true";
+        // ic_func.cpp: "random" is the in-process generator provided here (the
+        // reference's default, "loop collision", needs its SOR string profiles)
+        v["ic_type"] = "random";
+        v["seed"] = "1";
+        break;
     }
 }
 
@@ -287,6 +311,10 @@ struct Run {
             p.damped_nt = 0;
             p.dampFac = 0;
             p.alpha = 0;
+        } else if (prog == Program::IcwEvolution) {  // damping only, no expansion (ic_w_evolution.cpp:281)
+            p.damped_nt = (int32_t)prm.integer("damped_nt");
+            p.dampFac = prm.num("dampFac");
+            p.alpha = 0;
         } else {
             p.damped_nt = (int32_t)prm.integer("damped_nt");
             p.dampFac = prm.num("dampFac");
@@ -295,9 +323,9 @@ struct Run {
         p.energy_form = is_mpi(prog) ? LAT_ENERGY_MPI : LAT_ENERGY_EVOLUTION;
         p.moore_current = prog == Program::MooreEvol ? LAT_MOORE_CURRENT_CHARGE : LAT_MOORE_CURRENT_PLAIN;
         p.bc = LAT_BC_PERIODIC;
-        if (prog == Program::Evolution || prog == Program::MooreEvol) {
+        if (prog == Program::Evolution || prog == Program::MooreEvol || prog == Program::IcwEvolution) {
             const std::string xy = prm.str("xyBC");
-            const std::string z = prog == Program::Evolution ? prm.str("zBC") : std::string("fixed");
+            const std::string z = prog == Program::MooreEvol ? std::string("fixed") : prm.str("zBC");
             auto kind = [](const std::string& b) {
                 if (b == "periodic") return 0;
                 if (b == "neumann" || b == "absorbing") return -1;
@@ -556,6 +584,72 @@ int run_openmp(Run& r)
     return 0;
 }
 
+// ic_func.cpp:647-683 "random": per site in linear order phi_re, phi_im (and,
+// when g != 0, the three links dmu*u) drawn from minstd_rand(seed) through
+// uniform_real_distribution<double>(-1, 1); both levels equal.
+void icfunc_random(const Run& r, double seed, std::vector<double>& now)
+{
+    std::minstd_rand eng;
+    eng.seed((std::minstd_rand::result_type)seed);
+    std::uniform_real_distribution<double> unif(-1, 1);
+    now.assign((size_t)5 * r.N, 0.0);
+    const double d[3] = {r.p.dx, r.p.dy, r.p.dz};
+    for (int64_t s = 0; s < r.N; ++s) {
+        now[s] = unif(eng);
+        now[r.N + s] = unif(eng);
+        if (r.p.g != 0)
+            for (int m = 0; m < 3; ++m) now[(size_t)(2 + m) * r.N + s] = d[m] * unif(eng);
+    }
+}
+
+int run_icw(Run& r)
+{
+    // ic_w_evolution.cpp:52-1190
+    Params& q = r.prm;
+    const long long nt = q.integer("nt"), saveFreq = q.integer("saveFreq"), countRate = q.integer("countRate");
+    const bool makeGif = q.flag("makeGif"), stringPos = q.flag("stringPos"), detect = q.flag("stringDetect");
+    const bool split = q.flag("splitLength");
+    struct timeval start, end;
+    gettimeofday(&start, nullptr);
+    if (q.str("ic_type") != "random")
+        fail("ic_type: only the \"random\" initial conditions of ic_func.cpp are provided by this program");
+    std::vector<double> now;
+    icfunc_random(r, q.num("seed"), now);
+    check(lat_create(&r.p, &r.h), "lat_create");
+    check(lat_set_state(r.h, now.data(), now.data(), 0), "lat_set_state");
+    std::ofstream valsPerLoop = r.open_out(r.data("valsPerLoop_test.txt"));  // input = "test" (:67)
+    const bool periodic = r.p.bc == LAT_BC_PERIODIC;
+    long long counter = 0, gifFrame = 0;
+    for (long long n = 0; n < nt; ++n) {
+        progress(n, counter, countRate);
+        const double pos = stringPos ? r.string_position() : 0;
+        double L0 = 0, L1 = 0;
+        if (detect) check(lat_string_length(r.h, LAT_FIELD_PHI1, split ? 1 : 0, LAT_CHAIN_AUTO, &L0, &L1, nullptr),
+                          "lat_string_length");
+        lat_diag d;
+        check(lat_step_diag(r.h, &d), "lat_step_diag");
+        double dev = d.gauss_abs_sum;  // ic_w_evolution.cpp:1141-1145
+        if (periodic) dev = dev / (double)(r.p.nx * r.p.ny) / (double)r.p.nz;
+        else dev = dev / (double)((r.p.nx - 2) * (r.p.ny - 2)) / (double)(r.p.nz - 2);
+        valsPerLoop << d.energy << " " << dev;
+        if (stringPos) valsPerLoop << " " << pos;
+        if (detect) {
+            valsPerLoop << " " << L0;
+            if (split) valsPerLoop << " " << L1;
+        }
+        valsPerLoop << std::endl;
+        if (makeGif && saveFreq > 0 && n % saveFreq == 0) {
+            r.write_field_magnitudes(r.gif("gifData_" + std::to_string(gifFrame) + ".txt"));
+            ++gifFrame;
+        }
+    }
+    std::cout << "\rTimestep " << nt << " completed." << std::endl;
+    r.write_final_field(r.data("finalField.txt"));
+    gettimeofday(&end, nullptr);
+    std::cout << "Time taken: " << end.tv_sec - start.tv_sec << "s" << std::endl;
+    return 0;
+}
+
 }  // namespace
 
 int run_program(Program prog, int argc, char** argv)
@@ -564,6 +658,7 @@ int run_program(Program prog, int argc, char** argv)
         Run r(prog);
         r.prm.parse_args(argc, argv);
         r.build_params();
+        if (prog == Program::IcwEvolution) return run_icw(r);
         return is_mpi(prog) ? run_mpi(r) : run_openmp(r);
     } catch (const std::exception& e) {
         std::cerr << "error: " << e.what() << std::endl;

@@ -13,7 +13,9 @@
 
 namespace axh {
 
-enum class Program { MpiEvolution, Evolution, MooreMpiEvolution, MooreEvol };
+// IcwEvolution is ic_w_evolution.cpp: evolution with its initial conditions
+// made in-process (ic_func.cpp) and the total string length every step.
+enum class Program { MpiEvolution, Evolution, MooreMpiEvolution, MooreEvol, IcwEvolution };
 
 // Parameter set: the reference defaults of `prog`, overridden by the file and
 // the command line.  Unknown keys are an error.

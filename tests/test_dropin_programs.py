@@ -114,3 +114,33 @@ def test_openmp_programs_reproduce_reference_output(tmp_path, name):
         frames = _frames(tmp_path, "gifStringPosData_")
         assert [len(f) for f in frames] == z["frame_counts"].tolist()
         np.testing.assert_allclose(np.concatenate(frames), z["frame_xyz"], rtol=0, atol=1e-9)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["ref_icw_len_periodic", "ref_icw_len_fixed", "ref_icw_len_nosplit"])
+def test_icw_program_reproduces_reference_output(tmp_path, name):
+    """bin/ic_w_evolution against ic_w_evolution itself: ic_func's random IC
+    made in-process, then per step energy, deviation and the string length
+    L0 [L1] (valsPerLoop_test.txt), and the last level (finalField.txt)."""
+    z = load_golden(name)
+    p = params_from_json(z["params"])
+    split = bool(z["split"])
+    nt = int(z["nt"])
+    bc = "periodic" if p.bc == 0 else "fixed"
+    args = {"nx": p.nx, "ny": p.ny, "nz": p.nz, "nt": nt, "dx": p.dx, "dy": p.dy, "dz": p.dz, "dt": p.dt,
+            "xyBC": bc, "zBC": bc, "seed": int(z["seed"]), "splitLength": "true" if split else "false",
+            "makeGif": "false"}
+    r = _run("ic_w_evolution", tmp_path, args)
+    assert r.returncode == 0, r.stderr.decode()
+    vals = _cols(tmp_path / "Data" / "valsPerLoop_test.txt").reshape(nt, 4 if split else 3)
+    assert np.array_equal(vals[:, 2], z["L0"])
+    if split:
+        assert np.array_equal(vals[:, 3], z["L1"])
+    assert np.max(np.abs(vals[:, 0] - z["energy"]) / np.abs(z["energy"])) <= 1e-12
+    final = _cols(tmp_path / "Data" / "finalField.txt").reshape(-1, 5).T
+    assert np.array_equal(final[:2], z["final_phi"])
+
+
+def test_icw_program_rejects_unprovided_ic(tmp_path):
+    r = _run("ic_w_evolution", tmp_path, {"nx": 4, "ny": 4, "nz": 4, "nt": 1, "ic_type": "loop collision"})
+    assert r.returncode == 2 and b"ic_type" in r.stderr
