@@ -97,7 +97,7 @@ def build_programs(verbose: bool = False) -> list[Path]:
         if exe.exists() and all(exe.stat().st_mtime >= d.stat().st_mtime for d in deps):
             outs.append(exe)
             continue
-        cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-ffp-contract=off", "-I", str(ROOT / "include"), str(s)] + [str(c) for c in common]
+        cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-pthread", "-ffp-contract=off", "-I", str(ROOT / "include"), str(s)] + [str(c) for c in common]
         cmd += ["-L", str(PKG), "-llattice_gpu", "-Wl,-rpath,$ORIGIN/..", "-o", str(exe)]
         if verbose:
             print(" ".join(cmd), flush=True)

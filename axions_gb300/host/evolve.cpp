@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 
+#include "ic_io.hpp"
 #include "lattice_gpu.h"
 
 namespace axh {
@@ -53,6 +54,9 @@ Params::Params(Program prog)
     v["out_dir"] = ".";         // where Data/ and GifData/ live (reference: next to its source)
     v["digits"] = "6";          // ostream precision of the text output (reference default 6)
     v["countRate"] = "10";
+    // initial-condition table under Data/: the reference's text file, or its
+    // binary form (ic_io.hpp); MPI programs read it for ic_type = data
+    v["ic_file"] = is_moore(prog) ? "moore_ic.txt" : "ic.txt";
     v["scaling"] = "1";
     switch (prog) {
     case Program::MpiEvolution:
@@ -174,6 +178,21 @@ Params::Params(Program prog)
         // reference's default, "loop collision", needs its SOR string profiles)
         v["ic_type"] = "random";
         v["seed"] = "1";
+        break;
+    case Program::InitialConditions:
+        // initialConditions.cpp:22-60 ("random" is the family provided here;
+        // ic_type = convert rewrites a table between text and binary)
+        v["ic_type"] = "random";
+        v["nx"] = v["ny"] = v["nz"] = "401";
+        v["dx"] = v["dy"] = v["dz"] = "0.5";
+        v["dt"] = "0.05";
+        v["g"] = "0";
+        v["seed"] = "42";
+        v["mean"] = "0";
+        v["stdev"] = "0.5";
+        v["ic_in"] = "";     // convert: the table to read (under Data/)
+        v["cols"] = "5";     // convert: columns of the table
+        v["levels"] = "1";   // convert: rows = levels * nx * ny * nz
         break;
     }
 }
@@ -345,22 +364,19 @@ struct Run {
     }
 
     // Whitespace-separated columns, one line per site in linear order.
+    // The text file or its binary form (ic_io.hpp), parsed on all host cores.
     void read_ic(const std::string& path, int cols, int levels, std::vector<double>& lv0, std::vector<double>& lv1)
     {
-        std::ifstream ic(path);
-        if (!ic) fail("cannot read " + path);
+        std::vector<double> tab;
+        read_table(path, cols, (int64_t)levels * N, tab);
+        const size_t rows = (size_t)levels * (size_t)N;
         lv0.assign((size_t)ncomp * N, 0.0);
         lv1.assign((size_t)ncomp * N, 0.0);
         for (int t = 0; t < levels; ++t) {
             std::vector<double>& dst = t == 0 ? lv0 : lv1;
-            for (int64_t s = 0; s < N; ++s)
-                for (int c = 0; c < cols; ++c) {
-                    double v;
-                    if (!(ic >> v)) fail(path + ": expected " + std::to_string(levels * N) + " lines of " +
-                                         std::to_string(cols) + " values");
-                    if (!std::isfinite(v)) fail(path + ": non-finite value");
-                    dst[(size_t)c * N + s] = v;
-                }
+            for (int c = 0; c < cols; ++c)
+                std::copy(tab.begin() + (ptrdiff_t)(c * rows + (size_t)t * N),
+                          tab.begin() + (ptrdiff_t)(c * rows + (size_t)(t + 1) * N), dst.begin() + (ptrdiff_t)c * N);
         }
         if (levels == 1) lv1 = lv0;
     }
@@ -377,27 +393,26 @@ struct Run {
         return n;
     }
 
+    // |phi|^2 of the current level (|phi1|^2 |phi2|^2 for Moore), one line per
+    // site (evolution.cpp:1423-1441, mooreEvol.cpp:700-718).
     void write_field_magnitudes(const std::string& path)
     {
         std::vector<double> now((size_t)ncomp * N);
         check(lat_get_state(h, now.data(), nullptr), "lat_get_state");
-        std::ofstream o = open_out(path);
+        const int cols = is_moore(prog) ? 2 : 1;
+        std::vector<double> mag((size_t)cols * N);
         for (int64_t s = 0; s < N; ++s) {
-            const double a = std::pow(now[s], 2) + std::pow(now[N + s], 2);
-            if (is_moore(prog)) o << a << " " << std::pow(now[2 * N + s], 2) + std::pow(now[3 * N + s], 2) << std::endl;
-            else o << a << std::endl;
+            mag[s] = now[s] * now[s] + now[N + s] * now[N + s];
+            if (cols == 2) mag[N + s] = now[2 * N + s] * now[2 * N + s] + now[3 * N + s] * now[3 * N + s];
         }
+        write_table_text(path, cols, N, mag.data(), digits);
     }
 
     void write_final_field(const std::string& path)
     {
         std::vector<double> now((size_t)ncomp * N);
         check(lat_get_state(h, now.data(), nullptr), "lat_get_state");
-        std::ofstream o = open_out(path);
-        for (int64_t s = 0; s < N; ++s) {
-            for (int c = 0; c < ncomp; ++c) o << (c ? " " : "") << now[(size_t)c * N + s];
-            o << std::endl;
-        }
+        write_table_text(path, ncomp, N, now.data(), digits);
     }
 
     // Position of the string along y = z = 0 by a parabolic fit to the
@@ -458,9 +473,9 @@ int run_mpi(Run& r)
         check(lat_random_phase_ic(&r.p, (uint32_t)seed, indep, now.data()), "lat_random_phase_ic");
         past = now;
     } else if (ic_type == "stationary data") {
-        r.read_ic(r.data(moore ? "moore_ic.txt" : "ic.txt"), r.ncomp, 1, past, now);
+        r.read_ic(r.data(q.str("ic_file")), r.ncomp, 1, past, now);
     } else if (ic_type == "data") {
-        r.read_ic(r.data(moore ? "moore_ic.txt" : "ic.txt"), r.ncomp, 2, past, now);  // block 0 = slot 0 = past
+        r.read_ic(r.data(q.str("ic_file")), r.ncomp, 2, past, now);  // block 0 = slot 0 = past
     } else {
         fail("ic_type must be random, data or stationary data");
     }
@@ -520,8 +535,8 @@ int run_openmp(Run& r)
         valsName = "valsPerLoop_" + tag + ".txt";
     }
     std::vector<double> now, past;
-    if (moore) r.read_ic(r.data("moore_ic.txt"), 7, 1, past, now);
-    else r.read_ic(r.data("ic.txt"), 5, q.flag("stationary_ic") ? 1 : 2, past, now);
+    if (moore) r.read_ic(r.data(q.str("ic_file")), 7, 1, past, now);
+    else r.read_ic(r.data(q.str("ic_file")), 5, q.flag("stationary_ic") ? 1 : 2, past, now);
     check(lat_create(&r.p, &r.h), "lat_create");
     check(lat_set_state(r.h, now.data(), past.data(), 0), "lat_set_state");
     std::ofstream valsPerLoop = r.open_out(r.data(valsName));
@@ -650,11 +665,67 @@ int run_icw(Run& r)
     return 0;
 }
 
+bool ends_with(const std::string& s, const std::string& suffix)
+{
+    return s.size() >= suffix.size() && s.compare(s.size() - suffix.size(), suffix.size(), suffix) == 0;
+}
+
+// initialConditions.cpp:670-708 ("random"): per site in linear order phi_re,
+// phi_im from normal_distribution<double>(mean, stdev) over
+// default_random_engine(seed); the link columns are dmu*g*A with A = 0.
+// Written as Data/<ic_file>: text (the reference's format and precision) or,
+// for a name ending in .bin, the binary form.  ic_type = convert reads
+// Data/<ic_in> (text or binary) and writes it as Data/<ic_file>.
+int run_initial_conditions(Params& q)
+{
+    struct timeval start, end;
+    gettimeofday(&start, nullptr);
+    const std::string dir = q.str("out_dir");
+    ::mkdir((dir + "/Data").c_str(), 0755);
+    const std::string out = dir + "/Data/" + q.str("ic_file");
+    const int digits = (int)q.integer("digits");
+    const int64_t N = q.integer("nx") * q.integer("ny") * q.integer("nz");
+    std::vector<double> tab;
+    int cols = 5;
+    int64_t rows = N;
+    const std::string type = q.str("ic_type");
+    if (type == "random") {
+        std::default_random_engine generator((std::default_random_engine::result_type)q.num("seed"));
+        std::normal_distribution<double> distribution(q.num("mean"), q.num("stdev"));
+        tab.assign((size_t)5 * N, 0.0);
+        const double A = 0.0, g = q.num("g");
+        for (int64_t s = 0; s < N; ++s) {
+            tab[s] = distribution(generator);
+            tab[N + s] = distribution(generator);
+            tab[2 * N + s] = q.num("dx") * g * A;
+            tab[3 * N + s] = q.num("dy") * g * A;
+            tab[4 * N + s] = q.num("dz") * g * A;
+        }
+    } else if (type == "convert") {
+        cols = (int)q.integer("cols");
+        rows = q.integer("levels") * N;
+        if (q.str("ic_in").empty()) fail("ic_type = convert needs ic_in");
+        read_table(dir + "/Data/" + q.str("ic_in"), cols, rows, tab);
+    } else {
+        fail("ic_type: this program provides \"random\" and \"convert\"");
+    }
+    if (ends_with(out, ".bin")) write_table_bin(out, cols, rows, tab.data());
+    else write_table_text(out, cols, rows, tab.data(), digits);
+    gettimeofday(&end, nullptr);
+    std::cout << "Time taken: " << end.tv_sec - start.tv_sec << "s" << std::endl;
+    return 0;
+}
+
 }  // namespace
 
 int run_program(Program prog, int argc, char** argv)
 {
     try {
+        if (prog == Program::InitialConditions) {
+            Params q(prog);
+            q.parse_args(argc, argv);
+            return run_initial_conditions(q);
+        }
         Run r(prog);
         r.prm.parse_args(argc, argv);
         r.build_params();

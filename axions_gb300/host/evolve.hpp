@@ -15,7 +15,8 @@ namespace axh {
 
 // IcwEvolution is ic_w_evolution.cpp: evolution with its initial conditions
 // made in-process (ic_func.cpp) and the total string length every step.
-enum class Program { MpiEvolution, Evolution, MooreMpiEvolution, MooreEvol, IcwEvolution };
+// InitialConditions is initialConditions.cpp (writes Data/ic.txt; host only).
+enum class Program { MpiEvolution, Evolution, MooreMpiEvolution, MooreEvol, IcwEvolution, InitialConditions };
 
 // Parameter set: the reference defaults of `prog`, overridden by the file and
 // the command line.  Unknown keys are an error.

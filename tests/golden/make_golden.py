@@ -220,6 +220,18 @@ def gen_icw_length(name, nx, ny, nz, nt, bc, seed, d=0.35, split=True):
     print(name, "vals", vals.shape)
 
 
+def gen_initial_conditions(name, nx, ny, nz, seed, mean, stdev, g):
+    """initialConditions.cpp, ic_type "random": Data/ic.txt (17 digits)."""
+    consts = {"nx": nx, "ny": ny, "nz": nz, "ic_type": "random", "seed": float(seed), "mean": float(mean),
+              "stdev": float(stdev), "g": float(g)}
+    build_ref.build("initialConditions", name, consts)
+    work = build_ref.run(name)
+    ic = build_ref.read_columns(work / "Data" / "ic.txt").reshape(nx * ny * nz, 5).T.copy()
+    np.savez_compressed(OUT / f"{name}.npz", program="initialConditions", nx=nx, ny=ny, nz=nz, seed=seed, mean=mean,
+                        stdev=stdev, g=g, dx=0.5, ic=ic)
+    print(name, ic.shape)
+
+
 def main():
     if not build_ref.reference_available():
         raise SystemExit("reference sources not found; fixtures can only be made where they are")
@@ -248,6 +260,7 @@ def main():
     gen_icw_length("ref_icw_len_wide", 13, 12, 11, 16, BC_PERIODIC, seed=4, d=1.0)
     gen_icw_length("ref_icw_len_fixed", 15, 15, 15, 25, BC_FIXED, seed=5)
     gen_icw_length("ref_icw_len_nosplit", 11, 13, 9, 12, BC_PERIODIC, seed=6, d=0.5, split=False)
+    gen_initial_conditions("ref_initial_conditions", 7, 6, 5, seed=42, mean=0.0, stdev=0.5, g=0.5)
 
 
 if __name__ == "__main__":
