@@ -36,6 +36,7 @@ UNITS = {
     "moore_f64.cu": ["-fmad=false"],
     "detect.cu": ["-fmad=false"],
     "string_length.cu": ["-fmad=false"],
+    "snapshot.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
     "ah_f64_fast.cu": [],
     "ah_f32.cu": [],

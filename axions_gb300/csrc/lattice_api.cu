@@ -326,6 +326,11 @@ int lat_destroy(lat_handle* h)
     cudaFree(h->wind);
     cudaFree(h->wind_sum);
     chain_buffers_release(h->chain, nullptr);
+    if (h->snap_pending) cudaEventSynchronize(h->snap_copied);
+    cudaFree(h->snap_dev);
+    if (h->snap_staged) cudaEventDestroy(h->snap_staged);
+    if (h->snap_copied) cudaEventDestroy(h->snap_copied);
+    if (h->snap_stream) cudaStreamDestroy(h->snap_stream);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
     return LAT_OK;

@@ -38,6 +38,13 @@ struct lat_handle {
     int8_t* wind = nullptr;
     unsigned long long* wind_sum = nullptr;
     lat::ChainBuffers chain;   // string-length buffers
+    // asynchronous snapshots (snapshot.cu)
+    double* snap_dev = nullptr;          // staged copy of the level, [cols][N] doubles
+    size_t snap_cap = 0;                 // bytes of snap_dev
+    cudaStream_t snap_stream = nullptr;  // device-to-host copies
+    cudaEvent_t snap_staged = nullptr;   // staging done (handle stream)
+    cudaEvent_t snap_copied = nullptr;   // copy done (snap_stream)
+    bool snap_pending = false;
     int64_t bytes = 0;
     int64_t launches = 0;      // kernels launched by this handle
 

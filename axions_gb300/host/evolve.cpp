@@ -13,6 +13,7 @@
 #include <sstream>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "ic_io.hpp"
@@ -393,21 +394,6 @@ struct Run {
         return n;
     }
 
-    // |phi|^2 of the current level (|phi1|^2 |phi2|^2 for Moore), one line per
-    // site (evolution.cpp:1423-1441, mooreEvol.cpp:700-718).
-    void write_field_magnitudes(const std::string& path)
-    {
-        std::vector<double> now((size_t)ncomp * N);
-        check(lat_get_state(h, now.data(), nullptr), "lat_get_state");
-        const int cols = is_moore(prog) ? 2 : 1;
-        std::vector<double> mag((size_t)cols * N);
-        for (int64_t s = 0; s < N; ++s) {
-            mag[s] = now[s] * now[s] + now[N + s] * now[N + s];
-            if (cols == 2) mag[N + s] = now[2 * N + s] * now[2 * N + s] + now[3 * N + s] * now[3 * N + s];
-        }
-        write_table_text(path, cols, N, mag.data(), digits);
-    }
-
     void write_final_field(const std::string& path)
     {
         std::vector<double> now((size_t)ncomp * N);
@@ -437,6 +423,81 @@ struct Run {
         const double l = mag(is - 1), r = mag(is + 1);
         return (is - x0) * p.dx + p.dx * (l - r) / (2 * l - 4 * smallest + 2 * r);
     }
+};
+
+// gifData frames written while the run goes on.  A frame is a snapshot of
+// |phi|^2 (lat_snapshot_begin) into one of two pinned buffers; its copy is
+// waited for only when the next frame starts (saveFreq steps later), and its
+// text is formatted and written by a background thread meanwhile.
+class AsyncFrames {
+public:
+    AsyncFrames(lat_handle* h, int cols, int64_t N, int digits) : h_(h), cols_(cols), N_(N), digits_(digits) {}
+    ~AsyncFrames()
+    {
+        try {
+            close();
+        } catch (...) {
+        }
+        for (double* b : buf_) lat_host_free(b);
+    }
+
+    void begin(const std::string& path)
+    {
+        hand_over();
+        if (!buf_[cur_]) {
+            buf_[cur_] = (double*)lat_host_alloc((int64_t)sizeof(double) * cols_ * N_);
+            if (!buf_[cur_]) fail(std::string("lat_host_alloc: ") + lat_last_error());
+        }
+        check(lat_snapshot_begin(h_, LAT_SNAP_MAGNITUDE, buf_[cur_]), "lat_snapshot_begin");
+        pending_ = true;
+        pending_path_ = path;
+        pending_buf_ = cur_;
+        cur_ ^= 1;
+    }
+
+    void close()
+    {
+        hand_over();
+        join();
+    }
+
+private:
+    // the pending frame's copy is complete: give it to the writer thread (the
+    // previous writer, which used the other buffer, finishes first)
+    void hand_over()
+    {
+        if (!pending_) return;
+        check(lat_snapshot_wait(h_), "lat_snapshot_wait");
+        pending_ = false;
+        join();
+        const double* src = buf_[pending_buf_];
+        const std::string path = pending_path_;
+        writer_ = std::thread([this, src, path] {
+            try {
+                write_table_text(path, cols_, N_, src, digits_);
+            } catch (const std::exception& e) {
+                error_ = e.what();
+            }
+        });
+    }
+
+    void join()
+    {
+        if (writer_.joinable()) writer_.join();
+        if (!error_.empty()) fail(error_);
+    }
+
+    lat_handle* h_;
+    int cols_;
+    int64_t N_;
+    int digits_;
+    double* buf_[2] = {nullptr, nullptr};
+    int cur_ = 0;
+    bool pending_ = false;
+    std::string pending_path_;
+    int pending_buf_ = 0;
+    std::thread writer_;
+    std::string error_;
 };
 
 void progress(long long TimeStep, long long& counter, long long countRate)
@@ -539,6 +600,7 @@ int run_openmp(Run& r)
     else r.read_ic(r.data(q.str("ic_file")), 5, q.flag("stationary_ic") ? 1 : 2, past, now);
     check(lat_create(&r.p, &r.h), "lat_create");
     check(lat_set_state(r.h, now.data(), past.data(), 0), "lat_set_state");
+    AsyncFrames frames(r.h, moore ? 2 : 1, r.N, r.digits);
     std::ofstream valsPerLoop = r.open_out(r.data(valsName));
 
     const bool makeGif = q.flag("makeGif");
@@ -587,11 +649,12 @@ int run_openmp(Run& r)
             valsPerLoop << std::endl;
         }
         if (makeGif && saveFreq > 0 && n % saveFreq == 0) {
-            r.write_field_magnitudes(r.gif("gifData_" + std::to_string(gifFrame) + ".txt"));
+            frames.begin(r.gif("gifData_" + std::to_string(gifFrame) + ".txt"));
             ++gifFrame;
         }
         n += k;
     }
+    frames.close();
     std::cout << "\rTimestep " << nt << " completed." << std::endl;
     if (moore || q.flag("finalOut")) r.write_final_field(r.data("finalField.txt"));
     gettimeofday(&end, nullptr);
@@ -632,6 +695,7 @@ int run_icw(Run& r)
     icfunc_random(r, q.num("seed"), now);
     check(lat_create(&r.p, &r.h), "lat_create");
     check(lat_set_state(r.h, now.data(), now.data(), 0), "lat_set_state");
+    AsyncFrames frames(r.h, 1, r.N, r.digits);
     std::ofstream valsPerLoop = r.open_out(r.data("valsPerLoop_test.txt"));  // input = "test" (:67)
     const bool periodic = r.p.bc == LAT_BC_PERIODIC;
     long long counter = 0, gifFrame = 0;
@@ -654,10 +718,11 @@ int run_icw(Run& r)
         }
         valsPerLoop << std::endl;
         if (makeGif && saveFreq > 0 && n % saveFreq == 0) {
-            r.write_field_magnitudes(r.gif("gifData_" + std::to_string(gifFrame) + ".txt"));
+            frames.begin(r.gif("gifData_" + std::to_string(gifFrame) + ".txt"));
             ++gifFrame;
         }
     }
+    frames.close();
     std::cout << "\rTimestep " << nt << " completed." << std::endl;
     r.write_final_field(r.data("finalField.txt"));
     gettimeofday(&end, nullptr);

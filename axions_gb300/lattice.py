@@ -28,6 +28,7 @@ EXPORTS = [
     "lat_kernel_launches",
     "lat_set_state", "lat_get_state", "lat_step", "lat_step_diag", "lat_advance", "lat_diagnostics",
     "lat_detect_crossings", "lat_winding", "lat_string_length", "lat_string_length_points",
+    "lat_snapshot_doubles", "lat_snapshot_begin", "lat_snapshot_wait", "lat_host_alloc", "lat_host_free",
     "lat_ah_step_f64_noalloc",
     "lat_batch_create", "lat_batch_destroy", "lat_batch_add", "lat_batch_remove", "lat_batch_size",
     "lat_batch_kernel_launches", "lat_batch_advance", "lat_batch_take_diags",
@@ -93,6 +94,13 @@ def load_library(path: Path | None = None):
     L.lat_detect_crossings.argtypes = [vp, ctypes.c_int32, dp, ctypes.c_int64, P(ctypes.c_int64)]
     L.lat_winding.argtypes = [vp, ctypes.c_int32, P(ctypes.c_int8), P(ctypes.c_int64)]
     L.lat_string_length.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, dp, dp, P(ctypes.c_int64)]
+    L.lat_snapshot_doubles.argtypes = [vp, ctypes.c_int32]
+    L.lat_snapshot_doubles.restype = ctypes.c_int64
+    L.lat_snapshot_begin.argtypes = [vp, ctypes.c_int32, dp]
+    L.lat_snapshot_wait.argtypes = [vp]
+    L.lat_host_alloc.argtypes = [ctypes.c_int64]
+    L.lat_host_alloc.restype = vp
+    L.lat_host_free.argtypes = [vp]
     L.lat_string_length_points.argtypes = [P(LatParams), dp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, dp, dp]
     L.lat_ah_step_f64_noalloc.argtypes = [P(LatParams), vp, ctypes.c_int64, ctypes.c_int32, vp]
     L.lat_batch_create.argtypes = [ctypes.c_int32, P(vp)]
@@ -300,6 +308,23 @@ class Lattice:
                    self.L.lat_detect_crossings(self.h, int(field), _dp(xyz), n, ctypes.byref(cnt)))
         return xyz[:n]
 
+    # asynchronous snapshots ------------------------------------------------------
+    def snapshot_begin(self, kind: int, out: np.ndarray):
+        """Start copying |phi|^2 (SNAP_MAGNITUDE) or the level (SNAP_LEVEL) of the
+        current level into `out` (float64, snapshot_doubles(kind) values; keep it
+        alive until snapshot_wait)."""
+        n = int(self.L.lat_snapshot_doubles(self.h, int(kind)))
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size >= n
+        self._snap_out = out
+        _check("lat_snapshot_begin", self.L.lat_snapshot_begin(self.h, int(kind), _dp(out)))
+
+    def snapshot_wait(self):
+        _check("lat_snapshot_wait", self.L.lat_snapshot_wait(self.h))
+        self._snap_out = None
+
+    def snapshot_doubles(self, kind: int) -> int:
+        return int(self.L.lat_snapshot_doubles(self.h, int(kind)))
+
     def count_crossings(self, field: int = 0) -> int:
         """Number of bilinear crossings on the current level (nothing copied)."""
         cnt = ctypes.c_int64(0)
@@ -418,6 +443,29 @@ class ServerStats(ctypes.Structure):
 
 
 CHAIN_AUTO, CHAIN_HASH, CHAIN_EXHAUSTIVE = 0, 1, 2
+SNAP_MAGNITUDE, SNAP_LEVEL = 0, 1
+
+
+class PinnedArray:
+    """float64 array in page-locked host memory (lat_host_alloc), for snapshots
+    that overlap the steps."""
+
+    def __init__(self, n: int):
+        self.L = load_library()
+        self.ptr = self.L.lat_host_alloc(8 * max(int(n), 1))
+        if not self.ptr:
+            raise LatticeError("lat_host_alloc", -2, (self.L.lat_last_error() or b"").decode())
+        buf = (ctypes.c_double * max(int(n), 1)).from_address(self.ptr)
+        self.array = np.frombuffer(buf, dtype=np.float64, count=int(n))
+
+    def close(self):
+        if self.ptr:
+            self.array = None
+            self.L.lat_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        self.close()
 
 
 def string_length_points(p: LatParams, xyz: np.ndarray, split: bool = True, method: int = CHAIN_AUTO):

@@ -248,6 +248,33 @@ int lat_string_length(lat_handle* h, int32_t field, int32_t split, int32_t metho
 int lat_string_length_points(const lat_params* p, const double* xyz, int64_t M, int32_t split, int32_t method,
                              double* L0, double* L1);
 
+/* ---- asynchronous snapshots ------------------------------------------------------
+ * The reference writes its field dumps (gifData |phi|^2 volumes,
+ * evolution.cpp:1423-1441, mooreEvol.cpp:700-718; finalField) from host arrays
+ * inside the step loop, so the loop waits for every dump.  A snapshot copies
+ * the current level to host memory while later steps run:
+ *   LAT_SNAP_MAGNITUDE  |phi|^2 per site, re*re + im*im in double ([N] doubles;
+ *                       Moore: [2][N], |phi1|^2 then |phi2|^2)
+ *   LAT_SNAP_LEVEL      the whole level, [ncomp][N] doubles (lat_get_state's
+ *                       `now` layout)
+ * lat_snapshot_begin stages the values on the handle's stream (before any step
+ * issued afterwards) and starts their copy into `dst` (lat_snapshot_doubles
+ * doubles) on a separate stream.  With `dst` from lat_host_alloc (pinned) the
+ * call returns at once and the copy overlaps the following steps; with
+ * ordinary memory it returns when the copy is done.  lat_snapshot_wait blocks
+ * until `dst` holds the values.  One snapshot is in flight per handle: a new
+ * begin first waits for the previous copy. */
+#define LAT_SNAP_MAGNITUDE 0
+#define LAT_SNAP_LEVEL     1
+int64_t lat_snapshot_doubles(const lat_handle* h, int32_t kind);
+int lat_snapshot_begin(lat_handle* h, int32_t kind, double* dst);
+int lat_snapshot_wait(lat_handle* h);
+
+/* Page-locked host memory for snapshot destinations (NULL on failure), and its
+ * release.  For callers that do not link the CUDA runtime themselves. */
+void* lat_host_alloc(int64_t bytes);
+void lat_host_free(void* ptr);
+
 /* ---- device-side random-phase IC ------------------------------------------------
  * The physics of lat_random_phase_ic (phi = eta*e^{i phase}, phase uniform in
  * [0, 2 pi), both levels equal, theta = 0, TimeStep 0) drawn on the GPU with
