@@ -27,6 +27,9 @@ F32 = 1
 F64_FAST = 2
 BC_PERIODIC = 0
 BC_FIXED = 1
+BC_NEUMANN = 2
+BC_ABSORBING = 3
+BCZ_AS_XY, BCZ_PERIODIC, BCZ_FIXED, BCZ_NEUMANN = 0, 1, 2, 3
 ENERGY_EVOLUTION = 0
 ENERGY_MPI = 1
 MOORE_CURRENT_PLAIN = 0
@@ -62,7 +65,9 @@ class LatParams(ctypes.Structure):
         ("tau0", ctypes.c_double),
         ("energy_form", ctypes.c_int32),
         ("kernel_variant", ctypes.c_int32),
-        ("reserved", ctypes.c_double * 4),
+        ("bc_z", ctypes.c_int32),
+        ("reserved_i", ctypes.c_int32),
+        ("reserved", ctypes.c_double * 3),
     ]
 
     @property

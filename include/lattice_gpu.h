@@ -60,11 +60,24 @@ extern "C" {
                                 reciprocal for /dt (each operation within an ulp of
                                 LAT_F64's); not bit-identical to the reference's order */
 
-/* boundary handling */
-#define LAT_BC_PERIODIC 0    /* periodic in x, y, z (mpi_evolution.cpp:385-405)             */
-#define LAT_BC_FIXED    1    /* only interior sites evolve; the outer layer of sites is
+/* boundary handling: `bc` for the x and y axes (the reference's xyBC), `bc_z`
+ * for z (zBC; 0 = the same as bc) */
+#define LAT_BC_PERIODIC  0   /* periodic (mpi_evolution.cpp:385-405)                         */
+#define LAT_BC_FIXED     1   /* only interior sites evolve; the outer layer of sites is
                                 held fixed (evolution.cpp:166-186 with xyBC/zBC "fixed";
                                 mooreEvol.cpp:187-189,672-692)                               */
+#define LAT_BC_NEUMANN   2   /* interior sites evolve; before each step the outer layer of
+                                the current level is set from the next layer in, phi
+                                transported along the link (evolution.cpp:194-265; the z
+                                pass covers x planes i < nz as the reference's does).
+                                Abelian-Higgs only                                           */
+#define LAT_BC_ABSORBING 3   /* x and y only: the outer layer evolves with the one-sided
+                                first-order absorbing updates of evolution.cpp:446-691 (and
+                                the whole layer is updated, :1375-1402). Abelian-Higgs only  */
+#define LAT_BCZ_AS_XY     0  /* bc_z values */
+#define LAT_BCZ_PERIODIC  1
+#define LAT_BCZ_FIXED     2
+#define LAT_BCZ_NEUMANN   3
 
 /* energy density variants (diagnostics) */
 #define LAT_ENERGY_EVOLUTION 0  /* evolution.cpp:322-334,398-427 and mooreEvol.cpp:341-391:
@@ -108,7 +121,9 @@ typedef struct lat_params {
     double tau0;           /* conformal time at step 0: tau = tau0 + TimeStep*dt (=1)    */
     int32_t energy_form;   /* LAT_ENERGY_*                                               */
     int32_t kernel_variant;/* 0: default kernels; 1: one-pass FP64 stencil (for checks)  */
-    double reserved[4];
+    int32_t bc_z;          /* LAT_BCZ_*: boundary of the z axis (0: the same as bc)        */
+    int32_t reserved_i;
+    double reserved[3];
 } lat_params;
 
 typedef struct lat_handle lat_handle;

@@ -120,17 +120,36 @@ int orc_get_threads(void)
 /* ------------------------------------------------------------------------- */
 typedef struct {
     int64_t nx, ny, nz, N, syz;
-    int lo, hix, hiy, hiz;   /* evolved region: [lo, hi) per axis */
+    int lox, loy, loz, hix, hiy, hiz;   /* evolved region: [lo, hi) per axis */
+    int kxy, kz;                        /* LAT_BC_* of the x/y axes and of z */
 } geo_t;
 
+/* the boundary kind of z: bc_z, or the same as bc */
+static int z_kind(const lat_params* p)
+{
+    switch (p->bc_z) {
+    case LAT_BCZ_PERIODIC: return LAT_BC_PERIODIC;
+    case LAT_BCZ_FIXED: return LAT_BC_FIXED;
+    case LAT_BCZ_NEUMANN: return LAT_BC_NEUMANN;
+    default: return p->bc;
+    }
+}
+
+/* evolution.cpp:166-186: every non-periodic axis evolves its interior */
 static geo_t make_geo(const lat_params* p)
 {
     geo_t g;
     g.nx = p->nx; g.ny = p->ny; g.nz = p->nz;
     g.N = g.nx * g.ny * g.nz;
     g.syz = g.ny * g.nz;
-    if (p->bc == LAT_BC_FIXED) { g.lo = 1; g.hix = (int)g.nx - 1; g.hiy = (int)g.ny - 1; g.hiz = (int)g.nz - 1; }
-    else { g.lo = 0; g.hix = (int)g.nx; g.hiy = (int)g.ny; g.hiz = (int)g.nz; }
+    g.kxy = p->bc;
+    g.kz = z_kind(p);
+    const int pxy = g.kxy == LAT_BC_PERIODIC, pz = g.kz == LAT_BC_PERIODIC;
+    g.lox = g.loy = pxy ? 0 : 1;
+    g.hix = pxy ? (int)g.nx : (int)g.nx - 1;
+    g.hiy = pxy ? (int)g.ny : (int)g.ny - 1;
+    g.loz = pz ? 0 : 1;
+    g.hiz = pz ? (int)g.nz : (int)g.nz - 1;
     return g;
 }
 
@@ -164,11 +183,11 @@ static void ah_update(const lat_params* p, double* st, int64_t n)
     const int c[2] = {1, -1};
 
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
-    for (int64_t i = G.lo; i < G.hix; ++i) {
+    for (int64_t i = G.lox; i < G.hix; ++i) {
         const int64_t ip = wrapp(i, G.nx), im = wrapm(i, G.nx);
-        for (int64_t j = G.lo; j < G.hiy; ++j) {
+        for (int64_t j = G.loy; j < G.hiy; ++j) {
             const int64_t jp = wrapp(j, G.ny), jm = wrapm(j, G.ny);
-            for (int64_t k = G.lo; k < G.hiz; ++k) {
+            for (int64_t k = G.loz; k < G.hiz; ++k) {
                 const int64_t kp = wrapp(k, G.nz), km = wrapm(k, G.nz);
                 const int64_t s = site(&G, i, j, k);
                 const int64_t ipx = site(&G, ip, j, k), imx = site(&G, im, j, k);
@@ -247,11 +266,11 @@ static void ah_diag(const lat_params* p, const double* st, int64_t n, lat_diag* 
     double energy = 0, dev = 0;
 
 #pragma omp parallel for schedule(static) reduction(+:energy,dev) num_threads(orc_get_threads())
-    for (int64_t i = G.lo; i < G.hix; ++i) {
+    for (int64_t i = G.lox; i < G.hix; ++i) {
         const int64_t ip = wrapp(i, G.nx), im = wrapm(i, G.nx);
-        for (int64_t j = G.lo; j < G.hiy; ++j) {
+        for (int64_t j = G.loy; j < G.hiy; ++j) {
             const int64_t jp = wrapp(j, G.ny), jm = wrapm(j, G.ny);
-            for (int64_t k = G.lo; k < G.hiz; ++k) {
+            for (int64_t k = G.loz; k < G.hiz; ++k) {
                 const int64_t kp = wrapp(k, G.nz), km = wrapm(k, G.nz);
                 const int64_t s = site(&G, i, j, k);
                 const int64_t ipx = site(&G, ip, j, k), imx = site(&G, im, j, k);
@@ -312,7 +331,7 @@ static void ah_diag(const lat_params* p, const double* st, int64_t n, lat_diag* 
     }
     out->energy = energy;
     out->gauss_abs_sum = dev;
-    out->sites = (int64_t)(G.hix - G.lo) * (G.hiy - G.lo) * (G.hiz - G.lo);
+    out->sites = (int64_t)(G.hix - G.lox) * (G.hiy - G.loy) * (G.hiz - G.loz);
     out->time_step = n;
 }
 
@@ -338,11 +357,11 @@ static void moore_update(const lat_params* p, double* st, int64_t n)
     const int c[2] = {1, -1};
 
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
-    for (int64_t i = G.lo; i < G.hix; ++i) {
+    for (int64_t i = G.lox; i < G.hix; ++i) {
         const int64_t ip = wrapp(i, G.nx), im = wrapm(i, G.nx);
-        for (int64_t j = G.lo; j < G.hiy; ++j) {
+        for (int64_t j = G.loy; j < G.hiy; ++j) {
             const int64_t jp = wrapp(j, G.ny), jm = wrapm(j, G.ny);
-            for (int64_t k = G.lo; k < G.hiz; ++k) {
+            for (int64_t k = G.loz; k < G.hiz; ++k) {
                 const int64_t kp = wrapp(k, G.nz), km = wrapm(k, G.nz);
                 const int64_t s = site(&G, i, j, k);
                 const int64_t ipx = site(&G, ip, j, k), imx = site(&G, im, j, k);
@@ -438,11 +457,11 @@ static void moore_diag(const lat_params* p, const double* st, int64_t n, lat_dia
     double energy = 0, dev = 0;
 
 #pragma omp parallel for schedule(static) reduction(+:energy,dev) num_threads(orc_get_threads())
-    for (int64_t i = G.lo; i < G.hix; ++i) {
+    for (int64_t i = G.lox; i < G.hix; ++i) {
         const int64_t ip = wrapp(i, G.nx), im = wrapm(i, G.nx);
-        for (int64_t j = G.lo; j < G.hiy; ++j) {
+        for (int64_t j = G.loy; j < G.hiy; ++j) {
             const int64_t jp = wrapp(j, G.ny), jm = wrapm(j, G.ny);
-            for (int64_t k = G.lo; k < G.hiz; ++k) {
+            for (int64_t k = G.loz; k < G.hiz; ++k) {
                 const int64_t kp = wrapp(k, G.nz), km = wrapm(k, G.nz);
                 const int64_t s = site(&G, i, j, k);
                 const int64_t ipx = site(&G, ip, j, k), imx = site(&G, im, j, k);
@@ -513,7 +532,7 @@ static void moore_diag(const lat_params* p, const double* st, int64_t n, lat_dia
     }
     out->energy = energy;
     out->gauss_abs_sum = dev;
-    out->sites = (int64_t)(G.hix - G.lo) * (G.hiy - G.lo) * (G.hiz - G.lo);
+    out->sites = (int64_t)(G.hix - G.lox) * (G.hiy - G.loy) * (G.hiz - G.loz);
     out->time_step = n;
 }
 
@@ -602,13 +621,13 @@ int orc_detect(const lat_params* p, const double* st, int64_t n, int field,
     const double dx = p->dx, dy = p->dy, dz = p->dz;
     const int64_t x0 = (int64_t)(0.5 * (G.nx - 1)), y0 = (int64_t)(0.5 * (G.ny - 1)), z0 = (int64_t)(0.5 * (G.nz - 1));
     sink_t o = {xyz, xyz ? cap : 0, 0};
-    for (int64_t i = G.lo; i < G.hix; ++i) {
+    for (int64_t i = G.lox; i < G.hix; ++i) {
         const int64_t ip = wrapp(i, G.nx);
         const double x = (double)(i - x0) * dx;
-        for (int64_t j = G.lo; j < G.hiy; ++j) {
+        for (int64_t j = G.loy; j < G.hiy; ++j) {
             const int64_t jp = wrapp(j, G.ny);
             const double y = (double)(j - y0) * dy;
-            for (int64_t k = G.lo; k < G.hiz; ++k) {
+            for (int64_t k = G.loz; k < G.hiz; ++k) {
                 const int64_t kp = wrapp(k, G.nz);
                 const double z = (double)(k - z0) * dz;
                 const int64_t s = site(&G, i, j, k);
@@ -665,7 +684,7 @@ int orc_winding(const lat_params* p, const double* st, int64_t n, int field,
     const int64_t N = G.N;
     const int tNow = (int)((n + 1) % 2);
     const int c0 = 2 * field;
-    const int fixed = p->bc == LAT_BC_FIXED;
+    const int pxy = G.kxy == LAT_BC_PERIODIC, pz = G.kz == LAT_BC_PERIODIC;
     int64_t tot = 0;
     if (out) memset(out, 0, (size_t)(3 * N));
     for (int64_t i = 0; i < G.nx; ++i) {
@@ -680,12 +699,9 @@ int orc_winding(const lat_params* p, const double* st, int64_t n, int field,
                     {s, site(&G, i, jp, k), site(&G, i, jp, kp), site(&G, i, j, kp)},
                     {s, site(&G, i, j, kp), site(&G, ip, j, kp), site(&G, ip, j, k)},
                     {s, site(&G, ip, j, k), site(&G, ip, jp, k), site(&G, i, jp, k)}};
-                int valid[3] = {1, 1, 1};
-                if (fixed) {
-                    valid[0] = (j + 1 < G.ny) && (k + 1 < G.nz);
-                    valid[1] = (k + 1 < G.nz) && (i + 1 < G.nx);
-                    valid[2] = (i + 1 < G.nx) && (j + 1 < G.ny);
-                }
+                /* a face is valid unless it wraps around a non-periodic axis */
+                const int xin = pxy || i + 1 < G.nx, yin = pxy || j + 1 < G.ny, zin = pz || k + 1 < G.nz;
+                const int valid[3] = {yin && zin, zin && xin, xin && yin};
                 for (int d = 0; d < 3; ++d) {
                     if (!valid[d]) continue;
                     int w = 0;
@@ -788,7 +804,8 @@ int orc_string_length(const lat_params* p, const double* xyz, int64_t M, int spl
     if (!p || (!xyz && M) || !L0 || !L1) return LAT_ERR_INVALID;
     const double dx = p->dx, dy = p->dy, dz = p->dz;
     const double bx = p->nx * dx, by = p->ny * dy, bz = p->nz * dz;
-    const int per = p->bc == LAT_BC_PERIODIC;
+    const geo_t G = make_geo(p);
+    const int pxy = G.kxy == LAT_BC_PERIODIC, pz = G.kz == LAT_BC_PERIODIC;
     const double c0 = dx * dx + dy * dy + dz * dz;
     const double cutoff = c0 * c0;
     *L0 = 0;
@@ -804,7 +821,7 @@ int orc_string_length(const lat_params* p, const double* xyz, int64_t M, int spl
         int64_t bi = -1;
         for (int64_t j = 0; j < M; ++j) {
             if (!alive[j] || j == f) continue;
-            const double d = chain_dist2(&xyz[3 * f], &xyz[3 * j], bx, by, bz, per, per);
+            const double d = chain_dist2(&xyz[3 * f], &xyz[3 * j], bx, by, bz, pxy, pz);
             if (d <= best) {
                 best = d;
                 bi = j;
@@ -819,7 +836,7 @@ int orc_string_length(const lat_params* p, const double* xyz, int64_t M, int spl
             alive[f] = 0;
             f = bi;
         } else {
-            const double d = chain_dist2(cf, begin, bx, by, bz, per, per);
+            const double d = chain_dist2(cf, begin, bx, by, bz, pxy, pz);
             if (d <= best) {
                 if (split && !inner) *L1 += sqrt(best);
                 else *L0 += sqrt(best);
