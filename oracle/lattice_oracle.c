@@ -171,11 +171,249 @@ static void friction_of(const lat_params* p, int64_t n, double* damp, double* fr
 /* Abelian-Higgs step: mpi_evolution.cpp:381-501 (== evolution.cpp:273-373 + */
 /* 1384-1402 for the fields).  Components: 0,1 = phi; 2,3,4 = theta_x,y,z.     */
 /* ------------------------------------------------------------------------- */
+/* ------------------------------------------------------------------------- */
+/* Neumann boundaries of the now level, in place (evolution.cpp:194-265): the  */
+/* y faces (x interior), then the x faces (all y), then the z faces, theta     */
+/* copied from the next layer in and phi transported along its link.  The z    */
+/* pass runs over x planes i < nz (and i < nx) as the reference's loop does.   */
+/* ------------------------------------------------------------------------- */
+#define TH(m, t, s) ST(2 + (m), t, s)
+#define PH(c, t, s) ST(c, t, s)
+
+static void neumann_pair(double* st, int64_t N, int tNow, int mu, int64_t b0, int64_t i0, int64_t b1, int64_t i1)
+{
+    const int c[2] = {1, -1};
+    for (int m = 0; m < 3; ++m) {
+        TH(m, tNow, b0) = TH(m, tNow, i0);
+        TH(m, tNow, b1) = TH(m, tNow, i1);
+    }
+    for (int comp = 0; comp < 2; ++comp) {
+        const int oc = comp + c[comp];
+        const double cc = (double)c[comp];
+        PH(comp, tNow, b0) = cos(TH(mu, tNow, b0)) * PH(comp, tNow, i0) + cc * sin(TH(mu, tNow, b0)) * PH(oc, tNow, i0);
+        PH(comp, tNow, b1) = cos(TH(mu, tNow, i1)) * PH(comp, tNow, i1) - cc * sin(TH(mu, tNow, i1)) * PH(oc, tNow, i1);
+    }
+}
+
+int orc_apply_boundaries(const lat_params* p, double* st, int64_t n)
+{
+    if (!p || !st) return LAT_ERR_INVALID;
+    const geo_t G = make_geo(p);
+    const int64_t N = G.N;
+    const int tNow = (int)((n + 1) % 2);
+    const int64_t nx = G.nx, ny = G.ny, nz = G.nz;
+    if (G.kxy == LAT_BC_NEUMANN) {
+        for (int64_t i = 1; i < nx - 1; ++i)
+            for (int64_t k = G.loz; k < G.hiz; ++k)
+                neumann_pair(st, N, tNow, 1, site(&G, i, 0, k), site(&G, i, 1, k), site(&G, i, ny - 1, k),
+                             site(&G, i, ny - 2, k));
+        for (int64_t j = 0; j < ny; ++j)
+            for (int64_t k = G.loz; k < G.hiz; ++k)
+                neumann_pair(st, N, tNow, 0, site(&G, 0, j, k), site(&G, 1, j, k), site(&G, nx - 1, j, k),
+                             site(&G, nx - 2, j, k));
+    }
+    if (G.kz == LAT_BC_NEUMANN) {
+        const int64_t ni = nz < nx ? nz : nx;
+        for (int64_t i = 0; i < ni; ++i)
+            for (int64_t j = 0; j < ny; ++j)
+                neumann_pair(st, N, tNow, 2, site(&G, i, j, 0), site(&G, i, j, 1), site(&G, i, j, nz - 1),
+                             site(&G, i, j, nz - 2));
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* absorbing x/y boundaries (evolution.cpp:446-691): second time derivatives  */
+/* of the outer layer from one-sided first-order formulas, into btt[5][N]     */
+/* (boundary sites only); written before the interior update overwrites the  */
+/* past level it reads.                                                       */
+/* ------------------------------------------------------------------------- */
+/* covariant second difference along mu at s (neighbours sp, sm) */
+static double cov2(const double* st, int64_t N, int tNow, int comp, int mu, int64_t s, int64_t sp, int64_t sm, double d)
+{
+    const int c[2] = {1, -1};
+    const int oc = comp + c[comp];
+    const double cc = (double)c[comp];
+    return (cos(TH(mu, tNow, s)) * PH(comp, tNow, sp) + cc * sin(TH(mu, tNow, s)) * PH(oc, tNow, sp) - 2 * PH(comp, tNow, s)
+            + cos(TH(mu, tNow, sm)) * PH(comp, tNow, sm) - cc * sin(TH(mu, tNow, sm)) * PH(oc, tNow, sm)) / (d * d);
+}
+
+/* one-sided time-space difference at the low face: s0 boundary, s1 = s0 + mu */
+static double near_ts(const double* st, int64_t N, int tNow, int tPast, int comp, int mu, int64_t s0, int64_t s1,
+                      double dt, double d)
+{
+    const int c[2] = {1, -1};
+    const int oc = comp + c[comp];
+    const double cc = (double)c[comp];
+    return (cos(TH(mu, tNow, s0)) * PH(comp, tNow, s1) + cc * sin(TH(mu, tNow, s0)) * PH(oc, tNow, s1) - PH(comp, tNow, s0)
+            - cos(TH(mu, tPast, s0)) * PH(comp, tPast, s1) - cc * sin(TH(mu, tPast, s0)) * PH(oc, tPast, s1)
+            + PH(comp, tPast, s0)) / (dt * d);
+}
+
+/* at the high face: s0 boundary, s1 = s0 - mu; the past cos reads the link at sc
+ * (s1, except at the (nx-1, ny-1) corner's x term, evolution.cpp:656) */
+static double far_ts(const double* st, int64_t N, int tNow, int tPast, int comp, int mu, int64_t s0, int64_t s1,
+                     int64_t sc, double dt, double d)
+{
+    const int c[2] = {1, -1};
+    const int oc = comp + c[comp];
+    const double cc = (double)c[comp];
+    return (PH(comp, tNow, s0) - cos(TH(mu, tNow, s1)) * PH(comp, tNow, s1) + cc * sin(TH(mu, tNow, s1)) * PH(oc, tNow, s1)
+            - PH(comp, tPast, s0) + cos(TH(mu, tPast, sc)) * PH(comp, tPast, s1)
+            - cc * sin(TH(mu, tPast, s1)) * PH(oc, tPast, s1)) / (dt * d);
+}
+
+static double th2(const double* st, int64_t N, int tNow, int m, int64_t sp, int64_t s, int64_t sm, double d)
+{
+    return (TH(m, tNow, sp) - 2 * TH(m, tNow, s) + TH(m, tNow, sm)) / (d * d);
+}
+
+static double th_near(const double* st, int64_t N, int tNow, int tPast, int m, int64_t s0, int64_t s1, double dt, double d)
+{
+    return (TH(m, tNow, s1) - TH(m, tNow, s0) - TH(m, tPast, s1) + TH(m, tPast, s0)) / (dt * d);
+}
+
+static double th_far(const double* st, int64_t N, int tNow, int tPast, int m, int64_t s0, int64_t s1, double dt, double d)
+{
+    return (TH(m, tNow, s0) - TH(m, tNow, s1) - TH(m, tPast, s0) + TH(m, tPast, s1)) / (dt * d);
+}
+
+#define BTT(c, s) btt[(int64_t)(c) * N + (s)]
+
+static void absorb_tt(const lat_params* p, const double* st, int64_t n, double* btt)
+{
+    const geo_t G = make_geo(p);
+    const int64_t N = G.N, nx = G.nx, ny = G.ny, nz = G.nz;
+    const int tNow = (int)((n + 1) % 2), tPast = (int)(n % 2);
+    const double dx = p->dx, dy = p->dy, dz = p->dz, dt = p->dt;
+    for (int64_t k = G.loz; k < G.hiz; ++k) {
+        const int64_t kp = (k + 1) % nz, km = (k - 1 + nz) % nz;
+        /* x faces (evolution.cpp:447-509) */
+        for (int64_t j = 1; j < ny - 1; ++j) {
+            const int64_t a = site(&G, 0, j, k), b = site(&G, nx - 1, j, k);
+            for (int comp = 0; comp < 2; ++comp) {
+                double yy = cov2(st, N, tNow, comp, 1, a, site(&G, 0, j + 1, k), site(&G, 0, j - 1, k), dy);
+                double zz = cov2(st, N, tNow, comp, 2, a, site(&G, 0, j, kp), site(&G, 0, j, km), dz);
+                double tx = near_ts(st, N, tNow, tPast, comp, 0, a, site(&G, 1, j, k), dt, dx);
+                BTT(comp, a) = tx + 0.5 * (yy + zz);
+                yy = cov2(st, N, tNow, comp, 1, b, site(&G, nx - 1, j + 1, k), site(&G, nx - 1, j - 1, k), dy);
+                zz = cov2(st, N, tNow, comp, 2, b, site(&G, nx - 1, j, kp), site(&G, nx - 1, j, km), dz);
+                const int64_t b1 = site(&G, nx - 2, j, k);
+                tx = far_ts(st, N, tNow, tPast, comp, 0, b, b1, b1, dt, dx);
+                BTT(comp, b) = -tx + 0.5 * (yy + zz);
+            }
+            for (int m = 0; m < 3; ++m) {
+                double yy = th2(st, N, tNow, m, site(&G, 0, j + 1, k), a, site(&G, 0, j - 1, k), dy);
+                double zz = th2(st, N, tNow, m, site(&G, 0, j, kp), a, site(&G, 0, j, km), dz);
+                double tx = th_near(st, N, tNow, tPast, m, a, site(&G, 1, j, k), dt, dx);
+                BTT(2 + m, a) = tx + 0.5 * (yy + zz);
+                yy = th2(st, N, tNow, m, site(&G, nx - 1, j + 1, k), b, site(&G, nx - 1, j - 1, k), dy);
+                zz = th2(st, N, tNow, m, site(&G, nx - 1, j, kp), b, site(&G, nx - 1, j, km), dz);
+                tx = th_far(st, N, tNow, tPast, m, b, site(&G, nx - 2, j, k), dt, dx);
+                BTT(2 + m, b) = -tx + 0.5 * (yy + zz);
+            }
+        }
+        /* y faces (:511-573) */
+        for (int64_t i = 1; i < nx - 1; ++i) {
+            const int64_t a = site(&G, i, 0, k), b = site(&G, i, ny - 1, k);
+            for (int comp = 0; comp < 2; ++comp) {
+                double xx = cov2(st, N, tNow, comp, 0, a, site(&G, i + 1, 0, k), site(&G, i - 1, 0, k), dx);
+                double zz = cov2(st, N, tNow, comp, 2, a, site(&G, i, 0, kp), site(&G, i, 0, km), dz);
+                double ty = near_ts(st, N, tNow, tPast, comp, 1, a, site(&G, i, 1, k), dt, dy);
+                BTT(comp, a) = ty + 0.5 * (xx + zz);
+                xx = cov2(st, N, tNow, comp, 0, b, site(&G, i + 1, ny - 1, k), site(&G, i - 1, ny - 1, k), dx);
+                zz = cov2(st, N, tNow, comp, 2, b, site(&G, i, ny - 1, kp), site(&G, i, ny - 1, km), dz);
+                const int64_t b1 = site(&G, i, ny - 2, k);
+                ty = far_ts(st, N, tNow, tPast, comp, 1, b, b1, b1, dt, dy);
+                BTT(comp, b) = -ty + 0.5 * (xx + zz);
+            }
+            for (int m = 0; m < 3; ++m) {
+                double xx = th2(st, N, tNow, m, site(&G, i + 1, 0, k), a, site(&G, i - 1, 0, k), dx);
+                double zz = th2(st, N, tNow, m, site(&G, i, 0, kp), a, site(&G, i, 0, km), dz);
+                double ty = th_near(st, N, tNow, tPast, m, a, site(&G, i, 1, k), dt, dy);
+                BTT(2 + m, a) = ty + 0.5 * (xx + zz);
+                xx = th2(st, N, tNow, m, site(&G, i + 1, ny - 1, k), b, site(&G, i - 1, ny - 1, k), dx);
+                zz = th2(st, N, tNow, m, site(&G, i, ny - 1, kp), b, site(&G, i, ny - 1, km), dz);
+                ty = th_far(st, N, tNow, tPast, m, b, site(&G, i, ny - 2, k), dt, dy);
+                BTT(2 + m, b) = -ty + 0.5 * (xx + zz);
+            }
+        }
+        /* corners (:575-689) */
+        const int64_t c00 = site(&G, 0, 0, k), c01 = site(&G, 0, ny - 1, k);
+        const int64_t c10 = site(&G, nx - 1, 0, k), c11 = site(&G, nx - 1, ny - 1, k);
+        for (int comp = 0; comp < 2; ++comp) {
+            double zz = cov2(st, N, tNow, comp, 2, c00, site(&G, 0, 0, kp), site(&G, 0, 0, km), dz);
+            double tx = near_ts(st, N, tNow, tPast, comp, 0, c00, site(&G, 1, 0, k), dt, dx);
+            double ty = near_ts(st, N, tNow, tPast, comp, 1, c00, site(&G, 0, 1, k), dt, dy);
+            BTT(comp, c00) = (zz + 2 * (tx + ty)) / 3;
+            zz = cov2(st, N, tNow, comp, 2, c01, site(&G, 0, ny - 1, kp), site(&G, 0, ny - 1, km), dz);
+            tx = near_ts(st, N, tNow, tPast, comp, 0, c01, site(&G, 1, ny - 1, k), dt, dx);
+            int64_t s1 = site(&G, 0, ny - 2, k);
+            ty = far_ts(st, N, tNow, tPast, comp, 1, c01, s1, s1, dt, dy);
+            BTT(comp, c01) = (zz + 2 * (tx - ty)) / 3;
+            zz = cov2(st, N, tNow, comp, 2, c10, site(&G, nx - 1, 0, kp), site(&G, nx - 1, 0, km), dz);
+            s1 = site(&G, nx - 2, 0, k);
+            tx = far_ts(st, N, tNow, tPast, comp, 0, c10, s1, s1, dt, dx);
+            ty = near_ts(st, N, tNow, tPast, comp, 1, c10, site(&G, nx - 1, 1, k), dt, dy);
+            BTT(comp, c10) = (zz - 2 * (tx - ty)) / 3;
+            zz = cov2(st, N, tNow, comp, 2, c11, site(&G, nx - 1, ny - 1, kp), site(&G, nx - 1, ny - 1, km), dz);
+            tx = far_ts(st, N, tNow, tPast, comp, 0, c11, site(&G, nx - 2, ny - 1, k), c11, dt, dx);
+            s1 = site(&G, nx - 1, ny - 2, k);
+            ty = far_ts(st, N, tNow, tPast, comp, 1, c11, s1, s1, dt, dy);
+            BTT(comp, c11) = (zz - 2 * (tx + ty)) / 3;
+        }
+        for (int m = 0; m < 3; ++m) {
+            double zz = th2(st, N, tNow, m, site(&G, 0, 0, kp), c00, site(&G, 0, 0, km), dz);
+            double tx = th_near(st, N, tNow, tPast, m, c00, site(&G, 1, 0, k), dt, dx);
+            double ty = th_near(st, N, tNow, tPast, m, c00, site(&G, 0, 1, k), dt, dy);
+            BTT(2 + m, c00) = (zz + 2 * (tx + ty)) / 3;
+            zz = th2(st, N, tNow, m, site(&G, 0, ny - 1, kp), c01, site(&G, 0, ny - 1, km), dz);
+            tx = th_near(st, N, tNow, tPast, m, c01, site(&G, 1, ny - 1, k), dt, dx);
+            ty = th_far(st, N, tNow, tPast, m, c01, site(&G, 0, ny - 2, k), dt, dy);
+            BTT(2 + m, c01) = (zz + 2 * (tx - ty)) / 3;
+            zz = th2(st, N, tNow, m, site(&G, nx - 1, 0, kp), c10, site(&G, nx - 1, 0, km), dz);
+            tx = th_far(st, N, tNow, tPast, m, c10, site(&G, nx - 2, 0, k), dt, dx);
+            ty = th_near(st, N, tNow, tPast, m, c10, site(&G, nx - 1, 1, k), dt, dy);
+            BTT(2 + m, c10) = (zz - 2 * (tx - ty)) / 3;
+            zz = th2(st, N, tNow, m, site(&G, nx - 1, ny - 1, kp), c11, site(&G, nx - 1, ny - 1, km), dz);
+            tx = th_far(st, N, tNow, tPast, m, c11, site(&G, nx - 2, ny - 1, k), dt, dx);
+            ty = th_far(st, N, tNow, tPast, m, c11, site(&G, nx - 1, ny - 2, k), dt, dy);
+            BTT(2 + m, c11) = (zz - 2 * (tx + ty)) / 3;
+        }
+    }
+}
+
+/* the outer x/y layer's update with btt (evolution.cpp:1375-1402) */
+static void absorb_update(const lat_params* p, double* st, int64_t n, const double* btt)
+{
+    const geo_t G = make_geo(p);
+    const int64_t N = G.N, nx = G.nx, ny = G.ny;
+    const int tNow = (int)((n + 1) % 2), tPast = (int)(n % 2);
+    const double dt = p->dt;
+    for (int64_t i = 0; i < nx; ++i)
+        for (int64_t j = 0; j < ny; ++j) {
+            if (i != 0 && i != nx - 1 && j != 0 && j != ny - 1) continue;
+            for (int64_t k = G.loz; k < G.hiz; ++k) {
+                const int64_t s = site(&G, i, j, k);
+                for (int c = 0; c < 5; ++c)
+                    ST(c, tPast, s) = 2 * ST(c, tNow, s) - ST(c, tPast, s) + dt * dt * BTT(c, s);
+            }
+        }
+}
+
+#undef TH
+#undef PH
+
 static void ah_update(const lat_params* p, double* st, int64_t n)
 {
     const geo_t G = make_geo(p);
     const int64_t N = G.N;
     const int tNow = (int)((n + 1) % 2), tPast = (int)(n % 2);
+    double* btt = NULL;
+    if (G.kxy == LAT_BC_ABSORBING) {
+        btt = (double*)calloc((size_t)(5 * N), sizeof(double));
+        if (btt) absorb_tt(p, st, n, btt);
+    }
     double damp, fric;
     friction_of(p, n, &damp, &fric);
     const double dx = p->dx, dy = p->dy, dz = p->dz, dt = p->dt;
@@ -249,6 +487,10 @@ static void ah_update(const lat_params* p, double* st, int64_t n)
                     ST(2 + m, tPast, s) = 2 * ST(2 + m, tNow, s) - ST(2 + m, tPast, s) + dt * dt * tt[m];
             }
         }
+    }
+    if (btt) {
+        absorb_update(p, st, n, btt);
+        free(btt);
     }
 }
 
@@ -547,6 +789,7 @@ int orc_diagnostics(const lat_params* p, const double* st, int64_t n, lat_diag* 
 int orc_step(const lat_params* p, double* st, int64_t n, lat_diag* diag)
 {
     if (!p || !st) return LAT_ERR_INVALID;
+    orc_apply_boundaries(p, st, n);  /* evolution.cpp:194-265: before the derivatives */
     if (diag) orc_diagnostics(p, st, n, diag);
     if (p->model == LAT_MODEL_MOORE) moore_update(p, st, n);
     else ah_update(p, st, n);

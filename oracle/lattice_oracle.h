@@ -41,6 +41,12 @@ int orc_random_phase_ic(const lat_params* p, uint32_t seed, int independent, dou
 void orc_set_threads(int n);
 int orc_get_threads(void);
 
+/* Neumann boundaries (bc or bc_z LAT_BC_NEUMANN) of level n, in place
+ * (evolution.cpp:194-265).  orc_step applies them first; a caller that reads
+ * level n as the reference's loop body does after its boundary step (crossing
+ * detection) applies them before.  Idempotent. */
+int orc_apply_boundaries(const lat_params* p, double* st, int64_t n);
+
 /* One leapfrog step at TimeStep n, in place.  If diag != NULL the
  * diagnostics of the level n (before the update) are computed first. */
 int orc_step(const lat_params* p, double* st, int64_t n, lat_diag* diag);

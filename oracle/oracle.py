@@ -53,6 +53,7 @@ def lib():
         L.orc_mt_seed.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
         L.orc_uniform_0_2pi.argtypes = [ctypes.c_void_p]
         L.orc_uniform_0_2pi.restype = ctypes.c_double
+        L.orc_apply_boundaries.argtypes = [P(LatParams), dp, ctypes.c_int64]
         L.orc_icfunc_random_ic.argtypes = [P(LatParams), ctypes.c_uint32, dp]
         L.orc_string_length.argtypes = [P(LatParams), dp, ctypes.c_int64, ctypes.c_int, dp, dp]
         _lib = L
@@ -138,6 +139,13 @@ def winding(p: LatParams, st: np.ndarray, n: int, field: int = 0):
     if rc != 0:
         raise RuntimeError(f"orc_winding rc={rc}")
     return out, int(tot.value)
+
+
+def apply_boundaries(p: LatParams, st: np.ndarray, n: int) -> None:
+    """Neumann boundaries of level n in place (evolution.cpp:194-265)."""
+    rc = lib().orc_apply_boundaries(ctypes.byref(p), _dp(st), int(n))
+    if rc != 0:
+        raise RuntimeError(f"orc_apply_boundaries rc={rc}")
 
 
 def icfunc_random_ic(p: LatParams, seed: int) -> np.ndarray:

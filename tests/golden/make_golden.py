@@ -143,15 +143,24 @@ def _two_level_ic(rng, N, ncomp_phi, amp_theta):
     return now, past
 
 
-def gen_evolution(name, nx, ny, nz, nt, lam, g, alpha, bc, seed, saveFreq=4, dt=0.1, d=0.5):
+XY_KIND = {"periodic": BC_PERIODIC, "neumann": 2, "absorbing": 3}
+Z_KIND = {"periodic": 1, "neumann": 3}
+
+
+def gen_evolution(name, nx, ny, nz, nt, lam, g, alpha, bc, seed, saveFreq=4, dt=0.1, d=0.5, xyBC=None, zBC=None):
+    """evolution.cpp; xyBC / zBC (the reference's strings) default to bc for all axes."""
     rng = np.random.default_rng(seed)
     N = nx * ny * nz
     now, past = _two_level_ic(rng, N, 2, 0.4)
     bcs = "periodic" if bc == BC_PERIODIC else "fixed"
+    xyBC = xyBC or bcs
+    zBC = zBC or bcs
+    bc = XY_KIND.get(xyBC, BC_FIXED)
+    bc_z = Z_KIND.get(zBC, 2)
     consts = {"nx": nx, "ny": ny, "nz": nz, "nt": nt, "dx": d, "dy": d, "dz": d, "dt": dt,
               "lambda": lam, "eta": 1.0, "g": g, "damped_nt": 0, "dampFac": 0.0, "alpha": alpha,
               "scaling": 1.0, "makeGif": False, "makeStringPosGif": True, "saveFreq": saveFreq,
-              "xyBC": bcs, "zBC": bcs, "stringPos": False, "stationary_ic": False,
+              "xyBC": xyBC, "zBC": zBC, "stringPos": False, "stationary_ic": False,
               "stringDetect": True, "detectBuffer": False, "splitLength": False, "finalOut": True}
     build_ref.build("evolution", name, consts)
     # "data" IC: level block 0 = slot 0 (past at step 0), block 1 = slot 1 (now)
@@ -165,7 +174,7 @@ def gen_evolution(name, nx, ny, nz, nt, lam, g, alpha, bc, seed, saveFreq=4, dt=
     frames = read_frames(work, "gifStringPosData_")
     counts, xyz = pack_frames(frames)
     p = make_params(MODEL_AH, nx=nx, ny=ny, nz=nz, d=d, dt=dt, lam=lam, eta=1.0, g=g, damped_nt=0,
-                    dampFac=0.0, alpha=alpha, scaling=1.0, tau0=1.0, energy_form=ENERGY_EVOLUTION, bc=bc)
+                    dampFac=0.0, alpha=alpha, scaling=1.0, tau0=1.0, energy_form=ENERGY_EVOLUTION, bc=bc, bc_z=bc_z)
     ic = np.stack([past, now], axis=1)  # (comp, slot, N)
     np.savez_compressed(OUT / f"{name}.npz", program="evolution", params=_params_json(p), nt=nt,
                         save_freq=saveFreq, ic=ic, final_newest=final_newest, energy=vals[:, 0],
@@ -261,6 +270,17 @@ def main():
     gen_icw_length("ref_icw_len_fixed", 15, 15, 15, 25, BC_FIXED, seed=5)
     gen_icw_length("ref_icw_len_nosplit", 11, 13, 9, 12, BC_PERIODIC, seed=6, d=0.5, split=False)
     gen_initial_conditions("ref_initial_conditions", 7, 6, 5, seed=42, mean=0.0, stdev=0.5, g=0.5)
+    # boundary kinds of evolution.cpp:166-265,446-691,1375-1408 (nz <= nx for a Neumann z, see orc_apply_boundaries)
+    gen_evolution("ref_evol_bc_neumann", 10, 9, 8, 10, lam=2.0, g=0.7, alpha=3.0, bc=BC_FIXED, seed=21, saveFreq=3,
+                  xyBC="neumann", zBC="neumann")
+    gen_evolution("ref_evol_bc_absorbing", 11, 10, 8, 12, lam=2.0, g=0.7, alpha=0.0, bc=BC_FIXED, seed=22, saveFreq=4,
+                  xyBC="absorbing", zBC="periodic")
+    gen_evolution("ref_evol_bc_absorbing_neumann", 10, 10, 7, 10, lam=1.0, g=1.0, alpha=3.0, bc=BC_FIXED, seed=23,
+                  saveFreq=5, xyBC="absorbing", zBC="neumann")
+    gen_evolution("ref_evol_bc_fixed_zper", 9, 9, 8, 8, lam=2.0, g=0.7, alpha=0.0, bc=BC_FIXED, seed=24, saveFreq=4,
+                  xyBC="fixed", zBC="periodic")
+    gen_evolution("ref_evol_bc_per_zfixed", 9, 8, 9, 8, lam=2.0, g=0.7, alpha=3.0, bc=BC_FIXED, seed=25, saveFreq=4,
+                  xyBC="periodic", zBC="fixed")
 
 
 if __name__ == "__main__":

@@ -13,6 +13,17 @@ from conftest import load_golden, params_from_json
 
 MPI_CASES = ["ref_mpi_ah_c1", "ref_mpi_ah_prs", "ref_mpi_ah_global", "ref_moore_mpi"]
 OMP_CASES = ["ref_evol_ah_periodic", "ref_evol_ah_fixed", "ref_moore_evol"]
+BC_CASES = ["ref_evol_bc_neumann", "ref_evol_bc_absorbing", "ref_evol_bc_absorbing_neumann",
+            "ref_evol_bc_fixed_zper", "ref_evol_bc_per_zfixed"]
+
+
+def evolution_deviation(p, D):
+    """evolution.cpp:1404-1408: the x/y and z normalisations follow each axis's boundary."""
+    from axions_gb300.params import BCZ_AS_XY, BCZ_PERIODIC, BC_PERIODIC
+    pxy = p.bc == BC_PERIODIC
+    pz = p.bc_z == BCZ_PERIODIC or (p.bc_z == BCZ_AS_XY and pxy)
+    D = D / (p.nx * p.ny) if pxy else D / ((p.nx - 2) * (p.ny - 2))
+    return D / p.nz if pz else D / (p.nz - 2)
 
 
 def test_random_ic_matches_reference_mt19937(oracle_mod):
@@ -49,7 +60,7 @@ def test_mpi_programs_bit_exact(oracle_mod, name):
     assert np.array_equal(np.concatenate(frames), z["frame_xyz"])
 
 
-@pytest.mark.parametrize("name", OMP_CASES)
+@pytest.mark.parametrize("name", OMP_CASES + BC_CASES)
 def test_openmp_programs_bit_exact(oracle_mod, name):
     O = oracle_mod
     O.set_threads(1)
@@ -61,6 +72,7 @@ def test_openmp_programs_bit_exact(oracle_mod, name):
     E, D, frames = [], [], []
     for n in range(nt):
         if sf and n % sf == 0:
+            O.apply_boundaries(p, st, n)   # detection reads the level after its boundary step
             frames.append(O.detect(p, st, n, 0))
         d = O.step(p, st, n, diag=True)
         E.append(d.energy)
@@ -69,11 +81,7 @@ def test_openmp_programs_bit_exact(oracle_mod, name):
     assert np.array_equal(st[:, (nt + 1) % 2, :], z["final_newest"])
     assert np.array_equal(E, z["energy"])
     if p.model == 0:
-        if p.bc == 0:
-            dev = D / (p.nx * p.ny) / p.nz                      # evolution.cpp:1404-1408
-        else:
-            dev = D / ((p.nx - 2) * (p.ny - 2)) / (p.nz - 2)
-        assert np.array_equal(dev, z["deviation"])
+        assert np.array_equal(evolution_deviation(p, D), z["deviation"])
     else:
         c = (p.nx - 2) * (p.ny - 2) * (p.nz - 2)               # mooreEvol.cpp:383,697
         np.testing.assert_allclose(D / c / c, z["deviation"], rtol=1e-13, atol=0)
