@@ -19,9 +19,9 @@ __global__ void __launch_bounds__(BLOCK) ah_step_kernel(const Geom g, const Fiel
                                                         const DiagOut d)
 {
     using TR = Trig<T>;
-    const int k = g.lo + (int)(blockIdx.x * BZ + threadIdx.x);
-    const int j = g.lo + (int)(blockIdx.y * BY + threadIdx.y);
-    const int i = g.lo + (int)blockIdx.z;
+    const int k = g.loz + (int)(blockIdx.x * BZ + threadIdx.x);
+    const int j = g.loy + (int)(blockIdx.y * BY + threadIdx.y);
+    const int i = g.lox + (int)blockIdx.z;
     double e_site = 0.0, g_site = 0.0;
 
     if (k < g.hiz && j < g.hiy) {
@@ -207,9 +207,9 @@ __global__ void __launch_bounds__(BLOCK) divergence_kernel(const Geom g, const T
                                                            const T* __restrict__ TY, const T* __restrict__ TZ,
                                                            const StepCoefT<T> c, T* __restrict__ out)
 {
-    const int k = g.lo + (int)(blockIdx.x * BZ + threadIdx.x);
-    const int j = g.lo + (int)(blockIdx.y * BY + threadIdx.y);
-    const int i = g.lo + (int)blockIdx.z;
+    const int k = g.loz + (int)(blockIdx.x * BZ + threadIdx.x);
+    const int j = g.loy + (int)(blockIdx.y * BY + threadIdx.y);
+    const int i = g.lox + (int)blockIdx.z;
     if (k >= g.hiz || j >= g.hiy) return;
     const Nbr n = make_nbr(g, i, j, k);
     const int s = n.s;

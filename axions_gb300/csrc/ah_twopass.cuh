@@ -110,9 +110,9 @@ __global__ void __launch_bounds__(BLOCK) ah_update_kernel(const Geom g, const Fi
                                                           const double* __restrict__ L, const int N, const StepCoef c,
                                                           const DiagOut d)
 {
-    const int k = g.lo + (int)(blockIdx.x * BZ + threadIdx.x);
-    const int j = g.lo + (int)(blockIdx.y * BY + threadIdx.y);
-    const int i = g.lo + (int)blockIdx.z;
+    const int k = g.loz + (int)(blockIdx.x * BZ + threadIdx.x);
+    const int j = g.loy + (int)(blockIdx.y * BY + threadIdx.y);
+    const int i = g.lox + (int)blockIdx.z;
     double e_site = 0.0, g_site = 0.0;
 
     if (k < g.hiz && j < g.hiy) {
@@ -259,7 +259,7 @@ cudaError_t launch_ah_twopass(const Geom& g, const Fields<double, 5>& f, double*
 {
     const int N = g.nx * g.syz;
     Geom all = g;
-    all.lo = 0;
+    all.lox = all.loy = all.loz = 0;
     all.hix = g.nx;
     all.hiy = g.ny;
     all.hiz = g.nz;

@@ -279,6 +279,10 @@ int lat_batch_add(lat_batch* b, lat_handle* h, int32_t diag_every, int64_t stop_
         set_error("lat_batch_add: batches step FP32 lattices (LAT_F32, default kernels)");
         return LAT_ERR_INVALID;
     }
+    if (h->p.bc > LAT_BC_FIXED || bc_z_kind(h->p) > LAT_BC_FIXED) {
+        set_error("lat_batch_add: batches step lattices with periodic or fixed boundaries");
+        return LAT_ERR_INVALID;
+    }
     if ((int)b->jobs.size() >= b->max_jobs) {
         set_error("lat_batch_add: batch is full");
         return LAT_ERR_CAPACITY;
@@ -395,7 +399,7 @@ int lat_batch_advance(lat_batch* b, int32_t nsteps)
             // lattice marches long x-ranges (one prologue per 128 planes).  The
             // value depends on the lattice's own shape only, never on its
             // company, so results do not depend on the mix.
-            J.chunk = std::min(h->geom.hix - h->geom.lo, 128);
+            J.chunk = std::min(h->geom.hix - h->geom.lox, 128);
             const dim3 tg = tiled_grid(h->geom, J.chunk);
             J.tiles_z = (int)tg.x;
             J.tiles_y = (int)tg.y;
@@ -420,7 +424,7 @@ int lat_batch_advance(lat_batch* b, int32_t nsteps)
             dg.energy = v[0];
             dg.gauss_abs_sum = v[1];
             const Geom& g = h->geom;
-            dg.sites = (int64_t)(g.hix - g.lo) * (g.hiy - g.lo) * (g.hiz - g.lo);
+            dg.sites = (int64_t)(g.hix - g.lox) * (g.hiy - g.loy) * (g.hiz - g.loz);
             dg.time_step = plan[q].n0 + s;
             j.diags.push_back(dg);
         }

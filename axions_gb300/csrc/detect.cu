@@ -82,7 +82,7 @@ __device__ __forceinline__ bool site_roots(const DetectArgs& a, const T* __restr
     const int rem = s - i * a.syz;
     const int j = rem / a.nz;
     const int k = rem - j * a.nz;
-    if (i < a.lo || i >= a.hix || j < a.lo || j >= a.hiy || k < a.lo || k >= a.hiz) return false;
+    if (i < a.lox || i >= a.hix || j < a.loy || j >= a.hiy || k < a.loz || k >= a.hiz) return false;
     const int oxp = (i + 1 == a.nx) ? -(a.nx - 1) * a.syz : a.syz;
     const int oyp = (j + 1 == a.ny) ? -(a.ny - 1) * a.nz : a.nz;
     const int ozp = (k + 1 == a.nz) ? -(a.nz - 1) : 1;
@@ -215,7 +215,7 @@ __device__ __forceinline__ int edge_cross(T ax, T ay, T bx, T by)
 }
 
 template <class T>
-__global__ void __launch_bounds__(DB) winding_kernel(const DetectArgs a, int fixed, const T* __restrict__ re,
+__global__ void __launch_bounds__(DB) winding_kernel(const DetectArgs a, int open_axes, const T* __restrict__ re,
                                                      const T* __restrict__ im, int8_t* out,
                                                      unsigned long long* abs_sum)
 {
@@ -235,8 +235,10 @@ __global__ void __launch_bounds__(DB) winding_kernel(const DetectArgs a, int fix
         const int cs[3][4] = {{s, s + oyp, s + oyp + ozp, s + ozp},
                               {s, s + ozp, s + ozp + oxp, s + oxp},
                               {s, s + oxp, s + oxp + oyp, s + oyp}};
-        const bool valid[3] = {!fixed || (j + 1 < a.ny && k + 1 < a.nz), !fixed || (k + 1 < a.nz && i + 1 < a.nx),
-                               !fixed || (i + 1 < a.nx && j + 1 < a.ny)};
+        // a face is valid unless it wraps around a non-periodic axis (bit 0: x/y, bit 1: z)
+        const bool xin = !(open_axes & 1) || i + 1 < a.nx, yin = !(open_axes & 1) || j + 1 < a.ny;
+        const bool zin = !(open_axes & 2) || k + 1 < a.nz;
+        const bool valid[3] = {yin && zin, zin && xin, xin && yin};
         T vr[3][4], vi[3][4];
 #pragma unroll
         for (int d = 0; d < 3; ++d)
@@ -303,16 +305,16 @@ cudaError_t launch_detect_write_f32(const DetectArgs& a, const float* re, const 
     detect_write_kernel<float><<<nb, DB, 0, st>>>(a, re, im, bo, xyz, cap);
     return cudaGetLastError();
 }
-cudaError_t launch_winding_f64(const DetectArgs& a, int fixed, const double* re, const double* im, int8_t* out,
+cudaError_t launch_winding_f64(const DetectArgs& a, int open_axes, const double* re, const double* im, int8_t* out,
                                unsigned long long* abs_sum, cudaStream_t st)
 {
-    winding_kernel<double><<<nblocks_of(a), DB, 0, st>>>(a, fixed, re, im, out, abs_sum);
+    winding_kernel<double><<<nblocks_of(a), DB, 0, st>>>(a, open_axes, re, im, out, abs_sum);
     return cudaGetLastError();
 }
-cudaError_t launch_winding_f32(const DetectArgs& a, int fixed, const float* re, const float* im, int8_t* out,
+cudaError_t launch_winding_f32(const DetectArgs& a, int open_axes, const float* re, const float* im, int8_t* out,
                                unsigned long long* abs_sum, cudaStream_t st)
 {
-    winding_kernel<float><<<nblocks_of(a), DB, 0, st>>>(a, fixed, re, im, out, abs_sum);
+    winding_kernel<float><<<nblocks_of(a), DB, 0, st>>>(a, open_axes, re, im, out, abs_sum);
     return cudaGetLastError();
 }
 

@@ -15,6 +15,18 @@ namespace lat {
 thread_local std::string g_err;
 void set_error(const std::string& m) { g_err = m; }
 
+int bc_z_kind(const lat_params& p)
+{
+    switch (p.bc_z) {
+    case LAT_BCZ_PERIODIC: return LAT_BC_PERIODIC;
+    case LAT_BCZ_FIXED: return LAT_BC_FIXED;
+    case LAT_BCZ_NEUMANN: return LAT_BC_NEUMANN;
+    default: return p.bc;
+    }
+}
+
+// evolution.cpp:166-186: a periodic axis evolves every site, any other kind
+// its interior (Neumann and absorbing layers are set or evolved separately)
 Geom make_geom(const lat_params& p)
 {
     Geom g;
@@ -22,17 +34,12 @@ Geom make_geom(const lat_params& p)
     g.ny = (int)p.ny;
     g.nz = (int)p.nz;
     g.syz = g.ny * g.nz;
-    if (p.bc == LAT_BC_FIXED) {
-        g.lo = 1;
-        g.hix = g.nx - 1;
-        g.hiy = g.ny - 1;
-        g.hiz = g.nz - 1;
-    } else {
-        g.lo = 0;
-        g.hix = g.nx;
-        g.hiy = g.ny;
-        g.hiz = g.nz;
-    }
+    const bool pxy = p.bc == LAT_BC_PERIODIC, pz = bc_z_kind(p) == LAT_BC_PERIODIC;
+    g.lox = g.loy = pxy ? 0 : 1;
+    g.hix = pxy ? g.nx : g.nx - 1;
+    g.hiy = pxy ? g.ny : g.ny - 1;
+    g.loz = pz ? 0 : 1;
+    g.hiz = pz ? g.nz : g.nz - 1;
     return g;
 }
 
@@ -189,10 +196,18 @@ static int validate(const lat_params* p)
     LAT_REQUIRE(p->precision == LAT_F64 || p->precision == LAT_F32 || p->precision == LAT_F64_FAST,
                 "unknown precision");
     LAT_REQUIRE(p->kernel_variant == 0 || p->kernel_variant == 1, "unknown kernel_variant");
-    LAT_REQUIRE(p->bc == LAT_BC_PERIODIC || p->bc == LAT_BC_FIXED, "unknown boundary condition");
-    const int64_t mn = p->bc == LAT_BC_FIXED ? 3 : 2;
-    LAT_REQUIRE(p->nx >= mn && p->ny >= mn && p->nz >= mn, "lattice sides too small for the boundary condition");
-    LAT_REQUIRE(p->nx <= 65535 + (p->bc == LAT_BC_FIXED ? 2 : 0), "nx above 65535 (grid z-dimension limit)");
+    LAT_REQUIRE(p->bc >= LAT_BC_PERIODIC && p->bc <= LAT_BC_ABSORBING, "unknown boundary condition");
+    LAT_REQUIRE(p->bc_z >= LAT_BCZ_AS_XY && p->bc_z <= LAT_BCZ_NEUMANN, "unknown bc_z");
+    const int kz = bc_z_kind(*p);
+    LAT_REQUIRE(kz != LAT_BC_ABSORBING, "absorbing boundaries are for x and y only (set bc_z)");
+    LAT_REQUIRE(p->model == LAT_MODEL_AH || (p->bc <= LAT_BC_FIXED && kz <= LAT_BC_FIXED),
+                "Neumann and absorbing boundaries are provided for the Abelian-Higgs model");
+    // the reference's z-Neumann pass runs over x planes i < nz (evolution.cpp:250): beyond nx it
+    // would leave the array
+    LAT_REQUIRE(kz != LAT_BC_NEUMANN || p->nz <= p->nx, "a Neumann z boundary needs nz <= nx");
+    const int64_t mxy = p->bc == LAT_BC_PERIODIC ? 2 : 3, mz = kz == LAT_BC_PERIODIC ? 2 : 3;
+    LAT_REQUIRE(p->nx >= mxy && p->ny >= mxy && p->nz >= mz, "lattice sides too small for the boundary condition");
+    LAT_REQUIRE(p->nx <= 65535 + (p->bc == LAT_BC_PERIODIC ? 0 : 2), "nx above 65535 (grid z-dimension limit)");
     LAT_REQUIRE(p->nx * p->ny * p->nz < ((int64_t)1 << 31) - 1, "nx*ny*nz must be below 2^31");
     LAT_REQUIRE(p->dx > 0 && p->dy > 0 && p->dz > 0 && p->dt > 0, "spacings and dt must be positive");
     LAT_REQUIRE(std::isfinite(p->tau0) && p->tau0 > 0, "tau0 must be positive");
@@ -291,7 +306,7 @@ int reconfigure_handle(lat_handle* h, const lat_params* p)
     int rc = validate(p);
     if (rc) return rc;
     LAT_REQUIRE(h, "reconfigure: null handle");
-    LAT_REQUIRE(p->model == h->p.model && p->precision == h->p.precision && p->bc == h->p.bc && p->nx == h->p.nx &&
+    LAT_REQUIRE(p->model == h->p.model && p->precision == h->p.precision && p->bc == h->p.bc && p->bc_z == h->p.bc_z && p->nx == h->p.nx &&
                     p->ny == h->p.ny && p->nz == h->p.nz && p->kernel_variant == h->p.kernel_variant,
                 "reconfigure: different shape");
     h->p = *p;
@@ -504,7 +519,7 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
 static int64_t evolved_sites(const lat_handle* h)
 {
     const Geom& g = h->geom;
-    return (int64_t)(g.hix - g.lo) * (g.hiy - g.lo) * (g.hiz - g.lo);
+    return (int64_t)(g.hix - g.lox) * (g.hiy - g.loy) * (g.hiz - g.loz);
 }
 
 static int ensure_diag(lat_handle* h, int64_t entries)
@@ -617,7 +632,9 @@ static DetectArgs detect_args(const lat_handle* h)
     a.ny = g.ny;
     a.nz = g.nz;
     a.syz = g.syz;
-    a.lo = g.lo;
+    a.lox = g.lox;
+    a.loy = g.loy;
+    a.loz = g.loz;
     a.hix = g.hix;
     a.hiy = g.hiy;
     a.hiz = g.hiz;
@@ -709,7 +726,7 @@ int lat_string_length(lat_handle* h, int32_t field, int32_t split, int32_t metho
     LAT_REQUIRE(field == LAT_FIELD_PHI1 || (field == LAT_FIELD_PHI2 && h->p.model == LAT_MODEL_MOORE),
                 "lat_string_length: bad field");
     LAT_REQUIRE(method >= LAT_CHAIN_AUTO && method <= LAT_CHAIN_EXHAUSTIVE, "lat_string_length: bad method");
-    const bool periodic = h->p.bc == LAT_BC_PERIODIC;
+    const bool periodic = h->p.bc == LAT_BC_PERIODIC && bc_z_kind(h->p) == LAT_BC_PERIODIC;
     LAT_REQUIRE(method != LAT_CHAIN_HASH || periodic, "lat_string_length: the hash needs a periodic lattice");
     LAT_CK(cudaSetDevice(h->device));
     *L0 = *L1 = 0.0;
@@ -745,9 +762,11 @@ int lat_winding(lat_handle* h, int32_t field, int8_t* out, int64_t* abs_sum)
     const void* im = h->slot(2 * field + 1, tNow);
     LAT_CK(cudaMemsetAsync(h->wind_sum, 0, sizeof(unsigned long long), h->stream));
     int8_t* dst = out ? h->wind : nullptr;
-    const int fixed = h->p.bc == LAT_BC_FIXED;
-    if (h->elem == 8) LAT_CKL(launch_winding_f64(a, fixed, (const double*)re, (const double*)im, dst, h->wind_sum, h->stream));
-    else LAT_CKL(launch_winding_f32(a, fixed, (const float*)re, (const float*)im, dst, h->wind_sum, h->stream));
+    const int open_axes = (h->p.bc != LAT_BC_PERIODIC ? 1 : 0) | (bc_z_kind(h->p) != LAT_BC_PERIODIC ? 2 : 0);
+    if (h->elem == 8)
+        LAT_CKL(launch_winding_f64(a, open_axes, (const double*)re, (const double*)im, dst, h->wind_sum, h->stream));
+    else
+        LAT_CKL(launch_winding_f32(a, open_axes, (const float*)re, (const float*)im, dst, h->wind_sum, h->stream));
     unsigned long long tot = 0;
     LAT_CK(cudaMemcpyAsync(&tot, h->wind_sum, sizeof(tot), cudaMemcpyDeviceToHost, h->stream));
     if (out) LAT_CK(cudaMemcpyAsync(out, h->wind, (size_t)3 * h->N, cudaMemcpyDeviceToHost, h->stream));

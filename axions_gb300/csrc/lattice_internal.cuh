@@ -17,7 +17,7 @@ namespace lat {
 struct Geom {
     int nx, ny, nz;       // lattice sides
     int syz;              // ny*nz
-    int lo;               // first evolved index per axis (0 periodic, 1 fixed)
+    int lox, loy, loz;    // first evolved index per axis (0 periodic, 1 otherwise)
     int hix, hiy, hiz;    // one past the last evolved index per axis
 };
 
@@ -28,8 +28,8 @@ constexpr int BLOCK = BZ * BY;
 
 inline dim3 site_grid(const Geom& g)
 {
-    return dim3((unsigned)((g.hiz - g.lo + BZ - 1) / BZ), (unsigned)((g.hiy - g.lo + BY - 1) / BY),
-                (unsigned)(g.hix - g.lo));
+    return dim3((unsigned)((g.hiz - g.loz + BZ - 1) / BZ), (unsigned)((g.hiy - g.loy + BY - 1) / BY),
+                (unsigned)(g.hix - g.lox));
 }
 
 // ---------------------------------------------------------------------------
@@ -77,6 +77,8 @@ inline StepCoefT<R> coef_as(const StepCoef& c)
 
 StepCoef make_coef(const lat_params& p, int64_t n);
 Geom make_geom(const lat_params& p);
+// LAT_BC_* of the z axis (bc_z, or the same as bc)
+int bc_z_kind(const lat_params& p);
 
 // Kernel argument block: base pointers of the two slots of every component.
 template <class T, int NC>
@@ -135,7 +137,7 @@ cudaError_t launch_f2d(const float* in, double* out, int64_t n, cudaStream_t);
 
 // detection
 struct DetectArgs {
-    int nx, ny, nz, syz, lo, hix, hiy, hiz;
+    int nx, ny, nz, syz, lox, loy, loz, hix, hiy, hiz;
     double dx, dy, dz;
     int x0, y0, z0;
 };
@@ -149,9 +151,9 @@ cudaError_t launch_detect_write_f64(const DetectArgs&, const double* re, const d
                                     int nblocks, double* xyz, long long cap, cudaStream_t);
 cudaError_t launch_detect_write_f32(const DetectArgs&, const float* re, const float* im, const long long* block_offsets,
                                     int nblocks, double* xyz, long long cap, cudaStream_t);
-cudaError_t launch_winding_f64(const DetectArgs&, int fixed, const double* re, const double* im, int8_t* out,
+cudaError_t launch_winding_f64(const DetectArgs&, int open_axes, const double* re, const double* im, int8_t* out,
                                unsigned long long* abs_sum, cudaStream_t);
-cudaError_t launch_winding_f32(const DetectArgs&, int fixed, const float* re, const float* im, int8_t* out,
+cudaError_t launch_winding_f32(const DetectArgs&, int open_axes, const float* re, const float* im, int8_t* out,
                                unsigned long long* abs_sum, cudaStream_t);
 
 // ---------------------------------------------------------------------------
@@ -164,7 +166,7 @@ struct ChainGeom {
     double lo[3];         // -x0*d: lower edge of crossing coordinates
     double w[3];          // hash cell width (>= the cutoff radius)
     int nb[3];            // hash cells per axis
-    int periodic;
+    int periodic[3];      // minimum image per axis (x, y from bc; z from bc_z)
     double cutoff;        // (dx*dx + dy*dy + dz*dz)^2, compared with squared distances
     double root_cutoff;   // sqrt(cutoff): the closing length the reference adds
     int nnb;              // distinct neighbour-cell offsets

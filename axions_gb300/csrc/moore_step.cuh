@@ -17,9 +17,9 @@ __global__ void __launch_bounds__(BLOCK) moore_step_kernel(const Geom g, const F
                                                            const DiagOut d)
 {
     using TR = Trig<T>;
-    const int k = g.lo + (int)(blockIdx.x * BZ + threadIdx.x);
-    const int j = g.lo + (int)(blockIdx.y * BY + threadIdx.y);
-    const int i = g.lo + (int)blockIdx.z;
+    const int k = g.loz + (int)(blockIdx.x * BZ + threadIdx.x);
+    const int j = g.loy + (int)(blockIdx.y * BY + threadIdx.y);
+    const int i = g.lox + (int)blockIdx.z;
     double e_site = 0.0, g_site = 0.0;
 
     if (k < g.hiz && j < g.hiy) {

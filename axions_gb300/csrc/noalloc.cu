@@ -78,11 +78,13 @@ extern "C" int lat_ah_step_f64_noalloc(const lat_params* p, double* fields, int6
         return LAT_ERR_INVALID;
     }
     if (p->abi_version != LAT_ABI_VERSION || p->model != LAT_MODEL_AH || p->precision != LAT_F64 ||
-        (p->bc != LAT_BC_PERIODIC && p->bc != LAT_BC_FIXED)) {
+        (p->bc != LAT_BC_PERIODIC && p->bc != LAT_BC_FIXED) ||
+        p->bc_z < LAT_BCZ_AS_XY || p->bc_z > LAT_BCZ_NEUMANN ||
+        (bc_z_kind(*p) != LAT_BC_PERIODIC && bc_z_kind(*p) != LAT_BC_FIXED)) {
         set_error("lat_ah_step_f64_noalloc: needs an Abelian-Higgs LAT_F64 parameter block");
         return LAT_ERR_INVALID;
     }
-    const int64_t mn = p->bc == LAT_BC_FIXED ? 3 : 2;
+    const int64_t mn = (p->bc == LAT_BC_FIXED || bc_z_kind(*p) == LAT_BC_FIXED) ? 3 : 2;
     if (p->nx < mn || p->ny < mn || p->nz < mn || !(p->dx > 0 && p->dy > 0 && p->dz > 0 && p->dt > 0)) {
         set_error("lat_ah_step_f64_noalloc: bad lattice sides or spacings");
         return LAT_ERR_INVALID;

@@ -39,9 +39,9 @@ int reconfigure_handle(lat_handle* h, const lat_params* p);
 namespace {
 
 using Clock = std::chrono::steady_clock;
-using ShapeKey = std::tuple<int, int, int, int64_t, int64_t, int64_t>;  // model, precision, bc, nx, ny, nz
+using ShapeKey = std::tuple<int, int, int, int64_t, int64_t, int64_t>;  // model, precision, bc|bc_z, nx, ny, nz
 
-ShapeKey shape_of(const lat_params& p) { return ShapeKey(p.model, p.precision, p.bc, p.nx, p.ny, p.nz); }
+ShapeKey shape_of(const lat_params& p) { return ShapeKey(p.model, p.precision, p.bc + 16 * p.bc_z, p.nx, p.ny, p.nz); }
 
 struct JobState {
     lat_job_spec spec;
@@ -126,7 +126,7 @@ void finish(lat_server* s, int64_t id, int status)
         if (status == 2) {
             // the per-shape chunk of the batch, so that the final diagnostics
             // depend on the job only (not on tuning done elsewhere in the process)
-            j.h->chunk = std::min(j.h->geom.hix - j.h->geom.lo, 128);
+            j.h->chunk = std::min(j.h->geom.hix - j.h->geom.lox, 128);
             lat_diag fd;
             if (lat_diagnostics(j.h, &fd) == LAT_OK) {
                 j.res.final_energy = fd.energy;

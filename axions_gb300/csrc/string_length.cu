@@ -138,9 +138,9 @@ __device__ __forceinline__ double axis_term(double a, double b, double L, double
 __device__ __forceinline__ double chain_d2(const ChainGeom& g, double ax, double ay, double az, double bx, double by,
                                            double bz)
 {
-    double d = axis_term(ax, bx, g.L[0], g.half[0], g.periodic);
-    d += axis_term(ay, by, g.L[1], g.half[1], g.periodic);
-    d += axis_term(az, bz, g.L[2], g.half[2], g.periodic);
+    double d = axis_term(ax, bx, g.L[0], g.half[0], g.periodic[0]);
+    d += axis_term(ay, by, g.L[1], g.half[1], g.periodic[1]);
+    d += axis_term(az, bz, g.L[2], g.half[2], g.periodic[2]);
     return d;
 }
 
@@ -846,7 +846,8 @@ ChainGeom make_chain_geom(const lat_params& p, int64_t M)
     const double c0 = p.dx * p.dx + p.dy * p.dy + p.dz * p.dz;
     g.cutoff = c0 * c0;  // pow(., 2) of ic_w_evolution.cpp:979
     g.root_cutoff = std::sqrt(g.cutoff);
-    g.periodic = p.bc == LAT_BC_PERIODIC;
+    g.periodic[0] = g.periodic[1] = p.bc == LAT_BC_PERIODIC;
+    g.periodic[2] = bc_z_kind(p) == LAT_BC_PERIODIC;
     long long nb[3];
     for (int a = 0; a < 3; ++a) {
         g.L[a] = (double)n[a] * d[a];
@@ -1017,7 +1018,7 @@ extern "C" int lat_string_length_points(const lat_params* p, const double* xyz, 
     *L0 = *L1 = 0.0;
     if (M == 0) return LAT_OK;
     const ChainGeom g = make_chain_geom(*p, M);
-    const bool hashable = g.periodic && chain_points_in_box(g, xyz, M);
+    const bool hashable = g.periodic[0] && g.periodic[1] && g.periodic[2] && chain_points_in_box(g, xyz, M);
     if (method == LAT_CHAIN_HASH && !hashable) {
         set_error("lat_string_length_points: the hash needs a periodic lattice and points inside the box");
         return LAT_ERR_INVALID;

@@ -131,9 +131,9 @@ __device__ __forceinline__ void tiled_tile(TiledSmem<T, NS>& sm, const Geom& g, 
     constexpr int TH0 = 2 * NS;  // first theta component
 
     const int tz = threadIdx.x, ty = threadIdx.y;
-    const int k0 = g.lo + bx * TT_Z;
-    const int j0 = g.lo + by * TT_Y;
-    const int ib = g.lo + bz * chunk;
+    const int k0 = g.loz + bx * TT_Z;
+    const int j0 = g.loy + by * TT_Y;
+    const int ib = g.lox + bz * chunk;
     const int ie = min(ib + chunk, g.hix);
     const int k = k0 + tz, j = j0 + ty;
     const bool active = (k < g.hiz) && (j < g.hiy);
@@ -429,8 +429,8 @@ tiled_step_kernel(const Geom g, const Fields<T, 2 * NS + 3> f, const StepCoefT<T
 
 inline dim3 tiled_grid(const Geom& g, int chunk)
 {
-    return dim3((unsigned)((g.hiz - g.lo + TT_Z - 1) / TT_Z), (unsigned)((g.hiy - g.lo + TT_Y - 1) / TT_Y),
-                (unsigned)((g.hix - g.lo + chunk - 1) / chunk));
+    return dim3((unsigned)((g.hiz - g.loz + TT_Z - 1) / TT_Z), (unsigned)((g.hiy - g.loy + TT_Y - 1) / TT_Y),
+                (unsigned)((g.hix - g.lox + chunk - 1) / chunk));
 }
 
 inline int small_int_power(double q)

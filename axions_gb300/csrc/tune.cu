@@ -51,11 +51,11 @@ int default_chunk(const lat_params& p)
         if (it != g_tune.end()) return it->second.chunk;
     }
     const Geom g = make_geom(p);
-    const int64_t cols = (int64_t)((g.hiz - g.lo + 31) / 32) * ((g.hiy - g.lo + 7) / 8);
+    const int64_t cols = (int64_t)((g.hiz - g.loz + 31) / 32) * ((g.hiy - g.loy + 7) / 8);
     const int64_t want = 4 * 152;
     int best = kCandidates[0];
     for (int c : kCandidates)
-        if (cols * ((g.hix - g.lo + c - 1) / c) >= want) best = c;
+        if (cols * ((g.hix - g.lox + c - 1) / c) >= want) best = c;
     return best;
 }
 
@@ -117,7 +117,7 @@ int lat_autotune(lat_handle* h, int32_t trial_steps, lat_tuning* out)
     double best_ms = 1e300;
     int best = h->chunk, tried = 0;
     for (int c : kCandidates) {
-        if (c > 2 * (g.hix - g.lo) && c != kCandidates[0]) continue;  // beyond the lattice: same as a shorter one
+        if (c > 2 * (g.hix - g.lox) && c != kCandidates[0]) continue;  // beyond the lattice: same as a shorter one
         t->chunk = c;
         if ((rc = lat_step(t, 1))) break;  // warm-up
         cudaEventRecord(e0, t->stream);
