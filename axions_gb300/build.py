@@ -37,6 +37,7 @@ UNITS = {
     "detect.cu": ["-fmad=false"],
     "string_length.cu": ["-fmad=false"],
     "snapshot.cu": ["-fmad=false"],
+    "boundary.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
     "ah_f64_fast.cu": [],
     "ah_f32.cu": [],

@@ -98,6 +98,7 @@ int lat_random_phase_ic_device(lat_handle* h, uint64_t seed, int32_t independent
         return LAT_ERR_CUDA;
     }
     h->n = 0;
+    h->bc_level = -1;  // new values: their Neumann layer is not set yet
     h->div_valid = false;
     const int tNow = 1, tPast = 0;  // level 0: now in slot 1, past in slot 0
     const int moore = h->p.model == LAT_MODEL_MOORE;

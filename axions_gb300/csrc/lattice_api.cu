@@ -311,6 +311,7 @@ int reconfigure_handle(lat_handle* h, const lat_params* p)
                 "reconfigure: different shape");
     h->p = *p;
     h->n = 0;
+    h->bc_level = -1;  // new values: their Neumann layer is not set yet
     h->div_valid = false;
     auto pow2 = [](double v) {
         int e;
@@ -341,6 +342,7 @@ int lat_destroy(lat_handle* h)
     cudaFree(h->wind);
     cudaFree(h->wind_sum);
     chain_buffers_release(h->chain, nullptr);
+    cudaFree(h->btt);
     if (h->snap_pending) cudaEventSynchronize(h->snap_copied);
     cudaFree(h->snap_dev);
     if (h->snap_staged) cudaEventDestroy(h->snap_staged);
@@ -412,6 +414,7 @@ int lat_set_state(lat_handle* h, const double* now, const double* past, int64_t 
     int rc;
     if (h->elem == 4 && (rc = ensure_staging(h))) return rc;
     h->n = time_step;
+    h->bc_level = -1;  // new values: their Neumann layer is not set yet
     const int tNow = (int)((time_step + 1) % 2), tPast = (int)(time_step % 2);
     if ((rc = upload_level(h, now, tNow))) return rc;
     if ((rc = upload_level(h, past, tPast))) return rc;
@@ -436,10 +439,49 @@ int lat_get_state(lat_handle* h, double* now, double* past)
 // One step of the loop body.  diag: compute energy/Gauss of the now level
 // into diag_dst[0..1] (device); store_div: keep div(theta) of the now level
 // for the next step's Gauss term.
+// Neumann layers of the current level (evolution.cpp:194-265), set once per
+// level before anything reads it as the reference's loop body does after its
+// boundary step: the step, diagnostics, detection, winding, string length.
+// get_state and snapshots see the level as stored (the reference's dumps of a
+// new level are written before its boundary step).
+static int ensure_boundaries(lat_handle* h)
+{
+    const int kxy = h->p.bc, kz = bc_z_kind(h->p);
+    if ((kxy != LAT_BC_NEUMANN && kz != LAT_BC_NEUMANN) || h->bc_level == h->n) return LAT_OK;
+    const int tNow = (int)((h->n + 1) % 2);
+    void* now[5];
+    for (int c = 0; c < 5; ++c) now[c] = h->slot(c, tNow);
+    int nl = 0;
+    LAT_CK(launch_neumann(h->geom, kxy, kz, (int)h->elem, now, h->stream, &nl));
+    h->launches += nl;
+    h->bc_level = h->n;
+    return LAT_OK;
+}
+
 static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, bool write = true)
 {
     const lat_params& p = h->p;
     const int tNow = (int)((h->n + 1) % 2), tPast = (int)(h->n % 2);
+    int rc = ensure_boundaries(h);
+    if (rc) return rc;
+    const bool absorb = write && p.bc == LAT_BC_ABSORBING;
+    void* nowv[5];
+    void* pastv[5];
+    if (absorb) {
+        for (int c = 0; c < 5; ++c) {
+            nowv[c] = h->slot(c, tNow);
+            pastv[c] = h->slot(c, tPast);
+        }
+        const size_t need = absorb_tt_bytes(h->geom, (int)h->elem);
+        if (need > h->btt_bytes) {
+            dev_free(h, &h->btt, h->btt_bytes);
+            h->btt_bytes = 0;
+            if ((rc = dev_alloc(h, &h->btt, need))) return rc;
+            h->btt_bytes = need;
+        }
+        // before the interior step overwrites the past level these read
+        LAT_CKL(launch_absorb_tt(h->geom, (int)h->elem, nowv, pastv, h->btt, p.dx, p.dy, p.dz, p.dt, h->stream));
+    }
     const StepCoef cf = make_coef(p, h->n);
     DiagOut d;
     d.partials = h->partials;
@@ -501,6 +543,7 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
             else LAT_CKL(launch_moore_step_f32(h->geom, f, cf, d, diag, h->stream));
         }
     }
+    if (absorb) LAT_CKL(launch_absorb_update(h->geom, (int)h->elem, nowv, pastv, h->btt, p.dt * p.dt, h->stream));
     if (diag) {
         // partials written by the step: one per CTA of the kernel that ran
         const bool tiled = h->elem == 4 && p.kernel_variant == 0;
@@ -650,6 +693,8 @@ static DetectArgs detect_args(const lat_handle* h)
 // count the crossings of `field` on the current level (block totals scanned in place)
 static int detect_count(lat_handle* h, int32_t field, int64_t* total_out)
 {
+    int rc0 = ensure_boundaries(h);
+    if (rc0) return rc0;
     const DetectArgs a = detect_args(h);
     const int tNow = (int)((h->n + 1) % 2);
     const int nb = (int)((h->N + detect_block_sites() - 1) / detect_block_sites());
@@ -756,6 +801,8 @@ int lat_winding(lat_handle* h, int32_t field, int8_t* out, int64_t* abs_sum)
         int rc = dev_alloc(h, (void**)&h->wind, (size_t)3 * h->N);
         if (rc) return rc;
     }
+    int rcb = ensure_boundaries(h);
+    if (rcb) return rcb;
     const DetectArgs a = detect_args(h);
     const int tNow = (int)((h->n + 1) % 2);
     const void* re = h->slot(2 * field, tNow);

@@ -38,6 +38,9 @@ struct lat_handle {
     int8_t* wind = nullptr;
     unsigned long long* wind_sum = nullptr;
     lat::ChainBuffers chain;   // string-length buffers
+    int64_t bc_level = -1;     // the level whose Neumann layer has been set
+    void* btt = nullptr;       // absorbing layer's second time derivatives
+    size_t btt_bytes = 0;
     // asynchronous snapshots (snapshot.cu)
     double* snap_dev = nullptr;          // staged copy of the level, [cols][N] doubles
     size_t snap_cap = 0;                 // bytes of snap_dev

@@ -128,6 +128,15 @@ cudaError_t launch_divergence_f64(const Geom&, const double* thx, const double* 
 cudaError_t launch_divergence_f32(const Geom&, const float* thx, const float* thy, const float* thz,
                                   const StepCoef&, float* out, cudaStream_t);
 
+// Neumann and absorbing boundaries (boundary.cu); `now`/`past` are the five
+// component slots of a level, elem the bytes per value
+cudaError_t launch_neumann(const Geom&, int kxy, int kz, int elem, void* const* now, cudaStream_t, int* launches);
+size_t absorb_tt_bytes(const Geom&, int elem);
+cudaError_t launch_absorb_tt(const Geom&, int elem, void* const* now, void* const* past, void* tt, double dx,
+                             double dy, double dz, double dt, cudaStream_t);
+cudaError_t launch_absorb_update(const Geom&, int elem, void* const* now, void* const* past, const void* tt,
+                                 double dt2, cudaStream_t);
+
 // deterministic sum of per-block partials into out[0..1] (energy, |G|)
 cudaError_t launch_finalize(const double* partials, int nblocks, double* out, cudaStream_t);
 

@@ -346,15 +346,13 @@ struct Run {
         if (prog == Program::Evolution || prog == Program::MooreEvol || prog == Program::IcwEvolution) {
             const std::string xy = prm.str("xyBC");
             const std::string z = prog == Program::MooreEvol ? std::string("fixed") : prm.str("zBC");
-            auto kind = [](const std::string& b) {
-                if (b == "periodic") return 0;
-                if (b == "neumann" || b == "absorbing") return -1;
-                return 1;  // any other string selects fixed boundaries (evolution.cpp:52-53)
-            };
-            const int kxy = kind(xy), kz = kind(z);
-            if (kxy < 0 || kz < 0) fail("neumann and absorbing boundaries are not provided by this library");
-            if (kxy != kz) fail("mixed periodic/fixed boundaries are not provided by this library");
-            p.bc = kxy == 0 ? LAT_BC_PERIODIC : LAT_BC_FIXED;
+            // evolution.cpp:44-45: "periodic", "neumann", "absorbing" (x and y), any
+            // other string fixed; the library rejects what a model does not provide
+            p.bc = xy == "periodic" ? LAT_BC_PERIODIC
+                 : xy == "neumann" ? LAT_BC_NEUMANN
+                 : xy == "absorbing" ? LAT_BC_ABSORBING
+                                     : LAT_BC_FIXED;
+            p.bc_z = z == "periodic" ? LAT_BCZ_PERIODIC : z == "neumann" ? LAT_BCZ_NEUMANN : LAT_BCZ_FIXED;
         }
         ncomp = is_moore(prog) ? 7 : 5;
         N = p.nx * p.ny * p.nz;
@@ -392,6 +390,15 @@ struct Run {
         std::ofstream o = open_out(path);
         for (int64_t q = 0; q < n; ++q) o << xyz[3 * q] << " " << xyz[3 * q + 1] << " " << xyz[3 * q + 2] << std::endl;
         return n;
+    }
+
+    // evolution.cpp:1404-1408: x/y and z normalised by their own boundary kind
+    double evolution_deviation(double D) const
+    {
+        const bool pxy = p.bc == LAT_BC_PERIODIC;
+        const bool pz = p.bc_z == LAT_BCZ_PERIODIC || (p.bc_z == LAT_BCZ_AS_XY && pxy);
+        D = pxy ? D / (double)(p.nx * p.ny) : D / (double)((p.nx - 2) * (p.ny - 2));
+        return pz ? D / (double)p.nz : D / (double)(p.nz - 2);
     }
 
     void write_final_field(const std::string& path)
@@ -633,10 +640,8 @@ int run_openmp(Run& r)
             double dev = diags[d].gauss_abs_sum;
             if (moore) {
                 dev = dev / interior / interior;
-            } else if (r.p.bc == LAT_BC_PERIODIC) {
-                dev = dev / (double)(r.p.nx * r.p.ny) / (double)r.p.nz;
             } else {
-                dev = dev / (double)((r.p.nx - 2) * (r.p.ny - 2)) / (double)(r.p.nz - 2);
+                dev = r.evolution_deviation(dev);
             }
             valsPerLoop << diags[d].energy << " " << dev;
             if (stringPos) valsPerLoop << " " << pos;
@@ -697,7 +702,6 @@ int run_icw(Run& r)
     check(lat_set_state(r.h, now.data(), now.data(), 0), "lat_set_state");
     AsyncFrames frames(r.h, 1, r.N, r.digits);
     std::ofstream valsPerLoop = r.open_out(r.data("valsPerLoop_test.txt"));  // input = "test" (:67)
-    const bool periodic = r.p.bc == LAT_BC_PERIODIC;
     long long counter = 0, gifFrame = 0;
     for (long long n = 0; n < nt; ++n) {
         progress(n, counter, countRate);
@@ -707,9 +711,7 @@ int run_icw(Run& r)
                           "lat_string_length");
         lat_diag d;
         check(lat_step_diag(r.h, &d), "lat_step_diag");
-        double dev = d.gauss_abs_sum;  // ic_w_evolution.cpp:1141-1145
-        if (periodic) dev = dev / (double)(r.p.nx * r.p.ny) / (double)r.p.nz;
-        else dev = dev / (double)((r.p.nx - 2) * (r.p.ny - 2)) / (double)(r.p.nz - 2);
+        const double dev = r.evolution_deviation(d.gauss_abs_sum);  // ic_w_evolution.cpp:1141-1145
         valsPerLoop << d.energy << " " << dev;
         if (stringPos) valsPerLoop << " " << pos;
         if (detect) {
