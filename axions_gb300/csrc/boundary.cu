@@ -86,6 +86,52 @@ __global__ void neumann_z_kernel(const BGeom g, const Lv<T> L, int ni)
     neumann_pair(L, 2, at(g, i, j, 0), at(g, i, j, 1), at(g, i, j, g.nz - 1), at(g, i, j, g.nz - 2));
 }
 
+// Moore (mooreEvol.cpp:114-160): phi_a transported along q_a * theta;
+// components phi1 (0, 1), phi2 (2, 3), theta (4, 5, 6)
+template <class T>
+struct Lv7 {
+    T* v[7];
+};
+
+template <class T>
+__device__ __forceinline__ void neumann_pair_moore(const Lv7<T>& L, T q1, T q2, int mu, int b0, int i0, int b1, int i1)
+{
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        L.v[4 + m][b0] = L.v[4 + m][i0];
+        L.v[4 + m][b1] = L.v[4 + m][i1];
+    }
+    const T t0 = L.v[4 + mu][b0], t1 = L.v[4 + mu][i1];
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        const T q = a == 0 ? q1 : q2;
+        const T c0 = cos(q * t0), s0 = sin(q * t0), c1 = cos(q * t1), s1 = sin(q * t1);
+        const T p0 = L.v[2 * a][i0], r0 = L.v[2 * a + 1][i0], p1 = L.v[2 * a][i1], r1 = L.v[2 * a + 1][i1];
+        L.v[2 * a][b0] = c0 * p0 + (T)1 * s0 * r0;
+        L.v[2 * a][b1] = c1 * p1 - (T)1 * s1 * r1;
+        L.v[2 * a + 1][b0] = c0 * r0 + (T)-1 * s0 * p0;
+        L.v[2 * a + 1][b1] = c1 * r1 - (T)-1 * s1 * p1;
+    }
+}
+
+template <class T>
+__global__ void neumann_y_moore_kernel(const BGeom g, const Lv7<T> L, T q1, T q2)
+{
+    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int k = g.loz + (int)blockIdx.y;
+    if (i >= g.nx - 1 || k >= g.hiz) return;
+    neumann_pair_moore(L, q1, q2, 1, at(g, i, 0, k), at(g, i, 1, k), at(g, i, g.ny - 1, k), at(g, i, g.ny - 2, k));
+}
+
+template <class T>
+__global__ void neumann_x_moore_kernel(const BGeom g, const Lv7<T> L, T q1, T q2)
+{
+    const int j = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int k = g.loz + (int)blockIdx.y;
+    if (j >= g.ny || k >= g.hiz) return;
+    neumann_pair_moore(L, q1, q2, 0, at(g, 0, j, k), at(g, 1, j, k), at(g, g.nx - 1, j, k), at(g, g.nx - 2, j, k));
+}
+
 // ---------------------------------------------------------------------------
 // absorbing x/y layer (evolution.cpp:446-691)
 // ---------------------------------------------------------------------------
@@ -279,6 +325,22 @@ Lv<T> level(void* const* slots)
 constexpr int BT = 128;
 
 template <class T>
+cudaError_t neumann_moore_t(const Geom& g, int kxy, double q1, double q2, void* const* now, cudaStream_t st,
+                            int* launches)
+{
+    const BGeom b = bgeom(g);
+    Lv7<T> L;
+    for (int c = 0; c < 7; ++c) L.v[c] = (T*)now[c];
+    const unsigned zs = (unsigned)(g.hiz - g.loz);
+    if (kxy == LAT_BC_NEUMANN && zs > 0) {
+        neumann_y_moore_kernel<T><<<dim3((unsigned)((g.nx - 2 + BT - 1) / BT), zs), BT, 0, st>>>(b, L, (T)q1, (T)q2);
+        neumann_x_moore_kernel<T><<<dim3((unsigned)((g.ny + BT - 1) / BT), zs), BT, 0, st>>>(b, L, (T)q1, (T)q2);
+        *launches += 2;
+    }
+    return cudaGetLastError();
+}
+
+template <class T>
 cudaError_t neumann_t(const Geom& g, int kxy, int kz, void* const* now, cudaStream_t st, int* launches)
 {
     const BGeom b = bgeom(g);
@@ -304,8 +366,12 @@ size_t absorb_tt_bytes(const Geom& g, int elem)
     return (size_t)elem * 5 * (size_t)(2 * (g.nx + g.ny) - 4) * (size_t)(g.hiz - g.loz);
 }
 
-cudaError_t launch_neumann(const Geom& g, int kxy, int kz, int elem, void* const* now, cudaStream_t st, int* launches)
+cudaError_t launch_neumann(const Geom& g, int model, double q1, double q2, int kxy, int kz, int elem, void* const* now,
+                           cudaStream_t st, int* launches)
 {
+    if (model == LAT_MODEL_MOORE)
+        return elem == 8 ? neumann_moore_t<double>(g, kxy, q1, q2, now, st, launches)
+                         : neumann_moore_t<float>(g, kxy, q1, q2, now, st, launches);
     return elem == 8 ? neumann_t<double>(g, kxy, kz, now, st, launches)
                      : neumann_t<float>(g, kxy, kz, now, st, launches);
 }

@@ -200,8 +200,9 @@ static int validate(const lat_params* p)
     LAT_REQUIRE(p->bc_z >= LAT_BCZ_AS_XY && p->bc_z <= LAT_BCZ_NEUMANN, "unknown bc_z");
     const int kz = bc_z_kind(*p);
     LAT_REQUIRE(kz != LAT_BC_ABSORBING, "absorbing boundaries are for x and y only (set bc_z)");
-    LAT_REQUIRE(p->model == LAT_MODEL_AH || (p->bc <= LAT_BC_FIXED && kz <= LAT_BC_FIXED),
-                "Neumann and absorbing boundaries are provided for the Abelian-Higgs model");
+    // mooreEvol.cpp:114-160 has Neumann x/y walls; its absorbing code is not written (:42, :402)
+    LAT_REQUIRE(p->model == LAT_MODEL_AH || ((p->bc <= LAT_BC_NEUMANN) && kz <= LAT_BC_FIXED),
+                "the Moore model provides periodic, fixed or Neumann x/y and periodic or fixed z boundaries");
     // the reference's z-Neumann pass runs over x planes i < nz (evolution.cpp:250): beyond nx it
     // would leave the array
     LAT_REQUIRE(kz != LAT_BC_NEUMANN || p->nz <= p->nx, "a Neumann z boundary needs nz <= nx");
@@ -449,10 +450,10 @@ static int ensure_boundaries(lat_handle* h)
     const int kxy = h->p.bc, kz = bc_z_kind(h->p);
     if ((kxy != LAT_BC_NEUMANN && kz != LAT_BC_NEUMANN) || h->bc_level == h->n) return LAT_OK;
     const int tNow = (int)((h->n + 1) % 2);
-    void* now[5];
-    for (int c = 0; c < 5; ++c) now[c] = h->slot(c, tNow);
+    void* now[7];
+    for (int c = 0; c < h->ncomp; ++c) now[c] = h->slot(c, tNow);
     int nl = 0;
-    LAT_CK(launch_neumann(h->geom, kxy, kz, (int)h->elem, now, h->stream, &nl));
+    LAT_CK(launch_neumann(h->geom, h->p.model, h->p.q1, h->p.q2, kxy, kz, (int)h->elem, now, h->stream, &nl));
     h->launches += nl;
     h->bc_level = h->n;
     return LAT_OK;

@@ -130,7 +130,8 @@ cudaError_t launch_divergence_f32(const Geom&, const float* thx, const float* th
 
 // Neumann and absorbing boundaries (boundary.cu); `now`/`past` are the five
 // component slots of a level, elem the bytes per value
-cudaError_t launch_neumann(const Geom&, int kxy, int kz, int elem, void* const* now, cudaStream_t, int* launches);
+cudaError_t launch_neumann(const Geom&, int model, double q1, double q2, int kxy, int kz, int elem,
+                           void* const* now, cudaStream_t, int* launches);
 size_t absorb_tt_bytes(const Geom&, int elem);
 cudaError_t launch_absorb_tt(const Geom&, int elem, void* const* now, void* const* past, void* tt, double dx,
                              double dy, double dz, double dt, cudaStream_t);

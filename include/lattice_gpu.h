@@ -70,7 +70,8 @@ extern "C" {
                                 the current level is set from the next layer in, phi
                                 transported along the link (evolution.cpp:194-265; the z
                                 pass covers x planes i < nz as the reference's does).
-                                Abelian-Higgs only                                           */
+                                Moore (mooreEvol.cpp:114-160): x and y only, phi_a along
+                                q_a*theta                                                    */
 #define LAT_BC_ABSORBING 3   /* x and y only: the outer layer evolves with the one-sided
                                 first-order absorbing updates of evolution.cpp:446-691 (and
                                 the whole layer is updated, :1375-1402). Abelian-Higgs only  */

@@ -195,6 +195,27 @@ static void neumann_pair(double* st, int64_t N, int tNow, int mu, int64_t b0, in
     }
 }
 
+/* Moore: phi_a transported along q_a * theta (mooreEvol.cpp:114-160); components
+ * phi1 (0, 1), phi2 (2, 3), theta (4, 5, 6) */
+static void neumann_pair_moore(const lat_params* p, double* st, int64_t N, int tNow, int mu, int64_t b0, int64_t i0,
+                               int64_t b1, int64_t i1)
+{
+    const int c[2] = {1, -1};
+    for (int m = 0; m < 3; ++m) {
+        ST(4 + m, tNow, b0) = ST(4 + m, tNow, i0);
+        ST(4 + m, tNow, b1) = ST(4 + m, tNow, i1);
+    }
+    for (int comp = 0; comp < 2; ++comp) {
+        const double cc = (double)c[comp];
+        for (int a = 0; a < 2; ++a) {
+            const double q = a == 0 ? p->q1 : p->q2;
+            const int f = 2 * a + comp, o = 2 * a + comp + c[comp];
+            ST(f, tNow, b0) = cos(q * ST(4 + mu, tNow, b0)) * ST(f, tNow, i0) + cc * sin(q * ST(4 + mu, tNow, b0)) * ST(o, tNow, i0);
+            ST(f, tNow, b1) = cos(q * ST(4 + mu, tNow, i1)) * ST(f, tNow, i1) - cc * sin(q * ST(4 + mu, tNow, i1)) * ST(o, tNow, i1);
+        }
+    }
+}
+
 int orc_apply_boundaries(const lat_params* p, double* st, int64_t n)
 {
     if (!p || !st) return LAT_ERR_INVALID;
@@ -202,6 +223,19 @@ int orc_apply_boundaries(const lat_params* p, double* st, int64_t n)
     const int64_t N = G.N;
     const int tNow = (int)((n + 1) % 2);
     const int64_t nx = G.nx, ny = G.ny, nz = G.nz;
+    if (p->model == LAT_MODEL_MOORE) {
+        if (G.kxy == LAT_BC_NEUMANN) {
+            for (int64_t i = 1; i < nx - 1; ++i)
+                for (int64_t k = G.loz; k < G.hiz; ++k)
+                    neumann_pair_moore(p, st, N, tNow, 1, site(&G, i, 0, k), site(&G, i, 1, k), site(&G, i, ny - 1, k),
+                                       site(&G, i, ny - 2, k));
+            for (int64_t j = 0; j < ny; ++j)
+                for (int64_t k = G.loz; k < G.hiz; ++k)
+                    neumann_pair_moore(p, st, N, tNow, 0, site(&G, 0, j, k), site(&G, 1, j, k), site(&G, nx - 1, j, k),
+                                       site(&G, nx - 2, j, k));
+        }
+        return 0;
+    }
     if (G.kxy == LAT_BC_NEUMANN) {
         for (int64_t i = 1; i < nx - 1; ++i)
             for (int64_t k = G.loz; k < G.hiz; ++k)

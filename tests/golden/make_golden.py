@@ -185,13 +185,13 @@ def gen_evolution(name, nx, ny, nz, nt, lam, g, alpha, bc, seed, saveFreq=4, dt=
 # --------------------------------------------------------------------------
 # mooreEvol.cpp: fixed boundaries, stationary IC from file, q-weighted current
 # --------------------------------------------------------------------------
-def gen_moore_evol(name, nx, ny, nz, nt, lam1, lam2, lam12, q1, q2, seed, dt=0.1, d=0.5):
+def gen_moore_evol(name, nx, ny, nz, nt, lam1, lam2, lam12, q1, q2, seed, dt=0.1, d=0.5, xyBC="fixed"):
     rng = np.random.default_rng(seed)
     N = nx * ny * nz
     now, _ = _two_level_ic(rng, N, 4, 0.4)
     consts = {"nx": nx, "ny": ny, "nz": nz, "nt": nt, "dx": d, "dy": d, "dz": d, "dt": dt,
               "eta1": 1.0, "eta2": 1.0, "lambda1": lam1, "lambda2": lam2, "lambda12": lam12,
-              "q1": q1, "q2": q2, "makeGif": False, "saveFreq": 10, "xyBC": "fixed"}
+              "q1": q1, "q2": q2, "makeGif": False, "saveFreq": 10, "xyBC": xyBC}
     build_ref.build("mooreEvol", name, consts)
     lines = [" ".join(_fmt(now[c, s]) for c in range(7)) for s in range(N)]
     work = build_ref.run(name, ic_lines=lines, ic_name="moore_ic.txt")
@@ -200,8 +200,8 @@ def gen_moore_evol(name, nx, ny, nz, nt, lam1, lam2, lam12, q1, q2, seed, dt=0.1
     g = float(np.sqrt(0.5 * lam1 * 1.0 ** 2 / (q1 * q1 + q2 * q2)))
     p = make_params(MODEL_MOORE, nx=nx, ny=ny, nz=nz, d=d, dt=dt, lam=lam1, lambda2=lam2, lambda12=lam12,
                     eta=1.0, eta2=1.0, q1=float(q1), q2=float(q2), g=g, damped_nt=0, dampFac=0.0,
-                    alpha=0.0, scaling=1.0, tau0=1.0, energy_form=ENERGY_EVOLUTION, bc=BC_FIXED,
-                    moore_current=MOORE_CURRENT_CHARGE)
+                    alpha=0.0, scaling=1.0, tau0=1.0, energy_form=ENERGY_EVOLUTION,
+                    bc=2 if xyBC == "neumann" else BC_FIXED, bc_z=2, moore_current=MOORE_CURRENT_CHARGE)
     ic = np.stack([now, now], axis=1)
     np.savez_compressed(OUT / f"{name}.npz", program="mooreEvol", params=_params_json(p), nt=nt, ic=ic,
                         final_newest=final_newest, energy=vals[:, 0], deviation=vals[:, 1])
@@ -271,6 +271,7 @@ def main():
     gen_icw_length("ref_icw_len_nosplit", 11, 13, 9, 12, BC_PERIODIC, seed=6, d=0.5, split=False)
     gen_initial_conditions("ref_initial_conditions", 7, 6, 5, seed=42, mean=0.0, stdev=0.5, g=0.5)
     # boundary kinds of evolution.cpp:166-265,446-691,1375-1408 (nz <= nx for a Neumann z, see orc_apply_boundaries)
+    gen_moore_evol("ref_moore_evol_neumann", 10, 9, 8, 10, 2.0, 2.0, 0.5, 2, 1, seed=26, xyBC="neumann")
     gen_evolution("ref_evol_bc_neumann", 10, 9, 8, 10, lam=2.0, g=0.7, alpha=3.0, bc=BC_FIXED, seed=21, saveFreq=3,
                   xyBC="neumann", zBC="neumann")
     gen_evolution("ref_evol_bc_absorbing", 11, 10, 8, 12, lam=2.0, g=0.7, alpha=0.0, bc=BC_FIXED, seed=22, saveFreq=4,

@@ -87,6 +87,23 @@ def test_fp32_boundaries_track_fp64(lattice_mod, oracle_mod, name):
     lat.close()
 
 
+def test_moore_neumann_walls_against_reference(lattice_mod):
+    """mooreEvol.cpp with xyBC = neumann: phi1, phi2 transported along q1*theta,
+    q2*theta (mooreEvol.cpp:114-160)."""
+    z = load_golden("ref_moore_evol_neumann")
+    p = params_from_json(z["params"])
+    lat = lattice_mod.Lattice(p)
+    lat.set_slots(z["ic"], 0)
+    nt = int(z["nt"])
+    out = lat.advance(nt, diag_every=1)
+    now, _ = lat.get_state()
+    assert_components_close(now, z["final_newest"], TOL)
+    np.testing.assert_allclose([o[1] for o in out], z["energy"], rtol=TOL, atol=0)
+    c = (p.nx - 2) * (p.ny - 2) * (p.nz - 2)              # mooreEvol.cpp:383,697
+    np.testing.assert_allclose(np.array([o[2] for o in out]) / c / c, z["deviation"], rtol=TOL, atol=0)
+    lat.close()
+
+
 def test_neumann_layer_is_set_lazily(lattice_mod, oracle_mod):
     """get_state shows the level as stored; detection (like a step) first sets
     the level's Neumann layer, once."""
@@ -111,7 +128,7 @@ def test_neumann_layer_is_set_lazily(lattice_mod, oracle_mod):
 def test_boundary_parameters_are_checked(lattice_mod):
     from axions_gb300.lattice import LatticeError
     from axions_gb300.params import (BC_ABSORBING, BC_NEUMANN, BCZ_NEUMANN, MODEL_MOORE, make_params)
-    bad = [make_params(MODEL_MOORE, n=8, bc=BC_NEUMANN),                # Moore: not provided
+    bad = [make_params(MODEL_MOORE, n=8, bc=BC_NEUMANN),                # Moore: no Neumann z
            make_params(0, n=8, bc=BC_ABSORBING),                         # absorbing z (bc_z same as bc)
            make_params(0, nx=6, ny=8, nz=8, bc=BC_ABSORBING, bc_z=BCZ_NEUMANN),  # z-Neumann needs nz <= nx
            make_params(0, n=8, bc=7)]

@@ -13,7 +13,7 @@ from conftest import load_golden, params_from_json
 
 MPI_CASES = ["ref_mpi_ah_c1", "ref_mpi_ah_prs", "ref_mpi_ah_global", "ref_moore_mpi"]
 OMP_CASES = ["ref_evol_ah_periodic", "ref_evol_ah_fixed", "ref_moore_evol"]
-BC_CASES = ["ref_evol_bc_neumann", "ref_evol_bc_absorbing", "ref_evol_bc_absorbing_neumann",
+BC_CASES = ["ref_moore_evol_neumann", "ref_evol_bc_neumann", "ref_evol_bc_absorbing", "ref_evol_bc_absorbing_neumann",
             "ref_evol_bc_fixed_zper", "ref_evol_bc_per_zfixed"]
 
 
