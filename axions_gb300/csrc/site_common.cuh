@@ -15,11 +15,24 @@ struct Trig<double> {
     static __device__ __forceinline__ double cos(double x) { return ::cos(x); }
     static __device__ __forceinline__ void sincos(double x, double* s, double* c) { ::sincos(x, s, c); }
 };
+// FP32: the argument is reduced to [-pi, pi] by Cody-Waite with 2*pi split in
+// two parts (Cody & Waite 1980; 6.28125 has 8 significant bits, so k*6.28125 is
+// exact for |k| < 2^16, i.e. |x| < 4e5), then the hardware approximations
+// __sinf/__cosf are used (documented absolute error 2^-21.41 on [-pi, pi]).
+// That error is below the rounding an FP32 phase or plaquette angle already
+// carries (|theta| up to ~10 gives ~1e-6), and it costs a few instructions
+// instead of a full-range software sine.  FP64 keeps the library functions.
 template <>
 struct Trig<float> {
-    static __device__ __forceinline__ float sin(float x) { return ::sinf(x); }
-    static __device__ __forceinline__ float cos(float x) { return ::cosf(x); }
-    static __device__ __forceinline__ void sincos(float x, float* s, float* c) { ::sincosf(x, s, c); }
+    static __device__ __forceinline__ float reduce(float x)
+    {
+        const float k = rintf(x * 0.159154943091895336f);  // x / (2 pi)
+        const float r = fmaf(-k, 6.28125f, x);
+        return fmaf(-k, 1.93530717958647692e-3f, r);      // 2 pi - 6.28125
+    }
+    static __device__ __forceinline__ float sin(float x) { return __sinf(reduce(x)); }
+    static __device__ __forceinline__ float cos(float x) { return __cosf(reduce(x)); }
+    static __device__ __forceinline__ void sincos(float x, float* s, float* c) { __sincosf(reduce(x), s, c); }
 };
 
 // a / b.  FP64 divides (the reference's rounding); FP32 multiplies by the

@@ -416,7 +416,7 @@ __device__ __forceinline__ void tiled_tile(TiledSmem<T, NS>& sm, const Geom& g, 
 }
 
 template <class T, int NS, bool DIAG>
-__global__ void __launch_bounds__(TT_THREADS, 2)
+__global__ void __launch_bounds__(TT_THREADS, NS == 1 ? 4 : 2)
 tiled_step_kernel(const Geom g, const Fields<T, 2 * NS + 3> f, const StepCoefT<T> c, const Charges<T> ch,
                   const DiagOut d, const int chunk)
 {
