@@ -18,6 +18,7 @@
 
 #include "ic_io.hpp"
 #include "lattice_gpu.h"
+#include "sor.hpp"
 
 namespace axh {
 
@@ -194,6 +195,20 @@ Params::Params(Program prog)
         v["ic_in"] = "";     // convert: the table to read (under Data/)
         v["cols"] = "5";     // convert: columns of the table
         v["levels"] = "1";   // convert: rows = levels * nx * ny * nz
+        break;
+    case Program::SingleSemiAnalytic:
+        // singleSemiAnalytic.cpp:19-33; ic_type 0 starts from eta*tanh(r/2),
+        // 1 from the current Data/SOR_Fields.txt
+        v["nx"] = "30001";
+        v["h"] = "0.01";
+        v["w"] = "1.5";
+        v["maxIter"] = "2000000";
+        v["tol"] = "1e-3";
+        v["ic_type"] = "0";
+        v["n"] = "1";
+        v["lambda"] = "1";
+        v["eta"] = "1";
+        v["g"] = "0";
         break;
     }
 }
@@ -783,15 +798,52 @@ int run_initial_conditions(Params& q)
     return 0;
 }
 
+int run_single_semi_analytic(Params& q)
+{
+    struct timeval start, end;
+    gettimeofday(&start, nullptr);
+    const std::string dir = q.str("out_dir");
+    ::mkdir((dir + "/Data").c_str(), 0755);
+    const std::string path = dir + "/Data/SOR_Fields.txt";
+    SorParams p;
+    p.nx = q.integer("nx");
+    p.h = q.num("h");
+    p.w = q.num("w");
+    p.max_iter = q.integer("maxIter");
+    p.tol = q.num("tol");
+    p.n = q.num("n");
+    p.lambda = q.num("lambda");
+    p.eta = q.num("eta");
+    p.g = q.num("g");
+    if (p.nx < 3) fail("nx must be at least 3");
+    std::vector<double> phi, A;
+    if (q.integer("ic_type") == 1) {
+        std::vector<double> tab;
+        read_table(path, 2, p.nx, tab);
+        phi.assign(tab.begin(), tab.begin() + p.nx);
+        A.assign(tab.begin() + p.nx, tab.end());
+    } else {
+        sor_initial_guess(p, phi, A);
+    }
+    const SorResult r = solve_sor(p, std::move(phi), std::move(A));
+    std::vector<double> tab(r.phi);
+    tab.insert(tab.end(), r.A.begin(), r.A.end());
+    write_table_text(path, 2, p.nx, tab.data(), (int)q.integer("digits"));
+    std::cout << "Number of iterations: " << r.iterations << std::endl;
+    gettimeofday(&end, nullptr);
+    std::cout << "Time taken: " << end.tv_sec - start.tv_sec << "s" << std::endl;
+    return 0;
+}
+
 }  // namespace
 
 int run_program(Program prog, int argc, char** argv)
 {
     try {
-        if (prog == Program::InitialConditions) {
+        if (prog == Program::InitialConditions || prog == Program::SingleSemiAnalytic) {
             Params q(prog);
             q.parse_args(argc, argv);
-            return run_initial_conditions(q);
+            return prog == Program::InitialConditions ? run_initial_conditions(q) : run_single_semi_analytic(q);
         }
         Run r(prog);
         r.prm.parse_args(argc, argv);

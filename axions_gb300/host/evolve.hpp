@@ -15,8 +15,11 @@ namespace axh {
 
 // IcwEvolution is ic_w_evolution.cpp: evolution with its initial conditions
 // made in-process (ic_func.cpp) and the total string length every step.
-// InitialConditions is initialConditions.cpp (writes Data/ic.txt; host only).
-enum class Program { MpiEvolution, Evolution, MooreMpiEvolution, MooreEvol, IcwEvolution, InitialConditions };
+// InitialConditions is initialConditions.cpp (writes Data/ic.txt).
+// SingleSemiAnalytic is singleSemiAnalytic.cpp (writes Data/SOR_Fields.txt,
+// the straight-string profile the string IC families interpolate; host only).
+enum class Program { MpiEvolution, Evolution, MooreMpiEvolution, MooreEvol, IcwEvolution, InitialConditions,
+                     SingleSemiAnalytic };
 
 // Parameter set: the reference defaults of `prog`, overridden by the file and
 // the command line.  Unknown keys are an error.

@@ -40,6 +40,7 @@ PROGRAMS = {
     # ic_w_evolution.cpp:79 builds its IC in-process with ic_func() (ic_func.cpp:18)
     "ic_w_evolution": (["ic_func.cpp", "array.cpp"], None),
     "initialConditions": (["array.cpp"], None),
+    "singleSemiAnalytic": (["array.cpp"], None),
 }
 
 

@@ -241,6 +241,36 @@ def gen_initial_conditions(name, nx, ny, nz, seed, mean, stdev, g):
     print(name, ic.shape)
 
 
+def gen_sor(name, nx, h, g, tol=1e-3):
+    """singleSemiAnalytic.cpp on one thread (its OpenMP sweep updates in place,
+    so only the single-thread order is reproducible): Data/SOR_Fields.txt."""
+    build_ref.build("singleSemiAnalytic", name, {"nx": nx, "h": float(h), "g": float(g), "tol": float(tol)})
+    work = build_ref.run(name, threads=1)
+    tab = build_ref.read_columns(work / "Data" / "SOR_Fields.txt").reshape(nx, 2).T.copy()
+    np.savez_compressed(OUT / f"{name}.npz", program="singleSemiAnalytic", nx=nx, h=h, g=g, tol=tol, w=1.5, n=1.0,
+                        lam=1.0, eta=1.0, profile=tab)
+    print(name, tab.shape)
+    return tab
+
+
+def gen_boost_ic(name, nx, ny, nz, g, dt, v, profile, sor_h):
+    """initialConditions.cpp, ic_type "boost" (a z-directed string boosted with
+    velocity v): Data/ic.txt, two levels (17 digits), from the given profile
+    table placed where the program reads it (dir_path/SOR_Fields.txt)."""
+    m = profile.shape[1]
+    consts = {"nx": nx, "ny": ny, "nz": nz, "ic_type": "boost", "g": float(g), "dt": float(dt),
+              "v1x": float(v[0]), "v1y": float(v[1]), "v1z": float(v[2]), "SORnx": m, "SORa": float(sor_h)}
+    build_ref.build("initialConditions", name, consts)
+    work = build_ref.SCRATCH / name
+    lines = [f"{profile[0, r]!r} {profile[1, r]!r}" for r in range(m)]
+    (work / "SOR_Fields.txt").write_text("\n".join(lines) + "\n")
+    work = build_ref.run(name)
+    ic = build_ref.read_columns(work / "Data" / "ic.txt").reshape(2, nx * ny * nz, 5).transpose(2, 0, 1).copy()
+    np.savez_compressed(OUT / f"{name}.npz", program="initialConditions", ic_type="boost", nx=nx, ny=ny, nz=nz,
+                        dx=0.5, g=g, dt=dt, v=np.array(v, dtype=np.float64), sor_h=sor_h, profile=profile, ic=ic)
+    print(name, ic.shape)
+
+
 def main():
     if not build_ref.reference_available():
         raise SystemExit("reference sources not found; fixtures can only be made where they are")
@@ -282,6 +312,10 @@ def main():
                   xyBC="fixed", zBC="periodic")
     gen_evolution("ref_evol_bc_per_zfixed", 9, 8, 9, 8, lam=2.0, g=0.7, alpha=3.0, bc=BC_FIXED, seed=25, saveFreq=4,
                   xyBC="periodic", zBC="fixed")
+    # straight-string profiles (global and gauged) and the boosted-string IC built on the gauged one
+    gen_sor("ref_sor_global", 3001, 0.01, 0.0)
+    prof = gen_sor("ref_sor_gauge", 2001, 0.01, 1.0)
+    gen_boost_ic("ref_boost_ic", 13, 12, 11, 1.0, 0.05, (0.24, 0.6 * (1 - 0.4 ** 2) ** 0.5, 0.0), prof, 0.01)
 
 
 if __name__ == "__main__":
