@@ -45,8 +45,19 @@ struct BatchJob {
 struct BatchStep {
     int njobs;
     int total_items;
+    int begin[kBatchMaxJobs];  // jobs[q].item_begin, contiguous for the item -> job lookup
     BatchJob jobs[kBatchMaxJobs];
 };
+
+// x-planes per work item of a lattice in a batch: long x-ranges (one
+// prologue per 64 planes), but at least two x-chunks for x-ranges up to 32
+// planes, where a single chunk leaves too few items per lattice.  Chosen from
+// a sweep of 4..128 on ensembles of 32^3, 64^3 and 128^3 lattices.
+int batch_chunk(const Geom& g)
+{
+    const int x = g.hix - g.lox;
+    return std::min(x, x <= 32 ? 16 : 64);
+}
 
 namespace {
 
@@ -66,7 +77,7 @@ __device__ __forceinline__ void run_item(unsigned char* smem_raw, const BatchJob
 // the work items of all of them.  One kernel per model keeps each kernel's
 // register use to that model's tile.
 template <int NS>
-__global__ void __launch_bounds__(TT_THREADS, NS == 1 ? 4 : 2) batch_step_kernel(const BatchStep* __restrict__ tab)
+__global__ void __launch_bounds__(TT_THREADS, NS == 1 ? 4 : 3) batch_step_kernel(const BatchStep* __restrict__ tab)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ BatchJob sj;
@@ -76,14 +87,17 @@ __global__ void __launch_bounds__(TT_THREADS, NS == 1 ? 4 : 2) batch_step_kernel
     const int nj = tab->njobs;
     const int tid = threadIdx.y * TT_Z + threadIdx.x;
     for (int w = blockIdx.x; w < total; w += gridDim.x) {
-        if (tid == 0) {
-            int lo = 0, hi = nj - 1;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (tab->jobs[mid].item_begin <= w) lo = mid;
-                else hi = mid - 1;
+        if (tid < 32) {
+            // the job of item w: jobs whose first item is <= w, counted by one
+            // warp over the contiguous begin[] (all loads independent)
+            int cnt = 0;
+#pragma unroll
+            for (int r = 0; r < kBatchMaxJobs / 32; ++r) {
+                const int q = r * 32 + tid;
+                const bool le = q < nj && tab->begin[q] <= w;
+                cnt += __popc(__ballot_sync(0xffffffffu, le));
             }
-            s_job = lo;
+            if (tid == 0) s_job = cnt - 1;
         }
         __syncthreads();
         // stage the job descriptor in shared memory (its coefficients are read
@@ -170,6 +184,7 @@ struct lat_batch {
     cudaStream_t stream = nullptr;
     int grid[2] = {0, 0};            // persistent CTAs of the AH / Moore step kernels
     int K = 0;                       // steps in the captured graph
+    int chunk = 0;                   // x-planes per work item; 0: the per-shape rule
     BatchStep* tab_host = nullptr;   // pinned [K][2]: per step, AH jobs then Moore jobs
     BatchStep* tab_dev = nullptr;    // [K][2]
     double* diag_dev = nullptr;      // [K][max_jobs][2]
@@ -313,6 +328,16 @@ int lat_batch_remove(lat_batch* b, lat_handle* h)
 
 int lat_batch_size(const lat_batch* b) { return b ? (int)b->jobs.size() : LAT_ERR_INVALID; }
 
+int lat_batch_set_chunk(lat_batch* b, int32_t chunk)
+{
+    if (!b || chunk < 0 || chunk > 4096) {
+        set_error("lat_batch_set_chunk: chunk must be in [0, 4096]");
+        return LAT_ERR_INVALID;
+    }
+    b->chunk = chunk;
+    return LAT_OK;
+}
+
 int64_t lat_batch_kernel_launches(const lat_batch* b) { return b ? b->launches : LAT_ERR_INVALID; }
 
 int lat_batch_advance(lat_batch* b, int32_t nsteps)
@@ -396,15 +421,16 @@ int lat_batch_advance(lat_batch* b, int32_t nsteps)
             J.d.write = 1;
             J.diag = diag ? 1 : 0;
             // In a batch the other lattices supply the parallelism, so each
-            // lattice marches long x-ranges (one prologue per 128 planes).  The
-            // value depends on the lattice's own shape only, never on its
-            // company, so results do not depend on the mix.
-            J.chunk = std::min(h->geom.hix - h->geom.lox, 128);
+            // lattice marches long x-ranges (batch_chunk).  The value depends
+            // on the lattice's own shape only, never on its company, so
+            // results do not depend on the mix.
+            J.chunk = b->chunk > 0 ? std::min(h->geom.hix - h->geom.lox, b->chunk) : batch_chunk(h->geom);
             const dim3 tg = tiled_grid(h->geom, J.chunk);
             J.tiles_z = (int)tg.x;
             J.tiles_y = (int)tg.y;
             J.items = (int)(tg.x * tg.y * tg.z);
             J.item_begin = T.total_items;
+            T.begin[T.njobs] = T.total_items;
             J.diag_out = b->diag_dev + 2 * ((size_t)s * b->max_jobs + (size_t)q);
             T.total_items += J.items;
             ++T.njobs;

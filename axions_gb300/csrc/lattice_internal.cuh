@@ -115,6 +115,8 @@ cudaError_t launch_ah_twopass_fast(const Geom&, const Fields<double, 5>&, double
 // x-planes per CTA of the tiled FP32 step for a new handle (tuned value of the
 // shape if known in this process, else a heuristic); tune.cu
 int default_chunk(const lat_params& p);
+// x-planes per work item of a lattice stepped in a batch (its shape only)
+int batch_chunk(const Geom& g);
 // number of CTAs (and diagnostic partials) of the tiled FP32 step
 int tiled_blocks(const Geom&, int chunk);
 // tiled, x-marching FP32 Abelian-Higgs step; `chunk` x-planes per CTA

@@ -126,7 +126,7 @@ void finish(lat_server* s, int64_t id, int status)
         if (status == 2) {
             // the per-shape chunk of the batch, so that the final diagnostics
             // depend on the job only (not on tuning done elsewhere in the process)
-            j.h->chunk = std::min(j.h->geom.hix - j.h->geom.lox, 128);
+            j.h->chunk = lat::batch_chunk(j.h->geom);
             lat_diag fd;
             if (lat_diagnostics(j.h, &fd) == LAT_OK) {
                 j.res.final_energy = fd.energy;

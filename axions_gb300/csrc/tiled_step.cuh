@@ -98,22 +98,21 @@ __device__ __forceinline__ void charged(T theta, T c1, T s1, const Charges<T>& c
 }
 
 // Issue the asynchronous copy of plane `pi` (tile + halo) into stage `b`.
-// One warp per halo row: lane l copies column l, lanes 0-1 also the last two.
+// The TT_HY x TT_HZ staged positions are spread evenly over the CTA's threads
+// (no warp copies more than two), so no warp arrives late at the barrier.
 template <class T, int NS>
 __device__ __forceinline__ void stage_plane(TiledSmem<T, NS>& sm, int b, const Fields<T, 2 * NS + 3>& f, const Geom& g,
                                             int pi, int j0, int k0)
 {
-    const int lane = threadIdx.x, warp = threadIdx.y;
+    const int tid = threadIdx.y * TT_Z + threadIdx.x;
     const int base = pi * g.syz;
-    for (int hy = warp; hy < TT_HY; hy += TT_Y) {
-        const int row = base + wrap_idx(j0 - 1 + hy, g.ny) * g.nz;
-        for (int hz = lane; hz < TT_HZ; hz += TT_Z) {
-            const int s = row + wrap_idx(k0 - 1 + hz, g.nz);
+    for (int q = tid; q < TT_HY * TT_HZ; q += TT_THREADS) {
+        const int hy = q / TT_HZ, hz = q - hy * TT_HZ;
+        const int s = base + wrap_idx(j0 - 1 + hy, g.ny) * g.nz + wrap_idx(k0 - 1 + hz, g.nz);
 #pragma unroll
-            for (int m = 0; m < 3; ++m) __pipeline_memcpy_async(&sm.th[b][m][hy][hz], f.now[2 * NS + m] + s, sizeof(T));
+        for (int m = 0; m < 3; ++m) __pipeline_memcpy_async(&sm.th[b][m][hy][hz], f.now[2 * NS + m] + s, sizeof(T));
 #pragma unroll
-            for (int c = 0; c < 2 * NS; ++c) __pipeline_memcpy_async(&sm.ph[b][c][hy][hz], f.now[c] + s, sizeof(T));
-        }
+        for (int c = 0; c < 2 * NS; ++c) __pipeline_memcpy_async(&sm.ph[b][c][hy][hz], f.now[c] + s, sizeof(T));
     }
     __pipeline_commit();
 }
@@ -172,13 +171,29 @@ __device__ __forceinline__ void tiled_tile(TiledSmem<T, NS>& sm, const Geom& g, 
 
     double e_acc = 0.0, g_acc = 0.0;
 
+    // Two barriers per plane.  The first (after the wait) makes planes i and
+    // i+1 visible and ends every read of plane i-1's stage and of the link
+    // data of plane i-1, so plane i+2 may then be copied into that stage and
+    // the link data rewritten.  The second publishes the link data.
     for (int i = ib; i < ie; ++i) {
         const int nxt = cur == 2 ? 0 : cur + 1;
         const int nn = nxt == 2 ? 0 : nxt + 1;
-        if (i + 1 < ie) stage_plane<T, NS>(sm, nn, f, g, wrap_idx(i + 2, g.nx), j0, k0);
-        else __pipeline_commit();
-        __pipeline_wait_prior(1);  // planes i and i+1 have landed
+        __pipeline_wait_prior(0);  // planes i and i+1 have landed
         __syncthreads();
+        if (i + 1 < ie) stage_plane<T, NS>(sm, nn, f, g, wrap_idx(i + 2, g.nx), j0, k0);
+        // the own site's level n-1, loaded now so that the link phase covers
+        // the memory latency
+        const int s = (i * g.ny + jj) * g.nz + kk;
+        T qv[2 * NS], qx = 0, qy = 0, qz = 0;
+#pragma unroll
+        for (int cc = 0; cc < 2 * NS; ++cc) qv[cc] = 0;
+        if (active) {
+#pragma unroll
+            for (int cc = 0; cc < 2 * NS; ++cc) qv[cc] = f.past[cc][s];
+            qx = f.past[TH0][s];
+            qy = f.past[TH0 + 1][s];
+            qz = f.past[TH0 + 2][s];
+        }
 
         // ---- link data of one staged position (ly, lz) of the current plane
         auto links = [&](int ly, int lz, T* cyq, T* syq, T* czq, T* szq, T& sxy, T& sxz, T& syz, T* cxq, T* sxq,
@@ -245,11 +260,6 @@ __device__ __forceinline__ void tiled_tile(TiledSmem<T, NS>& sm, const Geom& g, 
         for (int cc = 0; cc < 2 * NS; ++cc) v[cc] = sm.ph[cur][cc][hy][hz];
         const T tx = sm.th[cur][0][hy][hz], tyv = sm.th[cur][1][hy][hz], tzv = sm.th[cur][2][hy][hz];
         if (active) {
-            const int s = (i * g.ny + j) * g.nz + k;
-            T qv[2 * NS];
-#pragma unroll
-            for (int cc = 0; cc < 2 * NS; ++cc) qv[cc] = f.past[cc][s];
-            const T qx = f.past[TH0][s], qy = f.past[TH0 + 1][s], qz = f.past[TH0 + 2][s];
             const T sPxy_ym = sm.L[LI::pxy][hy - 1][hz], sPyz_ym = sm.L[LI::pyz][hy - 1][hz];
             const T sPxz_zm = sm.L[LI::pxz][hy][hz - 1], sPyz_zm = sm.L[LI::pyz][hy][hz - 1];
 
@@ -387,9 +397,8 @@ __device__ __forceinline__ void tiled_tile(TiledSmem<T, NS>& sm, const Geom& g, 
 #pragma unroll
         for (int cc = 0; cc < 2 * NS; ++cc) vm[cc] = v[cc];
         cur = nxt;
-        __syncthreads();  // stage `cur` and the link data are overwritten next
     }
-    __pipeline_wait_prior(0);
+    __pipeline_wait_prior(0);  // nothing is in flight here; kept for an empty x-range
 
     if constexpr (DIAG) {
 #pragma unroll
@@ -416,7 +425,7 @@ __device__ __forceinline__ void tiled_tile(TiledSmem<T, NS>& sm, const Geom& g, 
 }
 
 template <class T, int NS, bool DIAG>
-__global__ void __launch_bounds__(TT_THREADS, NS == 1 ? 4 : 2)
+__global__ void __launch_bounds__(TT_THREADS, NS == 1 ? 4 : 3)
 tiled_step_kernel(const Geom g, const Fields<T, 2 * NS + 3> f, const StepCoefT<T> c, const Charges<T> ch,
                   const DiagOut d, const int chunk)
 {

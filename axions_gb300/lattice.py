@@ -31,7 +31,7 @@ EXPORTS = [
     "lat_snapshot_doubles", "lat_snapshot_begin", "lat_snapshot_wait", "lat_host_alloc", "lat_host_free",
     "lat_ah_step_f64_noalloc",
     "lat_batch_create", "lat_batch_destroy", "lat_batch_add", "lat_batch_remove", "lat_batch_size",
-    "lat_batch_kernel_launches", "lat_batch_advance", "lat_batch_take_diags",
+    "lat_batch_kernel_launches", "lat_batch_set_chunk", "lat_batch_advance", "lat_batch_take_diags",
     "lat_random_phase_ic_device", "lat_philox4x32_10", "lat_autotune", "lat_get_tuning", "lat_set_tuning",
     "lat_tune_cache_save", "lat_tune_cache_load", "lat_footprint_bytes",
     "lat_server_create", "lat_server_submit", "lat_server_poll", "lat_server_wait", "lat_server_diags",
@@ -111,6 +111,7 @@ def load_library(path: Path | None = None):
     L.lat_batch_kernel_launches.argtypes = [vp]
     L.lat_batch_kernel_launches.restype = ctypes.c_int64
     L.lat_batch_advance.argtypes = [vp, ctypes.c_int32]
+    L.lat_batch_set_chunk.argtypes = [vp, ctypes.c_int32]
     L.lat_batch_take_diags.argtypes = [vp, vp, P(LatDiag), ctypes.c_int64, P(ctypes.c_int64)]
     u32p = P(ctypes.c_uint32)
     L.lat_random_phase_ic_device.argtypes = [vp, ctypes.c_uint64, ctypes.c_int32]
@@ -395,6 +396,10 @@ class Batch:
     @property
     def kernel_launches(self) -> int:
         return int(self.L.lat_batch_kernel_launches(self.b))
+
+    def set_chunk(self, chunk: int):
+        """x-planes per work item of every lattice (0: the per-shape default)."""
+        _check("lat_batch_set_chunk", self.L.lat_batch_set_chunk(self.b, int(chunk)))
 
     def close(self):
         if getattr(self, "b", None) is not None and self.b.value:

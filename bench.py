@@ -225,6 +225,30 @@ def load_traffic(precision: str, n: int):
         return None
 
 
+def fp64_ceiling(precision: str, res: dict, peaks: dict):
+    """The second ceiling of an FP64 step: FP64 instructions (DFMA, DADD,
+    DMUL per site, from the committed ncu summary) per second against the FP64
+    pipe's issue peak, 2 per SM per cycle at the SM clock sampled during the
+    timed region."""
+    f = ROOT / "profiles" / "traffic.json"
+    if precision == "f32" or not f.exists():
+        return None
+    try:
+        d = json.loads(f.read_text())
+        e = d.get(f"{'moore' if MODEL['name'] == 'moore' else 'ah'}_step_{precision}")
+        if not e or "fp64_inst_per_site" not in e:
+            return None
+        import torch
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+        mhz = (res.get("clocks") or {}).get("sm_mhz") or peaks.get("sm_max_mhz") or 2070.0
+        peak = d["fp64_issue_peak_per_sm_per_cycle"] * sms * mhz * 1e6 / 1e9
+        ach = e["fp64_inst_per_site"] * res["sites"] / (res["kern_ms"] * 1e-3) / 1e9
+        return {"bound": "fp64_pipe", "achieved": ach, "peak": peak, "unit": "G FP64-inst/s", "frac": ach / peak,
+                "inst_per_site": e["fp64_inst_per_site"], "sm_mhz": mhz, "sms": sms}
+    except Exception:
+        return None
+
+
 def measure_gpu(n: int, precision: str, steps: int, warmup: int, ws: int, local: int, peaks: dict):
     import numpy as np
     import torch
@@ -665,7 +689,8 @@ def main():
         forms[form] = {"value": units / (t2 * 1e-3), "ms_per_step": t2 / steps,
                        "dtype": "f32" if form == "f32" else "f64", "kernel_ms": r2["kern_ms"],
                        "roofline": {"bound": "hbm", "achieved": ach2, "peak": hbm, "unit": "GB/s",
-                                    "frac": ach2 / hbm, "traffic": load_traffic(form, n)},
+                                    "frac": ach2 / hbm, "traffic": load_traffic(form, n),
+                                    "fp64_pipe": fp64_ceiling(form, r2, peaks)},
                        "speedup_vs_f64": res["total_ms"] / r2["total_ms"]}
     def note(leg, t0):
         print(f"bench: {leg} done in {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
@@ -708,7 +733,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": load_traffic(head, n), "peak_source": peak_src,
                      "kernel": kernel_name(head), "kernel_ms": res["kern_ms"],
-                     "bytes_per_site": bytes_per_site(head)},
+                     "bytes_per_site": bytes_per_site(head), "fp64_pipe": fp64_ceiling(head, res, peaks)},
         "cpu_baseline": cpu,
         "e2e": {"value": units / (e2e_max * 1e-3), "unit": "site-updates/s",
                 "h2d_bytes_per_step": res["e2e_h2d"], "d2h_bytes_per_step": res["e2e_d2h"]},

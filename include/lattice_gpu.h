@@ -343,6 +343,11 @@ int lat_batch_destroy(lat_batch* b);                               /* handles ar
 int lat_batch_add(lat_batch* b, lat_handle* h, int32_t diag_every, int64_t stop_step);
 int lat_batch_remove(lat_batch* b, lat_handle* h);
 int lat_batch_size(const lat_batch* b);
+/* x-planes per work item for every lattice of the batch (clamped to its x
+   extent); 0 restores the default, which depends on each lattice's shape only
+   (64, or 16 for x extents up to 32, clamped to the extent).  Only the
+   partial sums of the diagnostics depend on it. */
+int lat_batch_set_chunk(lat_batch* b, int32_t chunk);
 int64_t lat_batch_kernel_launches(const lat_batch* b);
 /* Advance every lattice by up to nsteps (not past its stop_step).  Returns the
  * number of lattices that have not reached their stop_step. */

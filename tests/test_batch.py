@@ -112,3 +112,34 @@ def test_batch_rejects_fp64_handles():
         with pytest.raises(lattice.LatticeError):
             b.add(lat)
     lat.close()
+
+
+def test_batch_chunk_changes_only_the_diagnostic_sums():
+    """The x-chunk of the work items decides the tiling only: the fields are
+    bitwise the same for any chunk, the diagnostics agree to the rounding of
+    their partial sums."""
+    from axions_gb300 import lattice
+    specs = SPECS[:2] + SPECS[3:]
+    ref = None
+    for chunk in (0, 4, 16, 128):
+        lats = [_lat(lattice, m, s, sd, lam, g) for (m, s, sd, lam, g, _, _) in specs]
+        with lattice.Batch(4) as b:
+            b.set_chunk(chunk)
+            for lat, spec in zip(lats, specs):
+                b.add(lat, diag_every=spec[6], stop_step=spec[5])
+            while b.advance(7) > 0:
+                pass
+            out = [(lat.get_slots(), b.take_diags(lat)) for lat in lats]
+        for lat in lats:
+            lat.close()
+        if ref is None:
+            ref = out
+            continue
+        for (st, d), (st0, d0) in zip(out, ref):
+            assert np.array_equal(st, st0)
+            assert [x[0] for x in d] == [x[0] for x in d0]
+            np.testing.assert_allclose([x[1] for x in d], [x[1] for x in d0], rtol=1e-12)
+            np.testing.assert_allclose([x[2] for x in d], [x[2] for x in d0], rtol=1e-12)
+    with lattice.Batch(1) as b:
+        with pytest.raises(lattice.LatticeError):
+            b.set_chunk(-1)
