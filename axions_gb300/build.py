@@ -38,6 +38,7 @@ UNITS = {
     "string_length.cu": ["-fmad=false"],
     "snapshot.cu": ["-fmad=false"],
     "boundary.cu": ["-fmad=false"],
+    "string_ic.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
     "ah_f64_fast.cu": [],
     "ah_f32.cu": [],

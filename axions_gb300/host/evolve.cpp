@@ -195,6 +195,16 @@ Params::Params(Program prog)
         v["ic_in"] = "";     // convert: the table to read (under Data/)
         v["cols"] = "5";     // convert: columns of the table
         v["levels"] = "1";   // convert: rows = levels * nx * ny * nz
+        // boost (initialConditions.cpp:41-44,62-68): the straight-string table
+        // (singleSemiAnalytic's output, read from out_dir/sor_file) and the
+        // boost velocity 0.6*(0.4, sqrt(1 - 0.4^2), 0)
+        v["sor_file"] = "SOR_Fields.txt";
+        v["SORnx"] = "20001";
+        v["SORa"] = "0.01";
+        v["n"] = "1";
+        v["v1x"] = "0.24";
+        v["v1y"] = "0.5499090833947008";
+        v["v1z"] = "0";
         break;
     case Program::SingleSemiAnalytic:
         // singleSemiAnalytic.cpp:19-33; ic_type 0 starts from eta*tanh(r/2),
@@ -758,6 +768,56 @@ bool ends_with(const std::string& s, const std::string& suffix)
 // Written as Data/<ic_file>: text (the reference's format and precision) or,
 // for a name ending in .bin, the binary form.  ic_type = convert reads
 // Data/<ic_in> (text or binary) and writes it as Data/<ic_file>.
+// The boosted-string IC (both levels) built on the GPU from the straight-string
+// table at out_dir/sor_file: column-major [5][2N], level 0 (t = 0) rows first.
+void boost_ic_table(Params& q, const std::string& dir, int form, std::vector<double>& tab)
+{
+    const int64_t m = q.integer("SORnx");
+    std::vector<double> prof;
+    read_table(dir + "/" + q.str("sor_file"), 2, m, prof);
+    lat_params p;
+    check(lat_params_init(&p, LAT_MODEL_AH), "lat_params_init");
+    p.nx = q.integer("nx");
+    p.ny = q.integer("ny");
+    p.nz = q.integer("nz");
+    p.dx = q.num("dx");
+    p.dy = q.num("dy");
+    p.dz = q.num("dz");
+    p.dt = q.num("dt");
+    p.g = q.num("g");
+    p.precision = LAT_F64;
+    lat_handle* h = nullptr;
+    check(lat_create(&p, &h), "lat_create");
+    lat_string_profile sp;
+    sp.phi = prof.data();
+    sp.A = prof.data() + m;
+    sp.m = m;
+    sp.h = q.num("SORa");
+    sp.winding = q.num("n");
+    lat_boost_ic b;
+    b.v[0] = q.num("v1x");
+    b.v[1] = q.num("v1y");
+    b.v[2] = q.num("v1z");
+    b.form = form;
+    b.reserved = 0;
+    int64_t off = 0;
+    const int rc = lat_boost_ic_device(h, &sp, &b, &off);
+    if (rc != LAT_OK) {
+        lat_destroy(h);
+        check(rc, "lat_boost_ic_device");
+    }
+    const int64_t N = p.nx * p.ny * p.nz;
+    std::vector<double> now((size_t)5 * N), past((size_t)5 * N);
+    check(lat_get_state(h, now.data(), past.data()), "lat_get_state");
+    lat_destroy(h);
+    if (off) std::cout << "Off straight string solution grid at " << off << " site evaluations" << std::endl;
+    tab.assign((size_t)10 * N, 0.0);
+    for (int c = 0; c < 5; ++c) {
+        std::copy(past.begin() + c * N, past.begin() + (c + 1) * N, tab.begin() + (size_t)c * 2 * N);
+        std::copy(now.begin() + c * N, now.begin() + (c + 1) * N, tab.begin() + (size_t)c * 2 * N + N);
+    }
+}
+
 int run_initial_conditions(Params& q)
 {
     struct timeval start, end;
@@ -783,13 +843,16 @@ int run_initial_conditions(Params& q)
             tab[3 * N + s] = q.num("dy") * g * A;
             tab[4 * N + s] = q.num("dz") * g * A;
         }
+    } else if (type == "boost") {
+        boost_ic_table(q, dir, LAT_IC_FORM_FILE, tab);
+        rows = 2 * N;
     } else if (type == "convert") {
         cols = (int)q.integer("cols");
         rows = q.integer("levels") * N;
         if (q.str("ic_in").empty()) fail("ic_type = convert needs ic_in");
         read_table(dir + "/Data/" + q.str("ic_in"), cols, rows, tab);
     } else {
-        fail("ic_type: this program provides \"random\" and \"convert\"");
+        fail("ic_type: this program provides \"random\", \"boost\" and \"convert\"");
     }
     if (ends_with(out, ".bin")) write_table_bin(out, cols, rows, tab.data());
     else write_table_text(out, cols, rows, tab.data(), digits);

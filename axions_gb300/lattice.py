@@ -32,7 +32,7 @@ EXPORTS = [
     "lat_ah_step_f64_noalloc",
     "lat_batch_create", "lat_batch_destroy", "lat_batch_add", "lat_batch_remove", "lat_batch_size",
     "lat_batch_kernel_launches", "lat_batch_set_chunk", "lat_batch_advance", "lat_batch_take_diags",
-    "lat_random_phase_ic_device", "lat_philox4x32_10", "lat_autotune", "lat_get_tuning", "lat_set_tuning",
+    "lat_random_phase_ic_device", "lat_boost_ic_device", "lat_philox4x32_10", "lat_autotune", "lat_get_tuning", "lat_set_tuning",
     "lat_tune_cache_save", "lat_tune_cache_load", "lat_footprint_bytes",
     "lat_server_create", "lat_server_submit", "lat_server_poll", "lat_server_wait", "lat_server_diags",
     "lat_server_get_stats", "lat_server_destroy",
@@ -115,6 +115,7 @@ def load_library(path: Path | None = None):
     L.lat_batch_take_diags.argtypes = [vp, vp, P(LatDiag), ctypes.c_int64, P(ctypes.c_int64)]
     u32p = P(ctypes.c_uint32)
     L.lat_random_phase_ic_device.argtypes = [vp, ctypes.c_uint64, ctypes.c_int32]
+    L.lat_boost_ic_device.argtypes = [vp, vp, vp, P(ctypes.c_int64)]
     L.lat_philox4x32_10.argtypes = [u32p, u32p, u32p]
     L.lat_autotune.argtypes = [vp, ctypes.c_int32, P(LatTuning)]
     L.lat_get_tuning.argtypes = [vp, P(LatTuning)]
@@ -227,6 +228,20 @@ class Lattice:
         """Random-phase IC drawn on the GPU (Philox-4x32-10); state at TimeStep 0."""
         _check("lat_random_phase_ic_device",
                self.L.lat_random_phase_ic_device(self.h, ctypes.c_uint64(seed), int(bool(independent))))
+
+    def boost_ic_device(self, phi, A, h: float, v, form: int = 0, winding: float = 1.0) -> int:
+        """Boosted straight-string IC (initialConditions.cpp:710-992, form 0;
+        ic_func.cpp:685-964, form 1) from the profile table (phi, A) with
+        spacing h, built on the GPU; state at TimeStep 0.  Returns the number
+        of site evaluations that fell beyond the table."""
+        from .params import boost_ic, string_profile
+        prof, keep = string_profile(phi, A, h, winding)
+        b = boost_ic(v, form)
+        off = ctypes.c_int64(0)
+        _check("lat_boost_ic_device", self.L.lat_boost_ic_device(self.h, ctypes.byref(prof), ctypes.byref(b),
+                                                                 ctypes.byref(off)))
+        del keep
+        return int(off.value)
 
     def autotune(self, trial_steps: int = 3) -> LatTuning:
         t = LatTuning()

@@ -154,3 +154,38 @@ def make_params(model: int = MODEL_AH, **kw) -> LatParams:
             raise KeyError(k)
         setattr(p, k, v)
     return p
+
+
+# ---- string initial conditions (lat_string_profile, lat_boost_ic) ----------
+IC_FORM_FILE = 0        # initialConditions.cpp rounding
+IC_FORM_INPROCESS = 1   # ic_func.cpp rounding
+
+
+class LatStringProfile(ctypes.Structure):
+    _fields_ = [("phi", ctypes.POINTER(ctypes.c_double)), ("A", ctypes.POINTER(ctypes.c_double)),
+                ("m", ctypes.c_int64), ("h", ctypes.c_double), ("winding", ctypes.c_double)]
+
+
+class LatBoostIC(ctypes.Structure):
+    _fields_ = [("v", ctypes.c_double * 3), ("form", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+def string_profile(phi, A, h: float, winding: float = 1.0):
+    """A LatStringProfile over float64 copies of phi and A; returns (struct,
+    arrays) — keep the arrays alive while the struct is in use."""
+    import numpy as np
+    phi = np.ascontiguousarray(phi, dtype=np.float64)
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    if phi.shape != A.shape or phi.ndim != 1:
+        raise ValueError("phi and A must be 1-d arrays of the same length")
+    dp = ctypes.POINTER(ctypes.c_double)
+    s = LatStringProfile(phi.ctypes.data_as(dp), A.ctypes.data_as(dp), len(phi), float(h), float(winding))
+    return s, (phi, A)
+
+
+def boost_ic(v, form: int = IC_FORM_FILE) -> LatBoostIC:
+    b = LatBoostIC()
+    for q in range(3):
+        b.v[q] = float(v[q])
+    b.form = int(form)
+    return b

@@ -301,6 +301,44 @@ void lat_host_free(void* ptr);
  * ensembles and served jobs, where reproducing it is not needed.  No
  * counterpart in the reference. */
 int lat_random_phase_ic_device(lat_handle* h, uint64_t seed, int32_t independent);
+
+/* ---- string initial conditions from a straight-string profile --------------------
+ * The radial profile of a static straight string of winding n, as
+ * singleSemiAnalytic.cpp writes it to SOR_Fields.txt: phi[i] = |phi|(r_i),
+ * A[i] = A_theta(r_i), r_i = i*h.  The reference's families read it with
+ * second-order interpolation about the nearest point (first order at r < h/2,
+ * initialConditions.cpp:760-774).  A site farther out than the table's last
+ * interior point takes |phi| = 1, A = n/g (0 for g = 0), as the reference does
+ * off its table; the reference also reads one entry past its table when the
+ * nearest point is the last one, which here counts as off the table. */
+typedef struct lat_string_profile {
+    const double* phi;   /* m host values */
+    const double* A;     /* m host values */
+    int64_t m;           /* >= 2 */
+    double h;            /* > 0 */
+    double winding;      /* n */
+} lat_string_profile;
+
+/* the two roundings of the reference's boost family: initialConditions.cpp
+ * builds A and writes d*g*A; ic_func.cpp (the in-process IC of ic_w_evolution)
+ * writes theta = d*g*(...) and adds the gauge shift to theta */
+#define LAT_IC_FORM_FILE      0
+#define LAT_IC_FORM_INPROCESS 1
+
+typedef struct lat_boost_ic {
+    double v[3];         /* boost velocity, |v| < 1, not 0 */
+    int32_t form;        /* LAT_IC_FORM_* */
+    int32_t reserved;
+} lat_boost_ic;
+
+/* A z-directed straight string at the lattice centre, Lorentz-boosted with
+ * velocity v (initialConditions.cpp:710-992, ic_func.cpp:685-964): the fields
+ * at t = 0 go to the past slot and those at t = dt (with the gauge
+ * transformation back to temporal gauge) to the current slot; time step 0.
+ * Uses the handle's sizes (each >= 2), spacings, dt and g.  `off_table` (may
+ * be null) receives the number of site evaluations beyond the profile table.
+ * Abelian-Higgs handles only. */
+int lat_boost_ic_device(lat_handle* h, const lat_string_profile* prof, const lat_boost_ic* b, int64_t* off_table);
 /* The generator on the host (checks, reproduction of device ICs). */
 int lat_philox4x32_10(const uint32_t counter[4], const uint32_t key[2], uint32_t out[4]);
 

@@ -1131,3 +1131,140 @@ int orc_string_length(const lat_params* p, const double* xyz, int64_t M, int spl
     free(alive);
     return 0;
 }
+
+
+/* ---------------------------------------------------------------------------
+ * Boosted straight-string IC, initialConditions.cpp:710-992 and
+ * ic_func.cpp:685-964, restated with the reference's operation order and
+ * libm calls (pow(x, 2) included).
+ * ------------------------------------------------------------------------- */
+
+/* |phi| and A_theta at distance d: initialConditions.cpp:756-782 (second
+ * order about the nearest table point, first order next to r = 0); beyond the
+ * table (and at its last point, where the reference reads one past its end)
+ * |phi| = 1, A = n/g. */
+static int profile_at(const lat_string_profile* pr, double g, double d, double* phiMag, double* AMag)
+{
+    const double a = pr->h;
+    const int64_t p = (int64_t)round(d / a);
+    const double* S0 = pr->phi;
+    const double* S1 = pr->A;
+    if (p == 0) {
+        *phiMag = (S0[p + 1] * d - S0[p] * (d - a)) / a;
+        *AMag = (S1[p + 1] * d - S1[p] * (d - a)) / a;
+        return 0;
+    }
+    if (p + 1 < pr->m) {
+        const double pa = (double)p * a, pp = (double)(p + 1) * a, pm = (double)(p - 1) * a;
+        *phiMag = (S0[p - 1] * (d - pa) * (d - pp) - 2 * S0[p] * (d - pm) * (d - pp) + S0[p + 1] * (d - pm) * (d - pa))
+                / (2 * a * a);
+        *AMag = (S1[p - 1] * (d - pa) * (d - pp) - 2 * S1[p] * (d - pm) * (d - pp) + S1[p + 1] * (d - pm) * (d - pa))
+              / (2 * a * a);
+        return 0;
+    }
+    *phiMag = 1;
+    *AMag = g == 0 ? 0 : pr->winding / g;
+    return 1;
+}
+
+int64_t orc_boost_ic(const lat_params* p, const lat_string_profile* prof, const lat_boost_ic* b, double* st)
+{
+    const int nx = p->nx, ny = p->ny, nz = p->nz;
+    if (nx < 2 || ny < 2 || nz < 2 || !prof || prof->m < 2 || !(prof->h > 0) || !b) return -1;
+    const int64_t N = (int64_t)nx * ny * nz;
+    const double dx = p->dx, dy = p->dy, dz = p->dz, dt = p->dt, g = p->g;
+    const double v1x = b->v[0], v1y = b->v[1], v1z = b->v[2];
+    const double vMagSqr = pow(v1x, 2) + pow(v1y, 2) + pow(v1z, 2);
+    if (!(vMagSqr > 0 && vMagSqr < 1)) return -1;
+    const double gamma = 1 / sqrt(1 - vMagSqr);
+    const int x0 = (nx - 1) / 2, y0 = (ny - 1) / 2, z0 = (nz - 1) / 2;
+    double* At = (double*)malloc(sizeof(double) * (size_t)N);
+    if (!At) return -1;
+#define BST(c, t) (st + ((size_t)(c) * 2 + (t)) * (size_t)N)
+    int64_t off = 0;
+    /* t = 0 (zb uses dy, initialConditions.cpp:745) */
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j)
+            for (int k = 0; k < nz; ++k) {
+                const int64_t s = ((int64_t)i * ny + j) * nz + k;
+                const double xb = (i - x0) * dx, yb = (j - y0) * dy, zb = (k - z0) * dy;
+                const double xs = xb + (gamma - 1) * (v1x * xb + v1y * yb + v1z * zb) * v1x / vMagSqr;
+                const double ys = yb + (gamma - 1) * (v1x * xb + v1y * yb + v1z * zb) * v1y / vMagSqr;
+                const double distance = sqrt(pow(xs, 2) + pow(ys, 2));
+                double phiMag, AMag, Ax, Ay, re, im;
+                off += profile_at(prof, g, distance, &phiMag, &AMag);
+                if (xs == 0) { re = 0; Ay = 0; }
+                else { re = phiMag * xs / distance; Ay = AMag * xs / pow(distance, 2); }
+                if (ys == 0) { im = 0; Ax = 0; }
+                else { im = phiMag * ys / distance; Ax = -AMag * ys / pow(distance, 2); }
+                At[s] = -gamma * (v1x * Ax + v1y * Ay);
+                const double A0 = Ax + (gamma - 1) * (v1x * Ax + v1y * Ay) * v1x / vMagSqr;
+                const double A1 = Ay + (gamma - 1) * (v1x * Ax + v1y * Ay) * v1y / vMagSqr;
+                const double A2 = (gamma - 1) * (v1x * Ax + v1y * Ay) * v1z / vMagSqr;
+                BST(0, 0)[s] = re;
+                BST(1, 0)[s] = im;
+                BST(2, 0)[s] = dx * g * A0;
+                BST(3, 0)[s] = dy * g * A1;
+                BST(4, 0)[s] = dz * g * A2;
+            }
+    /* t = dt, then the gauge transformation that removes A_t (centred
+     * differences inside, one-sided on the faces: no periodic wrap) */
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j)
+            for (int k = 0; k < nz; ++k) {
+                const int64_t s = ((int64_t)i * ny + j) * nz + k;
+                const double xb = (i - x0) * dx, yb = (j - y0) * dy, zb = (k - z0) * dz;
+                const double xs = xb + (gamma - 1) * (v1x * xb + v1y * yb + v1z * zb) * v1x / vMagSqr - gamma * v1x * dt;
+                const double ys = yb + (gamma - 1) * (v1x * xb + v1y * yb + v1z * zb) * v1y / vMagSqr - gamma * v1y * dt;
+                const double distance = sqrt(pow(xs, 2) + pow(ys, 2));
+                double phiMag, AMag, Ax, Ay, re, im;
+                off += profile_at(prof, g, distance, &phiMag, &AMag);
+                if (xs == 0) { re = 0; Ay = 0; }
+                else { re = phiMag * xs / distance; Ay = AMag * xs / pow(distance, 2); }
+                if (ys == 0) { im = 0; Ax = 0; }
+                else { im = phiMag * ys / distance; Ax = -AMag * ys / pow(distance, 2); }
+                const int64_t sy = (int64_t)nz, sx = (int64_t)ny * nz;
+                double dAx, dAy, dAz;   /* At differences and their divisors */
+                double qx, qy, qz;
+                if (i == 0) { dAx = At[s + sx] - At[s]; qx = dx; }
+                else if (i == nx - 1) { dAx = At[s] - At[s - sx]; qx = dx; }
+                else { dAx = At[s + sx] - At[s - sx]; qx = 2 * dx; }
+                if (j == 0) { dAy = At[s + sy] - At[s]; qy = dy; }
+                else if (j == ny - 1) { dAy = At[s] - At[s - sy]; qy = dy; }
+                else { dAy = At[s + sy] - At[s - sy]; qy = 2 * dy; }
+                if (k == 0) { dAz = At[s + 1] - At[s]; qz = dz; }
+                else if (k == nz - 1) { dAz = At[s] - At[s - 1]; qz = dz; }
+                else { dAz = At[s + 1] - At[s - 1]; qz = 2 * dz; }
+                const double tx = (gamma - 1) * (v1x * Ax + v1y * Ay);
+                double th0, th1, th2;
+                if (b->form == LAT_IC_FORM_INPROCESS) {
+                    /* ic_func.cpp:901-951 */
+                    th0 = dx * g * (Ax + tx * v1x / vMagSqr);
+                    th1 = dy * g * (Ay + tx * v1y / vMagSqr);
+                    th2 = dz * g * (tx * v1z / vMagSqr);
+                    th0 += -dx * g * dt * dAx / qx;
+                    th1 += -dy * g * dt * dAy / qy;
+                    th2 += -dz * g * dt * dAz / qz;
+                } else {
+                    /* initialConditions.cpp:918-977 */
+                    double A0 = Ax + tx * v1x / vMagSqr;
+                    double A1 = Ay + tx * v1y / vMagSqr;
+                    double A2 = tx * v1z / vMagSqr;
+                    A0 += -dt * dAx / qx;
+                    A1 += -dt * dAy / qy;
+                    A2 += -dt * dAz / qz;
+                    th0 = dx * g * A0;
+                    th1 = dy * g * A1;
+                    th2 = dz * g * A2;
+                }
+                const double ang = -g * dt * At[s];
+                BST(0, 1)[s] = cos(ang) * re - sin(ang) * im;
+                BST(1, 1)[s] = cos(ang) * im + sin(ang) * re;
+                BST(2, 1)[s] = th0;
+                BST(3, 1)[s] = th1;
+                BST(4, 1)[s] = th2;
+            }
+#undef BST
+    free(At);
+    return off;
+}

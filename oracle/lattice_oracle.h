@@ -65,6 +65,12 @@ int orc_winding(const lat_params* p, const double* st, int64_t n, int field,
 /* ic_func.cpp's "random" IC (minstd_rand, uniform in [-1, 1] per component) */
 int orc_icfunc_random_ic(const lat_params* p, uint32_t seed, double* st);
 
+/* Boosted straight-string IC (initialConditions.cpp:710-992 for
+ * LAT_IC_FORM_FILE, ic_func.cpp:685-964 for LAT_IC_FORM_INPROCESS) into a
+ * full AH state: slot 0 = t 0, slot 1 = t dt.  Returns the number of site
+ * evaluations beyond the profile table, or -1 for bad arguments. */
+int64_t orc_boost_ic(const lat_params* p, const lat_string_profile* prof, const lat_boost_ic* b, double* st);
+
 /* total string length by greedy chaining of crossings, ic_w_evolution.cpp:961-1087 */
 int orc_string_length(const lat_params* p, const double* xyz, int64_t M, int split, double* L0, double* L1);
 

@@ -55,6 +55,8 @@ def lib():
         L.orc_uniform_0_2pi.restype = ctypes.c_double
         L.orc_apply_boundaries.argtypes = [P(LatParams), dp, ctypes.c_int64]
         L.orc_icfunc_random_ic.argtypes = [P(LatParams), ctypes.c_uint32, dp]
+        L.orc_boost_ic.argtypes = [P(LatParams), ctypes.c_void_p, ctypes.c_void_p, dp]
+        L.orc_boost_ic.restype = ctypes.c_int64
         L.orc_string_length.argtypes = [P(LatParams), dp, ctypes.c_int64, ctypes.c_int, dp, dp]
         _lib = L
     return _lib
@@ -155,6 +157,21 @@ def icfunc_random_ic(p: LatParams, seed: int) -> np.ndarray:
     if rc != 0:
         raise RuntimeError(f"orc_icfunc_random_ic rc={rc}")
     return st
+
+
+def boost_ic(p: LatParams, phi: np.ndarray, A: np.ndarray, h: float, v, form: int = 0, winding: float = 1.0):
+    """Boosted straight-string IC (initialConditions.cpp:710-992, form 0;
+    ic_func.cpp:685-964, form 1) from the profile table (phi, A) with spacing h.
+    Returns (state, number of evaluations off the table)."""
+    from axions_gb300.params import boost_ic as _b, string_profile
+    prof, keep = string_profile(phi, A, h, winding)
+    b = _b(v, form)
+    st = empty_state(p)
+    off = lib().orc_boost_ic(ctypes.byref(p), ctypes.byref(prof), ctypes.byref(b), _dp(st))
+    del keep
+    if off < 0:
+        raise RuntimeError("orc_boost_ic: bad arguments")
+    return st, int(off)
 
 
 def string_length(p: LatParams, xyz: np.ndarray, split: bool = True):

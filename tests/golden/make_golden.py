@@ -253,21 +253,23 @@ def gen_sor(name, nx, h, g, tol=1e-3):
     return tab
 
 
-def gen_boost_ic(name, nx, ny, nz, g, dt, v, profile, sor_h):
+def gen_boost_ic(name, nx, ny, nz, g, dt, v, profile, sor_h, dz=0.5):
     """initialConditions.cpp, ic_type "boost" (a z-directed string boosted with
     velocity v): Data/ic.txt, two levels (17 digits), from the given profile
     table placed where the program reads it (dir_path/SOR_Fields.txt)."""
     m = profile.shape[1]
     consts = {"nx": nx, "ny": ny, "nz": nz, "ic_type": "boost", "g": float(g), "dt": float(dt),
-              "v1x": float(v[0]), "v1y": float(v[1]), "v1z": float(v[2]), "SORnx": m, "SORa": float(sor_h)}
+              "v1x": float(v[0]), "v1y": float(v[1]), "v1z": float(v[2]), "SORnx": m, "SORa": float(sor_h),
+              "dz": float(dz)}
     build_ref.build("initialConditions", name, consts)
     work = build_ref.SCRATCH / name
-    lines = [f"{profile[0, r]!r} {profile[1, r]!r}" for r in range(m)]
+    lines = [f"{float(profile[0, r])!r} {float(profile[1, r])!r}" for r in range(m)]
     (work / "SOR_Fields.txt").write_text("\n".join(lines) + "\n")
     work = build_ref.run(name)
     ic = build_ref.read_columns(work / "Data" / "ic.txt").reshape(2, nx * ny * nz, 5).transpose(2, 0, 1).copy()
     np.savez_compressed(OUT / f"{name}.npz", program="initialConditions", ic_type="boost", nx=nx, ny=ny, nz=nz,
-                        dx=0.5, g=g, dt=dt, v=np.array(v, dtype=np.float64), sor_h=sor_h, profile=profile, ic=ic)
+                        dx=0.5, dy=0.5, dz=dz, g=g, dt=dt, v=np.array(v, dtype=np.float64), sor_h=sor_h,
+                        profile=profile, ic=ic)
     print(name, ic.shape)
 
 
@@ -316,6 +318,8 @@ def main():
     gen_sor("ref_sor_global", 3001, 0.01, 0.0)
     prof = gen_sor("ref_sor_gauge", 2001, 0.01, 1.0)
     gen_boost_ic("ref_boost_ic", 13, 12, 11, 1.0, 0.05, (0.24, 0.6 * (1 - 0.4 ** 2) ** 0.5, 0.0), prof, 0.01)
+    # a velocity with a z part and dz != dy (initialConditions.cpp:745 takes zb with dy at t = 0)
+    gen_boost_ic("ref_boost_ic_vz", 12, 11, 13, 0.8, 0.1, (0.3, -0.2, 0.45), prof, 0.01, dz=0.4)
 
 
 if __name__ == "__main__":

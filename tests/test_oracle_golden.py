@@ -151,3 +151,42 @@ def test_string_length_edge_cases(oracle_mod):
     # periodic image: x = -3.9 and x = 3.9 are 0.2 apart on a box of 8
     L0, L1 = O.string_length(p, np.array([[-3.9, 0.0, 0.0], [3.9, 0.0, 0.0]]))
     assert L0 == 0 and abs(L1 - (0.2 + c0)) < 1e-15
+
+
+BOOST_CASES = ["ref_boost_ic", "ref_boost_ic_vz"]
+
+
+def boost_params(z):
+    from axions_gb300.params import make_params
+    return make_params(0, nx=int(z["nx"]), ny=int(z["ny"]), nz=int(z["nz"]), dx=float(z["dx"]), dy=float(z["dy"]),
+                       dz=float(z["dz"]), dt=float(z["dt"]), g=float(z["g"]))
+
+
+@pytest.mark.parametrize("name", BOOST_CASES)
+def test_boost_ic_bit_exact(oracle_mod, name):
+    """initialConditions.cpp "boost" (both levels of Data/ic.txt) from the
+    straight-string table that singleSemiAnalytic.cpp produced."""
+    z = load_golden(name)
+    st, off = oracle_mod.boost_ic(boost_params(z), z["profile"][0], z["profile"][1], float(z["sor_h"]), z["v"])
+    assert off == 0
+    assert np.array_equal(st.reshape(5, 2, -1), z["ic"])
+
+
+def test_boost_ic_forms_and_table_edge(oracle_mod):
+    """The in-process form (ic_func.cpp) differs from the file form only in the
+    rounding of the t = dt links; a table shorter than the lattice's reach
+    gives |phi| = 1 and A = n/g off its end."""
+    z = load_golden("ref_boost_ic")
+    p = boost_params(z)
+    a = oracle_mod.boost_ic(p, z["profile"][0], z["profile"][1], float(z["sor_h"]), z["v"], 0)[0].reshape(5, 2, -1)
+    b = oracle_mod.boost_ic(p, z["profile"][0], z["profile"][1], float(z["sor_h"]), z["v"], 1)[0].reshape(5, 2, -1)
+    assert np.array_equal(a[:, 0], b[:, 0]) and np.array_equal(a[:2], b[:2])
+    assert np.allclose(a[2:, 1], b[2:, 1], rtol=0, atol=1e-15)
+    short = z["profile"][:, :120]        # r < 1.2
+    st, off = oracle_mod.boost_ic(p, short[0], short[1], float(z["sor_h"]), z["v"])
+    assert off > 0
+    v = st.reshape(5, 2, -1)
+    far = np.hypot(v[0, 0], v[1, 0])
+    assert np.sum(np.isclose(far, 1.0, rtol=0, atol=1e-15)) > 0
+    with pytest.raises(RuntimeError):
+        oracle_mod.boost_ic(p, short[0], short[1], 0.01, (0.0, 0.0, 0.0))

@@ -1,0 +1,154 @@
+"""Boosted straight-string initial conditions built on the GPU
+(lat_boost_ic_device) against initialConditions.cpp itself (golden fixtures
+made by running it on a profile table made by singleSemiAnalytic.cpp) and the
+oracle.
+
+Bar (FP64): each field of each time level within 1e-12 of the reference,
+relative to that field's largest value.  The t = 0 level uses the reference's
+operations and order; it can differ only where glibc's pow(x, 2) is not the
+correctly rounded x*x, and the t = dt level also in the last bits of cos/sin.
+"""
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, load_golden
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+CASES = ["ref_boost_ic", "ref_boost_ic_vz"]
+
+
+@pytest.fixture(scope="module")
+def lattice_mod():
+    from axions_gb300 import lattice
+    lattice.load_library()
+    return lattice
+
+
+def _params(z, precision=0):
+    from axions_gb300.params import make_params
+    return make_params(0, nx=int(z["nx"]), ny=int(z["ny"]), nz=int(z["nz"]), dx=float(z["dx"]), dy=float(z["dy"]),
+                       dz=float(z["dz"]), dt=float(z["dt"]), g=float(z["g"]), precision=precision)
+
+
+def _levels(lat):
+    now, past = lat.get_state()
+    return np.stack([past, now], axis=1)   # [comp][t][N], t = 0 then t = dt
+
+
+def _close(got, want, tol):
+    for c in range(want.shape[0]):
+        for t in range(want.shape[1]):
+            ref = np.max(np.abs(want[c, t]))
+            err = np.max(np.abs(got[c, t] - want[c, t]))
+            assert err <= tol * max(ref, 1e-300), f"component {c} level {t}: {err:.3e} of {ref:.3e}"
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_boost_ic_against_reference(lattice_mod, name):
+    z = load_golden(name)
+    with lattice_mod.Lattice(_params(z)) as lat:
+        off = lat.boost_ic_device(z["profile"][0], z["profile"][1], float(z["sor_h"]), z["v"])
+        assert off == 0 and lat.time_step == 0
+        _close(_levels(lat), z["ic"], TOL)
+
+
+def test_boost_ic_inprocess_form_and_fp32(lattice_mod, oracle_mod):
+    """ic_func.cpp's rounding (form 1) against the oracle; an FP32 handle holds
+    the FP64 values rounded to float."""
+    from axions_gb300.params import F32, IC_FORM_INPROCESS
+    z = load_golden("ref_boost_ic_vz")
+    p = _params(z)
+    want, _ = oracle_mod.boost_ic(p, z["profile"][0], z["profile"][1], float(z["sor_h"]), z["v"], IC_FORM_INPROCESS)
+    with lattice_mod.Lattice(p) as lat:
+        lat.boost_ic_device(z["profile"][0], z["profile"][1], float(z["sor_h"]), z["v"], IC_FORM_INPROCESS)
+        _close(_levels(lat), want.reshape(5, 2, -1), TOL)
+    with lattice_mod.Lattice(_params(z, F32)) as lat:
+        lat.boost_ic_device(z["profile"][0], z["profile"][1], float(z["sor_h"]), z["v"])
+        got = _levels(lat)
+        assert np.array_equal(got, z["ic"].astype(np.float32).astype(np.float64)) or \
+            np.max(np.abs(got - z["ic"])) <= 1e-6 * np.max(np.abs(z["ic"]))
+
+
+def test_boost_ic_off_table_count_and_values(lattice_mod, oracle_mod):
+    """A table shorter than the lattice's reach: the same count of evaluations
+    off the table as the oracle, and the same fields (|phi| = 1, A = n/g there)."""
+    z = load_golden("ref_boost_ic")
+    p = _params(z)
+    short = np.ascontiguousarray(z["profile"][:, :120])
+    want, off_want = oracle_mod.boost_ic(p, short[0], short[1], float(z["sor_h"]), z["v"])
+    assert off_want > 0
+    with lattice_mod.Lattice(p) as lat:
+        off = lat.boost_ic_device(short[0], short[1], float(z["sor_h"]), z["v"])
+        assert off == off_want
+        _close(_levels(lat), want.reshape(5, 2, -1), TOL)
+
+
+def test_boost_ic_then_evolution_tracks_oracle(lattice_mod, oracle_mod):
+    """The boosted string moves: 30 steps of the lattice from the GPU-built IC
+    against the oracle stepping the oracle-built IC (fixed walls, since the
+    single string is not periodic)."""
+    from axions_gb300.params import BC_FIXED, ENERGY_EVOLUTION
+    z = load_golden("ref_boost_ic")
+    p = _params(z)
+    p.bc = BC_FIXED
+    p.lam = 1.0
+    p.alpha = 0.0
+    p.damped_nt = 0
+    p.energy_form = ENERGY_EVOLUTION
+    st, _ = oracle_mod.boost_ic(p, z["profile"][0], z["profile"][1], float(z["sor_h"]), z["v"])
+    nt = 30
+    for n in range(nt):
+        oracle_mod.step(p, st, n)
+    with lattice_mod.Lattice(p) as lat:
+        lat.boost_ic_device(z["profile"][0], z["profile"][1], float(z["sor_h"]), z["v"])
+        lat.step(nt)
+        now, _ = lat.get_state()
+    want = st.reshape(5, 2, -1)[:, (nt + 1) % 2]
+    for c in range(5):
+        ref = np.linalg.norm(want[c])
+        if ref > 0:
+            assert np.linalg.norm(now[c] - want[c]) <= TOL * ref
+
+
+def test_boost_ic_rejects_bad_arguments(lattice_mod):
+    from axions_gb300.lattice import LatticeError
+    from axions_gb300.params import MODEL_MOORE, make_params
+    z = load_golden("ref_boost_ic")
+    prof = z["profile"]
+    with lattice_mod.Lattice(_params(z)) as lat:
+        for v in ((0.0, 0.0, 0.0), (0.8, 0.7, 0.0), (1.0, 0.0, 0.0)):
+            with pytest.raises(LatticeError):
+                lat.boost_ic_device(prof[0], prof[1], 0.01, v)
+        with pytest.raises(LatticeError):
+            lat.boost_ic_device(prof[0][:1], prof[1][:1], 0.01, (0.3, 0.0, 0.0))
+        with pytest.raises(LatticeError):
+            lat.boost_ic_device(prof[0], prof[1], 0.0, (0.3, 0.0, 0.0))
+        with pytest.raises(LatticeError):
+            lat.boost_ic_device(prof[0], prof[1], 0.01, (0.3, 0.0, 0.0), form=7)
+    with lattice_mod.Lattice(make_params(MODEL_MOORE, n=8)) as lat:
+        with pytest.raises(LatticeError):
+            lat.boost_ic_device(prof[0], prof[1], 0.01, (0.3, 0.0, 0.0))
+
+
+def test_initial_conditions_program_boost(tmp_path):
+    """bin/initialConditions ic_type=boost writes the reference's two-level
+    Data/ic.txt from out_dir/SOR_Fields.txt."""
+    z = load_golden("ref_boost_ic_vz")
+    prof = z["profile"]
+    (tmp_path / "Data").mkdir()
+    (tmp_path / "SOR_Fields.txt").write_text("".join(f"{float(a)!r} {float(b)!r}\n" for a, b in zip(prof[0], prof[1])))
+    v = z["v"]
+    args = {"ic_type": "boost", "nx": int(z["nx"]), "ny": int(z["ny"]), "nz": int(z["nz"]), "dx": 0.5, "dy": 0.5,
+            "dz": float(z["dz"]), "dt": float(z["dt"]), "g": float(z["g"]), "SORnx": prof.shape[1],
+            "SORa": float(z["sor_h"]), "v1x": repr(float(v[0])), "v1y": repr(float(v[1])), "v1z": repr(float(v[2])),
+            "digits": 17}
+    cmd = [str(ROOT / "axions_gb300" / "bin" / "initialConditions"), f"out_dir={tmp_path}"]
+    r = subprocess.run(cmd + [f"{k}={x}" for k, x in args.items()], capture_output=True, timeout=300)
+    assert r.returncode == 0, r.stderr.decode()
+    got = np.array([float(t) for t in (tmp_path / "Data" / "ic.txt").read_text().split()])
+    got = got.reshape(2, -1, 5).transpose(2, 0, 1)
+    _close(got, z["ic"], TOL)
