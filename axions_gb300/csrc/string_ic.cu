@@ -25,20 +25,26 @@ namespace lat {
 
 namespace {
 
+// the straight-string table on the device
+struct Profile {
+    const double* S0;   // |phi|
+    const double* S1;   // A_theta
+    long long m;
+    double a;           // spacing
+    double winding;
+    double g;
+};
+
 struct BoostArgs {
     int nx, ny, nz, x0, y0, z0;
     double dx, dy, dz, dt, g;
     double v1x, v1y, v1z, vsq, gamma;
-    const double* S0;   // |phi| table (device)
-    const double* S1;   // A table (device)
-    long long m;
-    double a;           // table spacing
-    double winding;
+    Profile pr;
     int form;
 };
 
 // initialConditions.cpp:756-782; off the table (or at its last point) |phi| = 1, A = n/g
-__device__ int profile_at(const BoostArgs& q, double d, double& phiMag, double& AMag)
+__device__ int profile_at(const Profile& q, double d, double& phiMag, double& AMag)
 {
     const double a = q.a;
     const long long p = (long long)round(d / a);
@@ -65,7 +71,7 @@ __device__ int string_fields(const BoostArgs& q, double xs, double ys, double& r
 {
     const double distance = sqrt(xs * xs + ys * ys);
     double phiMag, AMag;
-    const int off = profile_at(q, distance, phiMag, AMag);
+    const int off = profile_at(q.pr, distance, phiMag, AMag);
     if (xs == 0) {
         re = 0;
         Ay = 0;
@@ -248,9 +254,10 @@ extern "C" int lat_boost_ic_device(lat_handle* h, const lat_string_profile* prof
     q.v1z = b->v[2];
     q.vsq = vsq;
     q.gamma = 1 / std::sqrt(1 - vsq);
-    q.m = prof->m;
-    q.a = prof->h;
-    q.winding = prof->winding;
+    q.pr.m = prof->m;
+    q.pr.a = prof->h;
+    q.pr.winding = prof->winding;
+    q.pr.g = p.g;
     q.form = b->form;
 
     cudaError_t e = cudaSetDevice(h->device);
@@ -266,8 +273,8 @@ extern "C" int lat_boost_ic_device(lat_handle* h, const lat_string_profile* prof
     double* S1 = S0 + prof->m;
     double* At = S1 + prof->m;
     unsigned long long* off = (unsigned long long*)(At + h->N);
-    q.S0 = S0;
-    q.S1 = S1;
+    q.pr.S0 = S0;
+    q.pr.S1 = S1;
     unsigned long long off_host = 0;
     e = cudaMemcpyAsync(S0, prof->phi, tab, cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(S1, prof->A, tab, cudaMemcpyHostToDevice, h->stream);
@@ -298,6 +305,365 @@ extern "C" int lat_boost_ic_device(lat_handle* h, const lat_string_profile* prof
     h->bc_level = -1;
     h->div_valid = false;
     h->launches += 2;
+    if (off_table) *off_table = (int64_t)off_host;
+    return LAT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Loop collision (initialConditions.cpp:994-1716).  Per level three kernels:
+//   A: per site, the four boosted strings' fields, each pair's product with
+//      its imaginary part tapered to zero on the faces (magnitude kept), and
+//      the links theta = d*g*(A1 + A2); at t = 0 also the four A_t fields;
+//   B: each pair divided by the linear interpolant of its magnitude across
+//      one pair of periodic faces (pair 1 over y, pair 2 over x);
+//   C: the same over the other faces (pair 1 over z, pair 2 over y), and the
+//      product of the two pairs -> phi.
+// B and C read whole boundary planes of the previous pass, hence the
+// separate launches.  Scratch: A_t (4N), the pass outputs (2 x 4N) doubles.
+// ---------------------------------------------------------------------------
+namespace lat {
+
+namespace {
+
+struct LcBoost {
+    double v[3], vsq, gamma;
+};
+
+struct LcArgs {
+    int nx, ny, nz, x0, y0, z0;
+    double dx, dy, dz, dt, g;
+    LcBoost B[4];        // 1s, 1a, 2s, 2a
+    double sf[4][2];     // rest-frame positions
+    Profile pr;
+};
+
+// (a + i b)/d as std::complex builds it from `a + ci*b` and `/ d`
+__device__ __forceinline__ void lc_unit(double a, double b, double d, double& re, double& im)
+{
+    re = (0.0 * b + a) / d;
+    im = b / d;
+}
+
+__device__ __forceinline__ double lc_sq(double x) { return x * x; }
+
+// initialConditions.cpp:1061-1330 (t = 0) and 1430-1690 (t = dt) for one site
+__device__ int lc_site(const LcArgs& q, int t, int i, int j, int k, long long s, double* At, long long N,
+                       double P0[4], double th[3])
+{
+    const double xb = (i - q.x0) * q.dx, yb = (j - q.y0) * q.dy, zb = (k - q.z0) * q.dy;   // zb with dy
+    double pos[4][2];   // (ys1s, zs1s), (ys1a, zs1a), (xs2s, ys2s), (xs2a, ys2a)
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        const LcBoost& b = q.B[w];
+        const double c0 = w < 2 ? yb : xb, c1 = w < 2 ? zb : yb;
+        if (b.vsq == 0) {
+            pos[w][0] = c0;
+            pos[w][1] = c1;
+            continue;
+        }
+        const double dot = b.v[0] * xb + b.v[1] * yb + b.v[2] * zb;
+        // pair 1 projects on v[1], v[2]; pair 2 on v[0], v[1], except that the
+        // reference projects the anti-string's x on v[1] (:1085, :1460)
+        const int e0 = w < 2 ? 1 : (w == 3 ? 1 : 0), e1 = w < 2 ? 2 : 1;
+        pos[w][0] = c0 + (b.gamma - 1) * dot * b.v[e0] / b.vsq;
+        pos[w][1] = c1 + (b.gamma - 1) * dot * b.v[e1] / b.vsq;
+        if (t) {
+            const int f0 = w < 2 ? 1 : 0;
+            pos[w][0] -= b.gamma * b.v[f0] * q.dt;
+            pos[w][1] -= b.gamma * b.v[f0 + 1] * q.dt;
+        }
+    }
+    // offsets from each string: pair 1 (y, z), pair 2 (x, y)
+    double off0[4], off1[4], d[4], pm[4], am[4];
+    int off = 0;
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        off0[w] = pos[w][0] - q.sf[w][0];
+        off1[w] = pos[w][1] - q.sf[w][1];
+        d[w] = sqrt(lc_sq(off0[w]) + lc_sq(off1[w]));
+        off += profile_at(q.pr, d[w], pm[w], am[w]);
+    }
+    double u[4][2];
+    lc_unit(-off1[0], off0[0], d[0], u[0][0], u[0][1]);   // 1s: (-(z - z1s), y - y1s)
+    lc_unit(off1[1], off0[1], d[1], u[1][0], u[1][1]);    // 1a: (z - z1a, y - y1a)
+    lc_unit(off0[2], off1[2], d[2], u[2][0], u[2][1]);    // 2s: (x - x2s, y - y2s)
+    lc_unit(-off0[3], off1[3], d[3], u[3][0], u[3][1]);   // 2a: (-(x - x2a), y - y2a)
+    if (t) {
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            double sn, cs;
+            sincos(q.g * q.dt * At[w * N + s], &sn, &cs);
+            const double gr = -(0.0 * sn) + cs, gi = -sn;
+            const double a = u[w][0], b = u[w][1];
+            u[w][0] = a * gr - b * gi;
+            u[w][1] = a * gi + b * gr;
+        }
+    }
+    double ph[4][2], A[4][3];
+    // x-directed pair: A has y, z components
+    A[0][0] = 0;
+    if (off1[0] == 0) { ph[0][0] = 0; A[0][1] = 0; }
+    else { ph[0][0] = pm[0] * u[0][0]; A[0][1] = -am[0] * off1[0] / lc_sq(d[0]); }
+    if (off0[0] == 0) { ph[0][1] = 0; A[0][2] = 0; }
+    else { ph[0][1] = pm[0] * u[0][1]; A[0][2] = am[0] * off0[0] / lc_sq(d[0]); }
+    A[1][0] = 0;
+    if (off1[1] == 0) { ph[1][0] = 0; A[1][1] = 0; }
+    else { ph[1][0] = pm[1] * u[1][0]; A[1][1] = am[1] * off1[1] / lc_sq(d[1]); }
+    if (off0[1] == 0) { ph[1][1] = 0; A[1][2] = 0; }
+    else { ph[1][1] = pm[1] * u[1][1]; A[1][2] = -am[1] * off0[1] / lc_sq(d[1]); }
+    // z-directed pair: A has x, y components
+    A[2][2] = 0;
+    if (off0[2] == 0) { ph[2][0] = 0; A[2][1] = 0; }
+    else { ph[2][0] = pm[2] * u[2][0]; A[2][1] = am[2] * off0[2] / lc_sq(d[2]); }
+    if (off1[2] == 0) { ph[2][1] = 0; A[2][0] = 0; }
+    else { ph[2][1] = pm[2] * u[2][1]; A[2][0] = -am[2] * off1[2] / lc_sq(d[2]); }
+    A[3][2] = 0;
+    if (off0[3] == 0) { ph[3][0] = 0; A[3][1] = 0; }
+    else { ph[3][0] = pm[3] * u[3][0]; A[3][1] = -am[3] * off0[3] / lc_sq(d[3]); }
+    if (off1[3] == 0) { ph[3][1] = 0; A[3][0] = 0; }
+    else { ph[3][1] = pm[3] * u[3][1]; A[3][0] = am[3] * off1[3] / lc_sq(d[3]); }
+    // Lorentz transformation of the one-forms
+    double Ap[4][3];
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        const LcBoost& b = q.B[w];
+        const double dotA = w < 2 ? b.v[1] * A[w][1] + b.v[2] * A[w][2] : b.v[0] * A[w][0] + b.v[1] * A[w][1];
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) Ap[w][cc] = b.vsq == 0 ? A[w][cc] : A[w][cc] + (b.gamma - 1) * dotA * b.v[cc] / b.vsq;
+        if (!t) At[w * N + s] = -b.gamma * dotA;
+    }
+    if (t) {
+        // gauge shift to A_t = 0 with periodic centred differences (:1618-1640)
+        const int ip = (i + 1 + q.nx) % q.nx, im = (i - 1 + q.nx) % q.nx;
+        const int jp = (j + 1 + q.ny) % q.ny, jm = (j - 1 + q.ny) % q.ny;
+        const int kp = (k + 1 + q.nz) % q.nz, km = (k - 1 + q.nz) % q.nz;
+        const long long sxp = ((long long)ip * q.ny + j) * q.nz + k, sxm = ((long long)im * q.ny + j) * q.nz + k;
+        const long long syp = ((long long)i * q.ny + jp) * q.nz + k, sym = ((long long)i * q.ny + jm) * q.nz + k;
+        const long long szp = ((long long)i * q.ny + j) * q.nz + kp, szm = ((long long)i * q.ny + j) * q.nz + km;
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            const double* a = At + w * N;
+            Ap[w][0] += -q.dt * (a[sxp] - a[sxm]) / (2 * q.dx);
+            Ap[w][1] += -q.dt * (a[syp] - a[sym]) / (2 * q.dy);
+            Ap[w][2] += -q.dt * (a[szp] - a[szm]) / (2 * q.dz);
+        }
+    }
+    double Asum[2][3];
+#pragma unroll
+    for (int pair = 0; pair < 2; ++pair) {
+        const double* a = ph[2 * pair];
+        const double* b = ph[2 * pair + 1];
+        double p0 = a[0] * b[0] - a[1] * b[1];
+        double p1 = a[1] * b[0] + a[0] * b[1];
+        const double pf = pair == 0 ? (1 - lc_sq(yb / (q.y0 * q.dy))) * (1 - lc_sq(zb / (q.z0 * q.dz)))
+                                    : (1 - lc_sq(xb / (q.x0 * q.dx))) * (1 - lc_sq(yb / (q.y0 * q.dy)));
+        if (lc_sq(p0) + lc_sq(p1 * pf) == 0) {
+            p0 = p1;
+            p1 = 0;
+        } else {
+            const double nf = sqrt((lc_sq(p0) + lc_sq(p1)) / (lc_sq(p0) + lc_sq(p1 * pf)));
+            p0 = nf * p0;
+            p1 = nf * pf * p1;
+        }
+        P0[2 * pair] = p0;
+        P0[2 * pair + 1] = p1;
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) Asum[pair][cc] = (Ap[2 * pair][cc] + Ap[2 * pair + 1][cc]) * pf;
+    }
+    th[0] = q.dx * q.g * (Asum[0][0] + Asum[1][0]);
+    th[1] = q.dy * q.g * (Asum[0][1] + Asum[1][1]);
+    th[2] = q.dz * q.g * (Asum[0][2] + Asum[1][2]);
+    return off;
+}
+
+template <class T>
+__global__ void lc_pass_a(LcArgs q, int t, long long N, double* At, double* P0, T* th0, T* th1, T* th2,
+                          unsigned long long* off)
+{
+    for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < N; s += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(s % q.nz);
+        const long long r = s / q.nz;
+        const int j = (int)(r % q.ny), i = (int)(r / q.ny);
+        double v4[4], th[3];
+        if (lc_site(q, t, i, j, k, s, At, N, v4, th)) atomicAdd(off, 1ull);
+#pragma unroll
+        for (int w = 0; w < 4; ++w) P0[w * N + s] = v4[w];
+        th0[s] = (T)th[0];
+        th1[s] = (T)th[1];
+        th2[s] = (T)th[2];
+    }
+}
+
+__device__ __forceinline__ double lc_mag(const double* re, const double* im, long long s)
+{
+    return sqrt(lc_sq(re[s]) + lc_sq(im[s]));
+}
+
+// initialConditions.cpp:1336-1372 (pass B) and 1376-1414 (pass C, which also
+// multiplies the pairs)
+template <class T, bool LAST>
+__global__ void lc_pass_bc(LcArgs q, long long N, const double* __restrict__ Pin, double* Pout, T* phr, T* phi)
+{
+    const double *r1 = Pin, *i1 = Pin + N, *r2 = Pin + 2 * N, *i2 = Pin + 3 * N;
+    for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < N; s += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(s % q.nz);
+        const long long r = s / q.nz;
+        const int j = (int)(r % q.ny), i = (int)(r / q.ny);
+        const long long row = ((long long)i * q.ny + j) * q.nz;
+        const double xb = (i - q.x0) * q.dx, yb = (j - q.y0) * q.dy, zb = (k - q.z0) * q.dz;
+        double m1t, m1b, m2t, m2b, w1, w2;
+        if (!LAST) {
+            // pair 1 across y, pair 2 across x
+            m1t = lc_mag(r1, i1, ((long long)i * q.ny + (q.ny - 1)) * q.nz + k);
+            m1b = lc_mag(r1, i1, ((long long)i * q.ny) * q.nz + k);
+            m2t = lc_mag(r2, i2, ((long long)(q.nx - 1) * q.ny + j) * q.nz + k);
+            m2b = lc_mag(r2, i2, ((long long)j) * q.nz + k);
+            w1 = (m1t - m1b) * (yb + q.y0 * q.dy) / (2 * q.y0 * q.dy) + m1b;
+            w2 = (m2t - m2b) * (xb + q.x0 * q.dx) / (2 * q.x0 * q.dx) + m2b;
+        } else {
+            // pair 1 across z, pair 2 across y
+            m1t = lc_mag(r1, i1, row + (q.nz - 1));
+            m1b = lc_mag(r1, i1, row);
+            m2t = lc_mag(r2, i2, ((long long)i * q.ny + (q.ny - 1)) * q.nz + k);
+            m2b = lc_mag(r2, i2, ((long long)i * q.ny) * q.nz + k);
+            w1 = (m1t - m1b) * (zb + q.z0 * q.dz) / (2 * q.z0 * q.dz) + m1b;
+            w2 = (m2t - m2b) * (yb + q.y0 * q.dy) / (2 * q.y0 * q.dy) + m2b;
+        }
+        const double a0 = r1[s] / w1, a1 = i1[s] / w1, b0 = r2[s] / w2, b1 = i2[s] / w2;
+        if (!LAST) {
+            Pout[s] = a0;
+            Pout[N + s] = a1;
+            Pout[2 * N + s] = b0;
+            Pout[3 * N + s] = b1;
+        } else {
+            phr[s] = (T)(a0 * b0 - a1 * b1);
+            phi[s] = (T)(a0 * b1 + a1 * b0);
+        }
+    }
+}
+
+template <class T>
+cudaError_t lc_launch(lat_handle* h, const LcArgs& q, double* At, double* P0, double* P1, unsigned long long* off)
+{
+    const int threads = 128;
+    long long blocks = ((long long)h->N + threads - 1) / threads;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    const long long N = h->N;
+    for (int t = 0; t < 2; ++t) {
+        T* sl[5];
+        for (int c = 0; c < 5; ++c) sl[c] = (T*)h->slot(c, t);
+        lc_pass_a<T><<<(unsigned)blocks, threads, 0, h->stream>>>(q, t, N, At, P0, sl[2], sl[3], sl[4], off);
+        lc_pass_bc<T, false><<<(unsigned)blocks, threads, 0, h->stream>>>(q, N, P0, P1, nullptr, nullptr);
+        lc_pass_bc<T, true><<<(unsigned)blocks, threads, 0, h->stream>>>(q, N, P1, nullptr, sl[0], sl[1]);
+    }
+    return cudaGetLastError();
+}
+
+void lc_boost_init(LcBoost& b, const double v[3])
+{
+    b.v[0] = v[0];
+    b.v[1] = v[1];
+    b.v[2] = v[2];
+    b.vsq = std::pow(v[0], 2) + std::pow(v[1], 2) + std::pow(v[2], 2);
+    b.gamma = 1 / std::sqrt(1 - b.vsq);
+}
+
+}  // namespace
+
+}  // namespace lat
+
+extern "C" int lat_loop_collision_ic_device(lat_handle* h, const lat_string_profile* prof,
+                                            const lat_loop_collision_ic* c, int64_t* off_table)
+{
+    if (!h || !prof || !c || !prof->phi || !prof->A) {
+        set_error("lat_loop_collision_ic_device: null argument");
+        return LAT_ERR_INVALID;
+    }
+    const lat_params& p = h->p;
+    if (p.model != LAT_MODEL_AH) {
+        set_error("lat_loop_collision_ic_device: Abelian-Higgs handles only");
+        return LAT_ERR_INVALID;
+    }
+    if (p.nx < 3 || p.ny < 3 || p.nz < 3) {
+        set_error("lat_loop_collision_ic_device: every side must be at least 3");
+        return LAT_ERR_INVALID;
+    }
+    if (prof->m < 2 || !(prof->h > 0)) {
+        set_error("lat_loop_collision_ic_device: the profile needs m >= 2 points and h > 0");
+        return LAT_ERR_INVALID;
+    }
+    LcArgs q;
+    q.nx = (int)p.nx;
+    q.ny = (int)p.ny;
+    q.nz = (int)p.nz;
+    q.x0 = (q.nx - 1) / 2;
+    q.y0 = (q.ny - 1) / 2;
+    q.z0 = (q.nz - 1) / 2;
+    q.dx = p.dx;
+    q.dy = p.dy;
+    q.dz = p.dz;
+    q.dt = p.dt;
+    q.g = p.g;
+    const double* vel[4] = {c->v1s, c->v1a, c->v2s, c->v2a};
+    const double* pos[4] = {c->pos1s, c->pos1a, c->pos2s, c->pos2a};
+    for (int w = 0; w < 4; ++w) {
+        lc_boost_init(q.B[w], vel[w]);
+        if (!(q.B[w].vsq < 1)) {
+            set_error("lat_loop_collision_ic_device: every |v| must be below 1");
+            return LAT_ERR_INVALID;
+        }
+        // rest-frame positions (initialConditions.cpp:1030-1046), on the host with
+        // the reference's operations
+        const LcBoost& b = q.B[w];
+        if (b.vsq == 0) {
+            q.sf[w][0] = pos[w][0];
+            q.sf[w][1] = pos[w][1];
+        } else {
+            const int e = w < 2 ? 1 : 0;
+            const double dot = b.v[e] * pos[w][0] + b.v[e + 1] * pos[w][1];
+            q.sf[w][0] = pos[w][0] + (b.gamma - 1) * dot * b.v[e] / b.vsq;
+            q.sf[w][1] = pos[w][1] + (b.gamma - 1) * dot * b.v[e + 1] / b.vsq;
+        }
+    }
+    q.pr.m = prof->m;
+    q.pr.a = prof->h;
+    q.pr.winding = prof->winding;
+    q.pr.g = p.g;
+
+    cudaError_t e = cudaSetDevice(h->device);
+    const size_t tab = sizeof(double) * (size_t)prof->m;
+    const size_t need = 2 * tab + sizeof(double) * 12 * (size_t)h->N + 64;
+    char* scratch = nullptr;
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&scratch, need, h->stream);
+    if (e != cudaSuccess) {
+        set_error(std::string("lat_loop_collision_ic_device: ") + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? LAT_ERR_NOMEM : LAT_ERR_CUDA;
+    }
+    double* S0 = (double*)scratch;
+    double* S1 = S0 + prof->m;
+    double* At = S1 + prof->m;
+    double* P0 = At + 4 * h->N;
+    double* P1 = P0 + 4 * h->N;
+    unsigned long long* off = (unsigned long long*)(P1 + 4 * h->N);
+    q.pr.S0 = S0;
+    q.pr.S1 = S1;
+    unsigned long long off_host = 0;
+    e = cudaMemcpyAsync(S0, prof->phi, tab, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(S1, prof->A, tab, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(off, 0, sizeof(unsigned long long), h->stream);
+    if (e == cudaSuccess) e = h->elem == 8 ? lc_launch<double>(h, q, At, P0, P1, off) : lc_launch<float>(h, q, At, P0, P1, off);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&off_host, off, sizeof(off_host), cudaMemcpyDeviceToHost, h->stream);
+    const cudaError_t ef = cudaFreeAsync(scratch, h->stream);
+    if (e == cudaSuccess) e = ef;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+        set_error(std::string("lat_loop_collision_ic_device: ") + cudaGetErrorString(e));
+        return LAT_ERR_CUDA;
+    }
+    h->n = 0;
+    h->bc_level = -1;
+    h->div_valid = false;
+    h->launches += 6;
     if (off_table) *off_table = (int64_t)off_host;
     return LAT_OK;
 }

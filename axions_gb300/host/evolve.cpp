@@ -176,10 +176,18 @@ Params::Params(Program prog)
         v["stringPos"] = "false";
         v["stringDetect"] = "true";
         v["splitLength"] = "true";
-        // ic_func.cpp: "random" is the in-process generator provided here (the
-        // reference's default, "loop collision", needs its SOR string profiles)
+        // ic_func.cpp: "random" and "boost" are built in-process here; its
+        // default, "loop collision", is an older variant of
+        // initialConditions.cpp's, whose Data/ic.txt "data" reads
         v["ic_type"] = "random";
         v["seed"] = "1";
+        v["sor_file"] = "SOR_Fields.txt";   // ic_func.cpp:38-39,692 (next to the program)
+        v["SORnx"] = "30001";
+        v["SORa"] = "0.01";
+        v["n"] = "1";
+        v["v1x"] = "0.24";                  // ic_func.cpp:62-64
+        v["v1y"] = "0.5499090833947008";
+        v["v1z"] = "0";
         break;
     case Program::InitialConditions:
         // initialConditions.cpp:22-60 ("random" is the family provided here;
@@ -195,16 +203,21 @@ Params::Params(Program prog)
         v["ic_in"] = "";     // convert: the table to read (under Data/)
         v["cols"] = "5";     // convert: columns of the table
         v["levels"] = "1";   // convert: rows = levels * nx * ny * nz
-        // boost (initialConditions.cpp:41-44,62-68): the straight-string table
-        // (singleSemiAnalytic's output, read from out_dir/sor_file) and the
-        // boost velocity 0.6*(0.4, sqrt(1 - 0.4^2), 0)
-        v["sor_file"] = "SOR_Fields.txt";
+        // boost and loop collision (initialConditions.cpp:41-44,62-84): the
+        // straight-string table (singleSemiAnalytic's output; the reference
+        // reads it from its own directory for boost, from Data/ for loop
+        // collision; sor_file, relative to out_dir, overrides), the boost
+        // velocity 0.6*(0.4, sqrt(1 - 0.4^2), 0), and the loop-collision
+        // strings ("a,b" positions, "a,b,c" velocities; empty: the reference's
+        // placement for the lattice)
+        v["sor_file"] = "";
         v["SORnx"] = "20001";
         v["SORa"] = "0.01";
         v["n"] = "1";
         v["v1x"] = "0.24";
         v["v1y"] = "0.5499090833947008";
         v["v1z"] = "0";
+        for (const char* k : {"pos1s", "pos1a", "pos2s", "pos2a", "v1s", "v1a", "v2s", "v2a"}) v[k] = "";
         break;
     case Program::SingleSemiAnalytic:
         // singleSemiAnalytic.cpp:19-33; ic_type 0 starts from eta*tanh(r/2),
@@ -710,6 +723,9 @@ void icfunc_random(const Run& r, double seed, std::vector<double>& now)
     }
 }
 
+enum class StringIc { Boost, LoopCollision };
+void string_ic_table(Params& q, const std::string& dir, StringIc kind, int form, std::vector<double>& tab);
+
 int run_icw(Run& r)
 {
     // ic_w_evolution.cpp:52-1190
@@ -719,12 +735,29 @@ int run_icw(Run& r)
     const bool split = q.flag("splitLength");
     struct timeval start, end;
     gettimeofday(&start, nullptr);
-    if (q.str("ic_type") != "random")
-        fail("ic_type: only the \"random\" initial conditions of ic_func.cpp are provided by this program");
-    std::vector<double> now;
-    icfunc_random(r, q.num("seed"), now);
+    // ic_func.cpp "random" and "boost" in-process; "data" reads the two levels
+    // of Data/<ic_file> (e.g. initialConditions' loop collision)
+    const std::string ic_type = q.str("ic_type");
+    std::vector<double> now, past;
+    if (ic_type == "random") {
+        icfunc_random(r, q.num("seed"), now);
+        past = now;
+    } else if (ic_type == "boost") {
+        std::vector<double> tab;
+        string_ic_table(q, q.str("out_dir"), StringIc::Boost, LAT_IC_FORM_INPROCESS, tab);
+        past.assign((size_t)5 * r.N, 0.0);
+        now.assign((size_t)5 * r.N, 0.0);
+        for (int c = 0; c < 5; ++c) {
+            std::copy(tab.begin() + (size_t)c * 2 * r.N, tab.begin() + (size_t)c * 2 * r.N + r.N, past.begin() + (size_t)c * r.N);
+            std::copy(tab.begin() + (size_t)c * 2 * r.N + r.N, tab.begin() + (size_t)(c + 1) * 2 * r.N, now.begin() + (size_t)c * r.N);
+        }
+    } else if (ic_type == "data") {
+        r.read_ic(r.data(q.str("ic_file")), 5, 2, past, now);
+    } else {
+        fail("ic_type: this program provides ic_func.cpp's \"random\" and \"boost\", and \"data\"");
+    }
     check(lat_create(&r.p, &r.h), "lat_create");
-    check(lat_set_state(r.h, now.data(), now.data(), 0), "lat_set_state");
+    check(lat_set_state(r.h, now.data(), past.data(), 0), "lat_set_state");
     AsyncFrames frames(r.h, 1, r.N, r.digits);
     std::ofstream valsPerLoop = r.open_out(r.data("valsPerLoop_test.txt"));  // input = "test" (:67)
     long long counter = 0, gifFrame = 0;
@@ -762,19 +795,34 @@ bool ends_with(const std::string& s, const std::string& suffix)
     return s.size() >= suffix.size() && s.compare(s.size() - suffix.size(), suffix.size(), suffix) == 0;
 }
 
-// initialConditions.cpp:670-708 ("random"): per site in linear order phi_re,
-// phi_im from normal_distribution<double>(mean, stdev) over
-// default_random_engine(seed); the link columns are dmu*g*A with A = 0.
-// Written as Data/<ic_file>: text (the reference's format and precision) or,
-// for a name ending in .bin, the binary form.  ic_type = convert reads
-// Data/<ic_in> (text or binary) and writes it as Data/<ic_file>.
-// The boosted-string IC (both levels) built on the GPU from the straight-string
-// table at out_dir/sor_file: column-major [5][2N], level 0 (t = 0) rows first.
-void boost_ic_table(Params& q, const std::string& dir, int form, std::vector<double>& tab)
+// "a,b,c" (commas or spaces) -> exactly n numbers
+std::vector<double> numbers(const std::string& key, const std::string& text, size_t n)
+{
+    std::vector<double> out;
+    std::string t = text;
+    for (char& ch : t)
+        if (ch == ',') ch = ' ';
+    std::istringstream in(t);
+    std::string tok;
+    while (in >> tok) {
+        char* end = nullptr;
+        const double v = std::strtod(tok.c_str(), &end);
+        if (!end || *end) fail("bad number in " + key + ": " + tok);
+        out.push_back(v);
+    }
+    if (out.size() != n) fail(key + " needs " + std::to_string(n) + " numbers");
+    return out;
+}
+
+// A string-profile IC (both levels) built on the GPU from the straight-string
+// table: column-major [5][2N], level 0 (t = 0) rows first.
+void string_ic_table(Params& q, const std::string& dir, StringIc kind, int form, std::vector<double>& tab)
 {
     const int64_t m = q.integer("SORnx");
     std::vector<double> prof;
-    read_table(dir + "/" + q.str("sor_file"), 2, m, prof);
+    std::string file = q.str("sor_file");
+    if (file.empty()) file = kind == StringIc::Boost ? "SOR_Fields.txt" : "Data/SOR_Fields.txt";
+    read_table(dir + "/" + file, 2, m, prof);
     lat_params p;
     check(lat_params_init(&p, LAT_MODEL_AH), "lat_params_init");
     p.nx = q.integer("nx");
@@ -794,17 +842,35 @@ void boost_ic_table(Params& q, const std::string& dir, int form, std::vector<dou
     sp.m = m;
     sp.h = q.num("SORa");
     sp.winding = q.num("n");
-    lat_boost_ic b;
-    b.v[0] = q.num("v1x");
-    b.v[1] = q.num("v1y");
-    b.v[2] = q.num("v1z");
-    b.form = form;
-    b.reserved = 0;
     int64_t off = 0;
-    const int rc = lat_boost_ic_device(h, &sp, &b, &off);
+    int rc;
+    if (kind == StringIc::Boost) {
+        lat_boost_ic b;
+        b.v[0] = q.num("v1x");
+        b.v[1] = q.num("v1y");
+        b.v[2] = q.num("v1z");
+        b.form = form;
+        b.reserved = 0;
+        rc = lat_boost_ic_device(h, &sp, &b, &off);
+    } else {
+        // initialConditions.cpp:72-84
+        const double Ly = (double)(p.ny - 1), Lz = (double)(p.nz - 1), Lx = (double)(p.nx - 1);
+        const std::vector<std::pair<const char*, std::vector<double>>> def = {
+            {"pos1s", {0.15 * Ly * p.dy, -0.25 * Lz * p.dz}}, {"pos1a", {-0.15 * Ly * p.dy, 0.25 * Lz * p.dz}},
+            {"pos2s", {0.25 * Lx * p.dx, 0}},                {"pos2a", {-0.25 * Lx * p.dx, 0}},
+            {"v1s", {0, -0.75, 0}}, {"v1a", {0, 0.75, 0}}, {"v2s", {0, 0, 0}}, {"v2a", {0, 0, 0}}};
+        lat_loop_collision_ic c;
+        double* dst[8] = {c.pos1s, c.pos1a, c.pos2s, c.pos2a, c.v1s, c.v1a, c.v2s, c.v2a};
+        for (int w = 0; w < 8; ++w) {
+            const std::string& txt = q.str(def[w].first);
+            const std::vector<double> v = txt.empty() ? def[w].second : numbers(def[w].first, txt, def[w].second.size());
+            for (size_t e = 0; e < v.size(); ++e) dst[w][e] = v[e];
+        }
+        rc = lat_loop_collision_ic_device(h, &sp, &c, &off);
+    }
     if (rc != LAT_OK) {
         lat_destroy(h);
-        check(rc, "lat_boost_ic_device");
+        check(rc, kind == StringIc::Boost ? "lat_boost_ic_device" : "lat_loop_collision_ic_device");
     }
     const int64_t N = p.nx * p.ny * p.nz;
     std::vector<double> now((size_t)5 * N), past((size_t)5 * N);
@@ -818,6 +884,12 @@ void boost_ic_table(Params& q, const std::string& dir, int form, std::vector<dou
     }
 }
 
+// initialConditions.cpp:670-708 ("random"): per site in linear order phi_re,
+// phi_im from normal_distribution<double>(mean, stdev) over
+// default_random_engine(seed); the link columns are dmu*g*A with A = 0.
+// Written as Data/<ic_file>: text (the reference's format and precision) or,
+// for a name ending in .bin, the binary form.  ic_type = convert reads
+// Data/<ic_in> (text or binary) and writes it as Data/<ic_file>.
 int run_initial_conditions(Params& q)
 {
     struct timeval start, end;
@@ -843,8 +915,8 @@ int run_initial_conditions(Params& q)
             tab[3 * N + s] = q.num("dy") * g * A;
             tab[4 * N + s] = q.num("dz") * g * A;
         }
-    } else if (type == "boost") {
-        boost_ic_table(q, dir, LAT_IC_FORM_FILE, tab);
+    } else if (type == "boost" || type == "loop collision") {
+        string_ic_table(q, dir, type == "boost" ? StringIc::Boost : StringIc::LoopCollision, LAT_IC_FORM_FILE, tab);
         rows = 2 * N;
     } else if (type == "convert") {
         cols = (int)q.integer("cols");
@@ -852,7 +924,7 @@ int run_initial_conditions(Params& q)
         if (q.str("ic_in").empty()) fail("ic_type = convert needs ic_in");
         read_table(dir + "/Data/" + q.str("ic_in"), cols, rows, tab);
     } else {
-        fail("ic_type: this program provides \"random\", \"boost\" and \"convert\"");
+        fail("ic_type: this program provides \"random\", \"boost\", \"loop collision\" and \"convert\"");
     }
     if (ends_with(out, ".bin")) write_table_bin(out, cols, rows, tab.data());
     else write_table_text(out, cols, rows, tab.data(), digits);

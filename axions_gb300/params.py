@@ -189,3 +189,33 @@ def boost_ic(v, form: int = IC_FORM_FILE) -> LatBoostIC:
         b.v[q] = float(v[q])
     b.form = int(form)
     return b
+
+
+class LatLoopCollisionIC(ctypes.Structure):
+    _fields_ = [("pos1s", ctypes.c_double * 2), ("pos1a", ctypes.c_double * 2), ("pos2s", ctypes.c_double * 2),
+                ("pos2a", ctypes.c_double * 2), ("v1s", ctypes.c_double * 3), ("v1a", ctypes.c_double * 3),
+                ("v2s", ctypes.c_double * 3), ("v2a", ctypes.c_double * 3)]
+
+
+LOOP_COLLISION_KEYS = ("pos1s", "pos1a", "pos2s", "pos2a", "v1s", "v1a", "v2s", "v2a")
+
+
+def loop_collision_ic(**geo) -> LatLoopCollisionIC:
+    """LatLoopCollisionIC from keyword arrays (all eight keys required)."""
+    c = LatLoopCollisionIC()
+    for k in LOOP_COLLISION_KEYS:
+        dst = getattr(c, k)
+        src = geo[k]
+        if len(src) != len(dst):
+            raise ValueError(f"{k} needs {len(dst)} values")
+        for q in range(len(dst)):
+            dst[q] = float(src[q])
+    return c
+
+
+def default_loop_collision(nx: int, ny: int, nz: int, dx: float, dy: float, dz: float) -> dict:
+    """initialConditions.cpp:72-84: pair 1 at y = +-0.15 L_y, z = -+0.25 L_z moving
+    along y at -+0.75; pair 2 at x = +-0.25 L_x at rest."""
+    return dict(pos1s=[0.15 * (ny - 1) * dy, -0.25 * (nz - 1) * dz], pos1a=[-0.15 * (ny - 1) * dy, 0.25 * (nz - 1) * dz],
+                pos2s=[0.25 * (nx - 1) * dx, 0.0], pos2a=[-0.25 * (nx - 1) * dx, 0.0],
+                v1s=[0.0, -0.75, 0.0], v1a=[0.0, 0.75, 0.0], v2s=[0.0, 0.0, 0.0], v2a=[0.0, 0.0, 0.0])

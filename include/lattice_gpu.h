@@ -339,6 +339,28 @@ typedef struct lat_boost_ic {
  * be null) receives the number of site evaluations beyond the profile table.
  * Abelian-Higgs handles only. */
 int lat_boost_ic_device(lat_handle* h, const lat_string_profile* prof, const lat_boost_ic* b, int64_t* off_table);
+
+/* Two string/anti-string pairs set up to collide and form loops
+ * (initialConditions.cpp:994-1716, ic_type "loop collision"): an x-directed
+ * pair at (y, z) = pos1s, pos1a moving with v1s, v1a and a z-directed pair at
+ * (x, y) = pos2s, pos2a moving with v2s, v2a (|v| < 1; 0 leaves a string at
+ * rest).  Each pair's product field has its imaginary part tapered to zero on
+ * the faces (magnitude kept), is divided by linear interpolants of its
+ * magnitude across the periodic faces (two passes), and the two pairs are
+ * multiplied.  Both levels: t = 0 into the past slot, t = dt (boosted
+ * positions, gauge rotation of phi and the periodic centred gauge shift of A)
+ * into the current slot; time step 0.  Sides >= 3.  The reference reads four
+ * uninitialised link components at t = dt (A1s[0], A1a[0], A2s[2], A2a[2]
+ * are only set in the t = 0 loop's private copies); here they are 0, their
+ * t = 0 value.  Abelian-Higgs handles only. */
+typedef struct lat_loop_collision_ic {
+    double pos1s[2], pos1a[2];   /* (y, z) of the x-directed string, anti-string */
+    double pos2s[2], pos2a[2];   /* (x, y) of the z-directed string, anti-string */
+    double v1s[3], v1a[3], v2s[3], v2a[3];
+} lat_loop_collision_ic;
+
+int lat_loop_collision_ic_device(lat_handle* h, const lat_string_profile* prof, const lat_loop_collision_ic* c,
+                                 int64_t* off_table);
 /* The generator on the host (checks, reproduction of device ICs). */
 int lat_philox4x32_10(const uint32_t counter[4], const uint32_t key[2], uint32_t out[4]);
 

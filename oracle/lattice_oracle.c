@@ -1268,3 +1268,263 @@ int64_t orc_boost_ic(const lat_params* p, const lat_string_profile* prof, const 
     free(At);
     return off;
 }
+
+/* ---------------------------------------------------------------------------
+ * Loop-collision IC, initialConditions.cpp:994-1716, restated with the
+ * reference's operation order: pow(x, 2), std::complex<double> arithmetic
+ * written out as libstdc++ performs it for finite values (double + complex
+ * adds to the real part only, complex * complex = (ac - bd, ad + bc)).
+ * ------------------------------------------------------------------------- */
+
+typedef struct { double v[3]; double vsq, gamma; } lc_boost;
+
+static void lc_boost_init(lc_boost* b, const double v[3])
+{
+    b->v[0] = v[0];
+    b->v[1] = v[1];
+    b->v[2] = v[2];
+    b->vsq = pow(v[0], 2) + pow(v[1], 2) + pow(v[2], 2);
+    b->gamma = 1 / sqrt(1 - b->vsq);
+}
+
+/* (a + i b)/d as std::complex builds it from `a + ci*b` and `/ d` */
+static void lc_unit(double a, double b, double d, double* re, double* im)
+{
+    *re = (0.0 * b + a) / d;
+    *im = b / d;
+}
+
+/* the per-site work of one level (initialConditions.cpp:1061-1330 at t = 0,
+ * 1430-1690 at t = dt); At is written at t = 0 and read at t = dt */
+static int lc_site(const lat_params* p, const lat_string_profile* prof, const lat_loop_collision_ic* c,
+                   const lc_boost B[4], const double sf[4][2], int t, int i, int j, int k, double* At[4],
+                   double P0[4], double th[3])
+{
+    const int nx = p->nx, ny = p->ny, nz = p->nz;
+    const int x0 = (nx - 1) / 2, y0 = (ny - 1) / 2, z0 = (nz - 1) / 2;
+    const double dx = p->dx, dy = p->dy, dz = p->dz, dt = p->dt, g = p->g;
+    const int64_t s = ((int64_t)i * ny + j) * nz + k;
+    const double xb = (i - x0) * dx, yb = (j - y0) * dy, zb = (k - z0) * dy;   /* zb with dy: :1067,:1442 */
+    const lc_boost *b1s = &B[0], *b1a = &B[1], *b2s = &B[2], *b2a = &B[3];
+    double ys1s, zs1s, ys1a, zs1a, xs2s, ys2s, xs2a, ys2a;
+#define DOT(b) ((b)->v[0] * xb + (b)->v[1] * yb + (b)->v[2] * zb)
+    if (b1s->vsq == 0) { ys1s = yb; zs1s = zb; }
+    else {
+        ys1s = yb + (b1s->gamma - 1) * DOT(b1s) * b1s->v[1] / b1s->vsq;
+        zs1s = zb + (b1s->gamma - 1) * DOT(b1s) * b1s->v[2] / b1s->vsq;
+        if (t) { ys1s -= b1s->gamma * b1s->v[1] * dt; zs1s -= b1s->gamma * b1s->v[2] * dt; }
+    }
+    if (b1a->vsq == 0) { ys1a = yb; zs1a = zb; }
+    else {
+        ys1a = yb + (b1a->gamma - 1) * DOT(b1a) * b1a->v[1] / b1a->vsq;
+        zs1a = zb + (b1a->gamma - 1) * DOT(b1a) * b1a->v[2] / b1a->vsq;
+        if (t) { ys1a -= b1a->gamma * b1a->v[1] * dt; zs1a -= b1a->gamma * b1a->v[2] * dt; }
+    }
+    if (b2s->vsq == 0) { xs2s = xb; ys2s = yb; }
+    else {
+        xs2s = xb + (b2s->gamma - 1) * DOT(b2s) * b2s->v[0] / b2s->vsq;
+        ys2s = yb + (b2s->gamma - 1) * DOT(b2s) * b2s->v[1] / b2s->vsq;
+        if (t) { xs2s -= b2s->gamma * b2s->v[0] * dt; ys2s -= b2s->gamma * b2s->v[1] * dt; }
+    }
+    if (b2a->vsq == 0) { xs2a = xb; ys2a = yb; }
+    else {
+        /* the reference projects xs2a on v2a[1] (:1085, :1460) */
+        xs2a = xb + (b2a->gamma - 1) * DOT(b2a) * b2a->v[1] / b2a->vsq;
+        ys2a = yb + (b2a->gamma - 1) * DOT(b2a) * b2a->v[1] / b2a->vsq;
+        if (t) { xs2a -= b2a->gamma * b2a->v[0] * dt; ys2a -= b2a->gamma * b2a->v[1] * dt; }
+    }
+#undef DOT
+    /* x - y style subtraction is written `a - b; a -= c` above: the reference
+     * computes (xb + boost) - gamma*v*dt, the same two roundings */
+    double d[4], pm[4], am[4];
+    d[0] = sqrt(pow(ys1s - sf[0][0], 2) + pow(zs1s - sf[0][1], 2));
+    d[1] = sqrt(pow(ys1a - sf[1][0], 2) + pow(zs1a - sf[1][1], 2));
+    d[2] = sqrt(pow(xs2s - sf[2][0], 2) + pow(ys2s - sf[2][1], 2));
+    d[3] = sqrt(pow(xs2a - sf[3][0], 2) + pow(ys2a - sf[3][1], 2));
+    int off = 0;
+    for (int q = 0; q < 4; ++q) off += profile_at(prof, g, d[q], &pm[q], &am[q]);
+    double u[4][2];
+    lc_unit(-(zs1s - sf[0][1]), ys1s - sf[0][0], d[0], &u[0][0], &u[0][1]);
+    lc_unit(zs1a - sf[1][1], ys1a - sf[1][0], d[1], &u[1][0], &u[1][1]);
+    lc_unit(xs2s - sf[2][0], ys2s - sf[2][1], d[2], &u[2][0], &u[2][1]);
+    lc_unit(-(xs2a - sf[3][0]), ys2a - sf[3][1], d[3], &u[3][0], &u[3][1]);
+    if (t) {
+        /* phi -> phi e^{-i g dt At(t=0)}: gRot = cos - ci*sin, then cUnit*gRot */
+        for (int q = 0; q < 4; ++q) {
+            const double x = g * dt * At[q][s];
+            const double sn = sin(x), cs = cos(x);
+            const double gr = -(0.0 * sn) + cs, gi = -sn;
+            const double a = u[q][0], bq = u[q][1];
+            u[q][0] = a * gr - bq * gi;
+            u[q][1] = a * gi + bq * gr;
+        }
+    }
+    double ph[4][2], A[4][3];
+    /* x-directed string (y, z components of A); A1s[0] = A1a[0] = 0 */
+    A[0][0] = 0;
+    if (zs1s - sf[0][1] == 0) { ph[0][0] = 0; A[0][1] = 0; }
+    else { ph[0][0] = pm[0] * u[0][0]; A[0][1] = -am[0] * (zs1s - sf[0][1]) / pow(d[0], 2); }
+    if (ys1s - sf[0][0] == 0) { ph[0][1] = 0; A[0][2] = 0; }
+    else { ph[0][1] = pm[0] * u[0][1]; A[0][2] = am[0] * (ys1s - sf[0][0]) / pow(d[0], 2); }
+    A[1][0] = 0;
+    if (zs1a - sf[1][1] == 0) { ph[1][0] = 0; A[1][1] = 0; }
+    else { ph[1][0] = pm[1] * u[1][0]; A[1][1] = am[1] * (zs1a - sf[1][1]) / pow(d[1], 2); }
+    if (ys1a - sf[1][0] == 0) { ph[1][1] = 0; A[1][2] = 0; }
+    else { ph[1][1] = pm[1] * u[1][1]; A[1][2] = -am[1] * (ys1a - sf[1][0]) / pow(d[1], 2); }
+    /* z-directed string (x, y components); A2s[2] = A2a[2] = 0 */
+    A[2][2] = 0;
+    if (xs2s - sf[2][0] == 0) { ph[2][0] = 0; A[2][1] = 0; }
+    else { ph[2][0] = pm[2] * u[2][0]; A[2][1] = am[2] * (xs2s - sf[2][0]) / pow(d[2], 2); }
+    if (ys2s - sf[2][1] == 0) { ph[2][1] = 0; A[2][0] = 0; }
+    else { ph[2][1] = pm[2] * u[2][1]; A[2][0] = -am[2] * (ys2s - sf[2][1]) / pow(d[2], 2); }
+    A[3][2] = 0;
+    if (xs2a - sf[3][0] == 0) { ph[3][0] = 0; A[3][1] = 0; }
+    else { ph[3][0] = pm[3] * u[3][0]; A[3][1] = -am[3] * (xs2a - sf[3][0]) / pow(d[3], 2); }
+    if (ys2a - sf[3][1] == 0) { ph[3][1] = 0; A[3][0] = 0; }
+    else { ph[3][1] = pm[3] * u[3][1]; A[3][0] = am[3] * (ys2a - sf[3][1]) / pow(d[3], 2); }
+    /* Lorentz transformation of the one-forms (pair 1 dots v with A's y, z;
+     * pair 2 with A's x, y) */
+    double Ap[4][3];
+    for (int cc = 0; cc < 3; ++cc) {
+        Ap[0][cc] = b1s->vsq == 0 ? A[0][cc]
+                                  : A[0][cc] + (b1s->gamma - 1) * (b1s->v[1] * A[0][1] + b1s->v[2] * A[0][2]) * b1s->v[cc] / b1s->vsq;
+        Ap[1][cc] = b1a->vsq == 0 ? A[1][cc]
+                                  : A[1][cc] + (b1a->gamma - 1) * (b1a->v[1] * A[1][1] + b1a->v[2] * A[1][2]) * b1a->v[cc] / b1a->vsq;
+        Ap[2][cc] = b2s->vsq == 0 ? A[2][cc]
+                                  : A[2][cc] + (b2s->gamma - 1) * (b2s->v[0] * A[2][0] + b2s->v[1] * A[2][1]) * b2s->v[cc] / b2s->vsq;
+        Ap[3][cc] = b2a->vsq == 0 ? A[3][cc]
+                                  : A[3][cc] + (b2a->gamma - 1) * (b2a->v[0] * A[3][0] + b2a->v[1] * A[3][1]) * b2a->v[cc] / b2a->vsq;
+    }
+    if (!t) {
+        At[0][s] = -b1s->gamma * (b1s->v[1] * A[0][1] + b1s->v[2] * A[0][2]);
+        At[1][s] = -b1a->gamma * (b1a->v[1] * A[1][1] + b1a->v[2] * A[1][2]);
+        At[2][s] = -b2s->gamma * (b2s->v[0] * A[2][0] + b2s->v[1] * A[2][1]);
+        At[3][s] = -b2a->gamma * (b2a->v[0] * A[3][0] + b2a->v[1] * A[3][1]);
+    } else {
+        /* gauge shift to At = 0, periodic centred differences (:1618-1640) */
+        const int ip = (i + 1 + nx) % nx, im = (i - 1 + nx) % nx;
+        const int jp = (j + 1 + ny) % ny, jm = (j - 1 + ny) % ny;
+        const int kp = (k + 1 + nz) % nz, km = (k - 1 + nz) % nz;
+        const int64_t sxp = ((int64_t)ip * ny + j) * nz + k, sxm = ((int64_t)im * ny + j) * nz + k;
+        const int64_t syp = ((int64_t)i * ny + jp) * nz + k, sym = ((int64_t)i * ny + jm) * nz + k;
+        const int64_t szp = ((int64_t)i * ny + j) * nz + kp, szm = ((int64_t)i * ny + j) * nz + km;
+        for (int q = 0; q < 4; ++q) Ap[q][0] += -dt * (At[q][sxp] - At[q][sxm]) / (2 * dx);
+        for (int q = 0; q < 4; ++q) Ap[q][1] += -dt * (At[q][syp] - At[q][sym]) / (2 * dy);
+        for (int q = 0; q < 4; ++q) Ap[q][2] += -dt * (At[q][szp] - At[q][szm]) / (2 * dz);
+    }
+    /* pair products, tapered imaginary parts, magnitude kept (:1234-1262) */
+    double A1[3], A2[3];
+    for (int pair = 0; pair < 2; ++pair) {
+        const double* a = ph[2 * pair];
+        const double* bq = ph[2 * pair + 1];
+        double p0 = a[0] * bq[0] - a[1] * bq[1];
+        double p1 = a[1] * bq[0] + a[0] * bq[1];
+        const double pf = pair == 0 ? (1 - pow(yb / (y0 * dy), 2)) * (1 - pow(zb / (z0 * dz), 2))
+                                    : (1 - pow(xb / (x0 * dx), 2)) * (1 - pow(yb / (y0 * dy), 2));
+        if (pow(p0, 2) + pow(p1 * pf, 2) == 0) {
+            p0 = p1;
+            p1 = 0;
+        } else {
+            const double nf = sqrt((pow(p0, 2) + pow(p1, 2)) / (pow(p0, 2) + pow(p1 * pf, 2)));
+            p0 = nf * p0;
+            p1 = nf * pf * p1;
+        }
+        P0[2 * pair] = p0;
+        P0[2 * pair + 1] = p1;
+        double* Ad = pair == 0 ? A1 : A2;
+        for (int cc = 0; cc < 3; ++cc) Ad[cc] = (Ap[2 * pair][cc] + Ap[2 * pair + 1][cc]) * pf;
+    }
+    th[0] = dx * g * (A1[0] + A2[0]);
+    th[1] = dy * g * (A1[1] + A2[1]);
+    th[2] = dz * g * (A1[2] + A2[2]);
+    return off;
+}
+
+static double lc_mag(const double* re, const double* im, int64_t s)
+{
+    return sqrt(pow(re[s], 2) + pow(im[s], 2));
+}
+
+int64_t orc_loop_collision_ic(const lat_params* p, const lat_string_profile* prof, const lat_loop_collision_ic* c,
+                              double* st)
+{
+    const int nx = p->nx, ny = p->ny, nz = p->nz;
+    if (nx < 3 || ny < 3 || nz < 3 || !prof || prof->m < 2 || !(prof->h > 0) || !c) return -1;
+    lc_boost B[4];
+    lc_boost_init(&B[0], c->v1s);
+    lc_boost_init(&B[1], c->v1a);
+    lc_boost_init(&B[2], c->v2s);
+    lc_boost_init(&B[3], c->v2a);
+    for (int q = 0; q < 4; ++q)
+        if (!(B[q].vsq < 1)) return -1;
+    /* positions in each string's rest frame (:1030-1046) */
+    double sf[4][2];
+    const double* pos[4] = {c->pos1s, c->pos1a, c->pos2s, c->pos2a};
+    for (int q = 0; q < 4; ++q) {
+        const lc_boost* b = &B[q];
+        if (b->vsq == 0) { sf[q][0] = pos[q][0]; sf[q][1] = pos[q][1]; continue; }
+        const int i0 = q < 2 ? 1 : 0;   /* pair 1: (y, z) use v[1], v[2]; pair 2: (x, y) use v[0], v[1] */
+        const double dot = b->v[i0] * pos[q][0] + b->v[i0 + 1] * pos[q][1];
+        sf[q][0] = pos[q][0] + (b->gamma - 1) * dot * b->v[i0] / b->vsq;
+        sf[q][1] = pos[q][1] + (b->gamma - 1) * dot * b->v[i0 + 1] / b->vsq;
+    }
+    const int64_t N = (int64_t)nx * ny * nz;
+    double* buf = (double*)malloc(sizeof(double) * (size_t)N * 12);
+    if (!buf) return -1;
+    double* At[4] = {buf, buf + N, buf + 2 * N, buf + 3 * N};
+    double* P0[4] = {buf + 4 * N, buf + 5 * N, buf + 6 * N, buf + 7 * N};   /* phi1_0 re, im; phi2_0 re, im */
+    double* P1[4] = {buf + 8 * N, buf + 9 * N, buf + 10 * N, buf + 11 * N};
+    const int x0 = (nx - 1) / 2, y0 = (ny - 1) / 2, z0 = (nz - 1) / 2;
+    const double dx = p->dx, dy = p->dy, dz = p->dz;
+    int64_t off = 0;
+#define LST(cc, t) (st + ((size_t)(cc) * 2 + (t)) * (size_t)N)
+#define IX(i, j, k) (((int64_t)(i) * ny + (j)) * nz + (k))
+    for (int t = 0; t < 2; ++t) {
+        for (int i = 0; i < nx; ++i)
+            for (int j = 0; j < ny; ++j)
+                for (int k = 0; k < nz; ++k) {
+                    double v4[4], th[3];
+                    off += lc_site(p, prof, c, B, sf, t, i, j, k, At, v4, th);
+                    const int64_t s = IX(i, j, k);
+                    for (int q = 0; q < 4; ++q) P0[q][s] = v4[q];
+                    LST(2, t)[s] = th[0];
+                    LST(3, t)[s] = th[1];
+                    LST(4, t)[s] = th[2];
+                }
+        /* magnitudes made continuous across the periodic faces: pair 1 over y,
+         * pair 2 over x (:1336-1372), then pair 1 over z, pair 2 over y
+         * (:1376-1414) */
+        for (int i = 0; i < nx; ++i)
+            for (int j = 0; j < ny; ++j)
+                for (int k = 0; k < nz; ++k) {
+                    const double xb = (i - x0) * dx, yb = (j - y0) * dy;
+                    const int64_t s = IX(i, j, k);
+                    const double m1t = lc_mag(P0[0], P0[1], IX(i, ny - 1, k)), m1b = lc_mag(P0[0], P0[1], IX(i, 0, k));
+                    const double m2t = lc_mag(P0[2], P0[3], IX(nx - 1, j, k)), m2b = lc_mag(P0[2], P0[3], IX(0, j, k));
+                    const double i1 = (m1t - m1b) * (yb + y0 * dy) / (2 * y0 * dy) + m1b;
+                    const double i2 = (m2t - m2b) * (xb + x0 * dx) / (2 * x0 * dx) + m2b;
+                    P1[0][s] = P0[0][s] / i1;
+                    P1[1][s] = P0[1][s] / i1;
+                    P1[2][s] = P0[2][s] / i2;
+                    P1[3][s] = P0[3][s] / i2;
+                }
+        for (int i = 0; i < nx; ++i)
+            for (int j = 0; j < ny; ++j)
+                for (int k = 0; k < nz; ++k) {
+                    const double yb = (j - y0) * dy, zb = (k - z0) * dz;
+                    const int64_t s = IX(i, j, k);
+                    const double m1t = lc_mag(P1[0], P1[1], IX(i, j, nz - 1)), m1b = lc_mag(P1[0], P1[1], IX(i, j, 0));
+                    const double m2t = lc_mag(P1[2], P1[3], IX(i, ny - 1, k)), m2b = lc_mag(P1[2], P1[3], IX(i, 0, k));
+                    const double i1 = (m1t - m1b) * (zb + z0 * dz) / (2 * z0 * dz) + m1b;
+                    const double i2 = (m2t - m2b) * (yb + y0 * dy) / (2 * y0 * dy) + m2b;
+                    const double a0 = P1[0][s] / i1, a1 = P1[1][s] / i1;
+                    const double b0 = P1[2][s] / i2, b1 = P1[3][s] / i2;
+                    LST(0, t)[s] = a0 * b0 - a1 * b1;
+                    LST(1, t)[s] = a0 * b1 + a1 * b0;
+                }
+    }
+#undef LST
+#undef IX
+    free(buf);
+    return off;
+}

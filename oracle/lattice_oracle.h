@@ -71,6 +71,12 @@ int orc_icfunc_random_ic(const lat_params* p, uint32_t seed, double* st);
  * evaluations beyond the profile table, or -1 for bad arguments. */
 int64_t orc_boost_ic(const lat_params* p, const lat_string_profile* prof, const lat_boost_ic* b, double* st);
 
+/* Loop-collision IC (initialConditions.cpp:994-1716) into a full AH state:
+ * slot 0 = t 0, slot 1 = t dt.  Returns the number of evaluations beyond the
+ * profile table, or -1 for bad arguments. */
+int64_t orc_loop_collision_ic(const lat_params* p, const lat_string_profile* prof, const lat_loop_collision_ic* c,
+                              double* st);
+
 /* total string length by greedy chaining of crossings, ic_w_evolution.cpp:961-1087 */
 int orc_string_length(const lat_params* p, const double* xyz, int64_t M, int split, double* L0, double* L1);
 

@@ -57,6 +57,8 @@ def lib():
         L.orc_icfunc_random_ic.argtypes = [P(LatParams), ctypes.c_uint32, dp]
         L.orc_boost_ic.argtypes = [P(LatParams), ctypes.c_void_p, ctypes.c_void_p, dp]
         L.orc_boost_ic.restype = ctypes.c_int64
+        L.orc_loop_collision_ic.argtypes = [P(LatParams), ctypes.c_void_p, ctypes.c_void_p, dp]
+        L.orc_loop_collision_ic.restype = ctypes.c_int64
         L.orc_string_length.argtypes = [P(LatParams), dp, ctypes.c_int64, ctypes.c_int, dp, dp]
         _lib = L
     return _lib
@@ -171,6 +173,21 @@ def boost_ic(p: LatParams, phi: np.ndarray, A: np.ndarray, h: float, v, form: in
     del keep
     if off < 0:
         raise RuntimeError("orc_boost_ic: bad arguments")
+    return st, int(off)
+
+
+def loop_collision_ic(p: LatParams, phi: np.ndarray, A: np.ndarray, h: float, geometry: dict, winding: float = 1.0):
+    """Loop-collision IC (initialConditions.cpp:994-1716).  `geometry` holds
+    pos1s, pos1a, pos2s, pos2a, v1s, v1a, v2s, v2a.  Returns (state, number of
+    evaluations off the table)."""
+    from axions_gb300.params import loop_collision_ic as _c, string_profile
+    prof, keep = string_profile(phi, A, h, winding)
+    c = _c(**geometry)
+    st = empty_state(p)
+    off = lib().orc_loop_collision_ic(ctypes.byref(p), ctypes.byref(prof), ctypes.byref(c), _dp(st))
+    del keep
+    if off < 0:
+        raise RuntimeError("orc_loop_collision_ic: bad arguments")
     return st, int(off)
 
 

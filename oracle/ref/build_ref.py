@@ -55,6 +55,8 @@ def _fmt(v) -> str:
         return '"' + v + '"'
     if isinstance(v, float):
         return repr(v)
+    if isinstance(v, (list, tuple)):
+        return "{" + ", ".join(_fmt(float(x)) for x in v) + "}"
     return str(v)
 
 
@@ -63,8 +65,8 @@ def substitute_consts(src: str, consts: dict) -> str:
     boundary-condition strings of ic_w_evolution.cpp:44-45 are not const)."""
     out = src
     for name, val in consts.items():
-        pat = re.compile(r"^(\s*(?:const\s+)?(?:int|double|bool|string)\s+" + re.escape(name) + r"\s*=\s*)([^;]*)(;)",
-                         re.MULTILINE)
+        pat = re.compile(r"^(\s*(?:const\s+)?(?:int|double|bool|string)\s+" + re.escape(name)
+                         + r"(?:\[\d*\])?\s*=\s*)([^;]*)(;)", re.MULTILINE)
         out, n = pat.subn(lambda m: m.group(1) + _fmt(val) + m.group(3), out, count=1)
         if n != 1:
             raise KeyError(f"const {name} not found")

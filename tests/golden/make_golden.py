@@ -273,6 +273,33 @@ def gen_boost_ic(name, nx, ny, nz, g, dt, v, profile, sor_h, dz=0.5):
     print(name, ic.shape)
 
 
+def gen_loop_collision_ic(name, nx, ny, nz, g, dt, profile, sor_h, dz=0.5, geometry=None):
+    """initialConditions.cpp, ic_type "loop collision": Data/ic.txt, two levels
+    (17 digits), from the profile table at dir_path/Data/SOR_Fields.txt.
+    `geometry` overrides the string positions and velocities (pos1s, pos1a,
+    pos2s, pos2a, v1s, v1a, v2s, v2a); by default they follow the lattice
+    (initialConditions.cpp:72-84)."""
+    m = profile.shape[1]
+    consts = {"nx": nx, "ny": ny, "nz": nz, "ic_type": "loop collision", "g": float(g), "dt": float(dt),
+              "SORnx": m, "SORa": float(sor_h), "dz": float(dz)}
+    geo = dict(pos1s=[0.15 * (ny - 1) * 0.5, -0.25 * (nz - 1) * dz], pos1a=[-0.15 * (ny - 1) * 0.5, 0.25 * (nz - 1) * dz],
+               pos2s=[0.25 * (nx - 1) * 0.5, 0.0], pos2a=[-0.25 * (nx - 1) * 0.5, 0.0],
+               v1s=[0.0, -0.75, 0.0], v1a=[0.0, 0.75, 0.0], v2s=[0.0, 0.0, 0.0], v2a=[0.0, 0.0, 0.0])
+    if geometry:
+        geo.update(geometry)
+        consts.update(geometry)
+    build_ref.build("initialConditions", name, consts)
+    work = build_ref.SCRATCH / name
+    lines = [f"{float(profile[0, r])!r} {float(profile[1, r])!r}" for r in range(m)]
+    (work / "Data" / "SOR_Fields.txt").write_text("\n".join(lines) + "\n")
+    work = build_ref.run(name)
+    ic = build_ref.read_columns(work / "Data" / "ic.txt").reshape(2, nx * ny * nz, 5).transpose(2, 0, 1).copy()
+    np.savez_compressed(OUT / f"{name}.npz", program="initialConditions", ic_type="loop collision", nx=nx, ny=ny,
+                        nz=nz, dx=0.5, dy=0.5, dz=dz, g=g, dt=dt, sor_h=sor_h, profile=profile, ic=ic,
+                        **{k: np.array(v, dtype=np.float64) for k, v in geo.items()})
+    print(name, ic.shape)
+
+
 def main():
     if not build_ref.reference_available():
         raise SystemExit("reference sources not found; fixtures can only be made where they are")
@@ -320,6 +347,12 @@ def main():
     gen_boost_ic("ref_boost_ic", 13, 12, 11, 1.0, 0.05, (0.24, 0.6 * (1 - 0.4 ** 2) ** 0.5, 0.0), prof, 0.01)
     # a velocity with a z part and dz != dy (initialConditions.cpp:745 takes zb with dy at t = 0)
     gen_boost_ic("ref_boost_ic_vz", 12, 11, 13, 0.8, 0.1, (0.3, -0.2, 0.45), prof, 0.01, dz=0.4)
+    # loop collision: the reference geometry, and every string moving (pair 2 too) with dz != dy
+    gen_loop_collision_ic("ref_loop_collision_ic", 14, 12, 16, 1.0, 0.05, prof, 0.01)
+    gen_loop_collision_ic("ref_loop_collision_ic_moving", 13, 15, 12, 0.7, 0.1, prof, 0.01, dz=0.4,
+                          geometry=dict(pos1s=[1.1, -0.9], pos1a=[-0.8, 1.3], pos2s=[1.4, 0.2], pos2a=[-1.2, -0.3],
+                                        v1s=[0.1, -0.5, 0.3], v1a=[0.0, 0.6, -0.2], v2s=[0.3, 0.2, 0.0],
+                                        v2a=[-0.25, -0.3, 0.1]))
 
 
 if __name__ == "__main__":

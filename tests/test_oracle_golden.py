@@ -190,3 +190,27 @@ def test_boost_ic_forms_and_table_edge(oracle_mod):
     assert np.sum(np.isclose(far, 1.0, rtol=0, atol=1e-15)) > 0
     with pytest.raises(RuntimeError):
         oracle_mod.boost_ic(p, short[0], short[1], 0.01, (0.0, 0.0, 0.0))
+
+
+LOOP_CASES = ["ref_loop_collision_ic", "ref_loop_collision_ic_moving"]
+
+
+@pytest.mark.parametrize("name", LOOP_CASES)
+def test_loop_collision_ic_bit_exact(oracle_mod, name):
+    """initialConditions.cpp "loop collision" (both levels of Data/ic.txt): the
+    reference's placement on one lattice, and every string moving with dz != dy
+    on another."""
+    from axions_gb300.params import LOOP_COLLISION_KEYS
+    z = load_golden(name)
+    geo = {k: z[k] for k in LOOP_COLLISION_KEYS}
+    st, off = oracle_mod.loop_collision_ic(boost_params(z), z["profile"][0], z["profile"][1], float(z["sor_h"]), geo)
+    assert off == 0
+    assert np.array_equal(st.reshape(5, 2, -1), z["ic"])
+
+
+def test_loop_collision_default_geometry_is_the_references(oracle_mod):
+    from axions_gb300.params import LOOP_COLLISION_KEYS, default_loop_collision
+    z = load_golden("ref_loop_collision_ic")
+    geo = default_loop_collision(int(z["nx"]), int(z["ny"]), int(z["nz"]), 0.5, 0.5, float(z["dz"]))
+    for k in LOOP_COLLISION_KEYS:
+        assert np.array_equal(np.array(geo[k], dtype=np.float64), z[k]), k

@@ -152,3 +152,122 @@ def test_initial_conditions_program_boost(tmp_path):
     got = np.array([float(t) for t in (tmp_path / "Data" / "ic.txt").read_text().split()])
     got = got.reshape(2, -1, 5).transpose(2, 0, 1)
     _close(got, z["ic"], TOL)
+
+
+LOOP_CASES = ["ref_loop_collision_ic", "ref_loop_collision_ic_moving"]
+
+
+def _geo(z):
+    from axions_gb300.params import LOOP_COLLISION_KEYS
+    return {k: z[k] for k in LOOP_COLLISION_KEYS}
+
+
+@pytest.mark.parametrize("name", LOOP_CASES)
+def test_loop_collision_ic_against_reference(lattice_mod, name):
+    """initialConditions.cpp "loop collision" (six launches: the per-site
+    strings, two passes across the periodic faces, per level)."""
+    z = load_golden(name)
+    with lattice_mod.Lattice(_params(z)) as lat:
+        off = lat.loop_collision_ic_device(z["profile"][0], z["profile"][1], float(z["sor_h"]), _geo(z))
+        assert off == 0 and lat.time_step == 0
+        _close(_levels(lat), z["ic"], TOL)
+
+
+def test_loop_collision_default_geometry_and_evolution(lattice_mod, oracle_mod):
+    """The reference's placement is the default; 20 periodic steps from the
+    GPU-built IC track the oracle from the oracle-built IC."""
+    from axions_gb300.params import ENERGY_EVOLUTION
+    z = load_golden("ref_loop_collision_ic")
+    p = _params(z)
+    p.lam = 1.0
+    p.alpha = 0.0
+    p.damped_nt = 0
+    p.energy_form = ENERGY_EVOLUTION
+    st, _ = oracle_mod.loop_collision_ic(p, z["profile"][0], z["profile"][1], float(z["sor_h"]), _geo(z))
+    nt = 20
+    for n in range(nt):
+        oracle_mod.step(p, st, n)
+    with lattice_mod.Lattice(p) as lat:
+        lat.loop_collision_ic_device(z["profile"][0], z["profile"][1], float(z["sor_h"]))
+        _close(_levels(lat), z["ic"], TOL)
+        lat.step(nt)
+        now, _ = lat.get_state()
+    want = st.reshape(5, 2, -1)[:, (nt + 1) % 2]
+    for c in range(5):
+        ref = np.linalg.norm(want[c])
+        assert np.linalg.norm(now[c] - want[c]) <= TOL * ref
+
+
+def test_loop_collision_rejects_bad_arguments(lattice_mod):
+    from axions_gb300.lattice import LatticeError
+    from axions_gb300.params import make_params
+    z = load_golden("ref_loop_collision_ic")
+    prof = z["profile"]
+    with lattice_mod.Lattice(_params(z)) as lat:
+        with pytest.raises(LatticeError):
+            lat.loop_collision_ic_device(prof[0], prof[1], 0.01, {"v1s": [0.0, 1.0, 0.0]})
+        with pytest.raises(LatticeError):
+            lat.loop_collision_ic_device(prof[0][:1], prof[1][:1], 0.01)
+    with lattice_mod.Lattice(make_params(0, nx=2, ny=8, nz=8)) as lat:
+        with pytest.raises(LatticeError):
+            lat.loop_collision_ic_device(prof[0], prof[1], 0.01)
+
+
+def test_initial_conditions_program_loop_collision(tmp_path):
+    """bin/initialConditions ic_type="loop collision" with explicit strings,
+    reading Data/SOR_Fields.txt as the reference does."""
+    z = load_golden("ref_loop_collision_ic_moving")
+    prof = z["profile"]
+    (tmp_path / "Data").mkdir()
+    (tmp_path / "Data" / "SOR_Fields.txt").write_text(
+        "".join(f"{float(a)!r} {float(b)!r}\n" for a, b in zip(prof[0], prof[1])))
+    args = {"ic_type": "loop collision", "nx": int(z["nx"]), "ny": int(z["ny"]), "nz": int(z["nz"]), "dx": 0.5,
+            "dy": 0.5, "dz": float(z["dz"]), "dt": float(z["dt"]), "g": float(z["g"]), "SORnx": prof.shape[1],
+            "SORa": float(z["sor_h"]), "digits": 17}
+    for k, v in _geo(z).items():
+        args[k] = ",".join(repr(float(x)) for x in v)
+    cmd = [str(ROOT / "axions_gb300" / "bin" / "initialConditions"), f"out_dir={tmp_path}"]
+    r = subprocess.run(cmd + [f"{k}={x}" for k, x in args.items()], capture_output=True, timeout=300)
+    assert r.returncode == 0, r.stderr.decode()
+    got = np.array([float(t) for t in (tmp_path / "Data" / "ic.txt").read_text().split()])
+    _close(got.reshape(2, -1, 5).transpose(2, 0, 1), z["ic"], TOL)
+
+
+def test_icw_program_boost_and_data_modes(tmp_path, oracle_mod):
+    """bin/ic_w_evolution builds ic_func.cpp's boost in-process (its rounding);
+    the same run from that IC written to Data/ic.txt (ic_type=data) gives the
+    same energies, lengths and final field."""
+    from axions_gb300.params import IC_FORM_INPROCESS, make_params
+    z = load_golden("ref_sor_gauge")
+    prof = z["profile"]
+    v = (0.3, 0.2, 0.0)
+    n, dt, g = 12, 0.05, 1.0
+    common = {"nx": n, "ny": n, "nz": n, "nt": 4, "dx": 0.5, "dy": 0.5, "dz": 0.5, "dt": dt, "g": g, "lambda": 1,
+              "makeGif": "false", "digits": 17, "saveFreq": 2, "xyBC": "fixed", "zBC": "fixed"}
+    runs = {}
+    for mode in ("boost", "data"):
+        d = tmp_path / mode
+        (d / "Data").mkdir(parents=True)
+        (d / "GifData").mkdir()
+        args = dict(common, ic_type=mode)
+        if mode == "boost":
+            (d / "SOR_Fields.txt").write_text("".join(f"{float(a)!r} {float(b)!r}\n" for a, b in zip(prof[0], prof[1])))
+            args.update(SORnx=prof.shape[1], SORa=0.01, v1x=v[0], v1y=v[1], v1z=v[2])
+        else:
+            p = make_params(0, n=n, d=0.5, dt=dt, g=g)
+            st, _ = oracle_mod.boost_ic(p, prof[0], prof[1], 0.01, v, IC_FORM_INPROCESS)
+            lv = st.reshape(5, 2, -1)
+            lines = [" ".join(repr(float(lv[c, t, s])) for c in range(5)) for t in (0, 1) for s in range(n ** 3)]
+            (d / "Data" / "ic.txt").write_text("\n".join(lines) + "\n")
+        cmd = [str(ROOT / "axions_gb300" / "bin" / "ic_w_evolution"), f"out_dir={d}"]
+        r = subprocess.run(cmd + [f"{k}={x}" for k, x in args.items()], input=b"", capture_output=True, timeout=300)
+        assert r.returncode == 0, r.stderr.decode()
+        vals = np.array([float(t) for t in (d / "Data" / "valsPerLoop_test.txt").read_text().split()])
+        final = np.array([float(t) for t in (d / "Data" / "finalField.txt").read_text().split()])
+        runs[mode] = (vals.reshape(4, -1), final.reshape(-1, 5).T)
+    (va, fa), (vb, fb) = runs["boost"], runs["data"]
+    np.testing.assert_allclose(va[:, 0], vb[:, 0], rtol=TOL, atol=0)
+    assert np.abs(va[:, 2:] - vb[:, 2:]).max() <= 1e-9 * max(1.0, np.abs(vb[:, 2:]).max())
+    for c in range(5):
+        ref = np.max(np.abs(fb[c]))
+        assert np.max(np.abs(fa[c] - fb[c])) <= TOL * max(ref, 1e-300)
