@@ -502,6 +502,68 @@ def measure_fp32_accuracy(n: int, steps: int, sample_every: int = 100):
     return out
 
 
+def measure_string_ic(n: int, cpu_n: int):
+    """The string initial conditions of initialConditions.cpp at its default
+    n^3 = 401^3 lattice (dx 0.5, dt 0.05; g = 1 so the links are not zero):
+    the straight-string profile relaxed by bin/singleSemiAnalytic (2001 points
+    at h = 0.1: out to r = 200 like the reference's 20001 points at h = 0.01;
+    the loop collision's farthest rest-frame distances lie beyond it, as with
+    the reference's table), then the
+    boosted string (both levels) and the loop collision (both levels, six
+    launches) built on the GPU from it (wall time, fields resident, best of
+    3).  CPU: the oracle's restatement of the same families (one thread, as
+    the reference's serial passes) timed on a cpu_n^3 lattice and scaled by
+    the sites."""
+    import subprocess as sp
+    import tempfile as tf
+
+    import numpy as np
+    import torch
+
+    from axions_gb300 import lattice
+    from axions_gb300.params import make_params
+    from oracle import oracle as O
+    prog = ROOT / "axions_gb300" / "bin" / "singleSemiAnalytic"
+    with tf.TemporaryDirectory() as d:
+        t0 = time.perf_counter()
+        r = sp.run([str(prog), f"out_dir={d}", "nx=2001", "h=0.1", "g=1", "digits=17"], stdout=sp.PIPE, stderr=sp.PIPE)
+        sor_s = time.perf_counter() - t0
+        if r.returncode != 0:
+            return {"error": r.stderr.decode()[-200:]}
+        prof = np.array([float(t) for t in (Path(d) / "Data" / "SOR_Fields.txt").read_text().split()]).reshape(-1, 2).T
+    prof = np.ascontiguousarray(prof)
+    h = 0.1
+    v = (0.24, 0.5499090833947008, 0.0)
+    out = {"lattice": n, "profile": {"program": "bin/singleSemiAnalytic nx=2001 h=0.1 g=1", "seconds": sor_s}}
+    p = make_params(0, n=n, d=0.5, dt=0.05, g=1.0)
+    with lattice.Lattice(p) as lat:
+        for kind in ("boost", "loop_collision"):
+            def build():
+                if kind == "boost":
+                    return lat.boost_ic_device(prof[0], prof[1], h, v)
+                return lat.loop_collision_ic_device(prof[0], prof[1], h)
+            off = build()
+            torch.cuda.synchronize()
+            best = 1e30
+            for _ in range(3):
+                t0 = time.perf_counter()
+                build()
+                torch.cuda.synchronize()
+                best = min(best, time.perf_counter() - t0)
+            pc = make_params(0, n=cpu_n, d=0.5, dt=0.05, g=1.0)
+            t0 = time.perf_counter()
+            if kind == "boost":
+                O.boost_ic(pc, prof[0], prof[1], h, v)
+            else:
+                from axions_gb300.params import default_loop_collision
+                O.loop_collision_ic(pc, prof[0], prof[1], h, default_loop_collision(cpu_n, cpu_n, cpu_n, 0.5, 0.5, 0.5))
+            cpu = (time.perf_counter() - t0) * (n / cpu_n) ** 3
+            out[kind] = {"gpu_s": best, "sites_per_s": n ** 3 / best, "off_table": off,
+                         "cpu_port_s_extrapolated": cpu, "cpu_sample": f"{cpu_n}^3, one thread",
+                         "speedup_vs_cpu": cpu / best}
+    return out
+
+
 def measure_string_length(n: int, max_steps: int, max_crossings: int, cpu_sample: int):
     """Total string length by greedy chaining (ic_w_evolution.cpp:961-1087) of
     the crossings of an n^3 lattice of global strings (the reference's default
@@ -624,6 +686,8 @@ def main():
     ap.add_argument("--accuracy-n", type=int, default=256, help="lattice side of the accuracy study (workload: 512)")
     ap.add_argument("--accuracy-steps", type=int, default=1000)
     ap.add_argument("--no-length", action="store_true", help="skip the string-length measurement")
+    ap.add_argument("--no-ic", action="store_true", help="skip the string initial-condition measurement")
+    ap.add_argument("--ic-n", type=int, default=401)
     ap.add_argument("--length-n", type=int, default=512)
     ap.add_argument("--length-max-steps", type=int, default=4000)
     ap.add_argument("--length-max-crossings", type=int, default=1500000)
@@ -717,6 +781,11 @@ def main():
         slen = measure_string_length(args.length_n, args.length_max_steps, args.length_max_crossings,
                                      args.length_cpu_sample)
     note("string length", t_leg)
+    t_leg = time.perf_counter()
+    string_ic = None
+    if not args.no_ic and args.model == "ah" and rank == 0:
+        string_ic = measure_string_ic(args.ic_n, 48)
+    note("string initial conditions", t_leg)
     if rank != 0:
         return
     achieved = bytes_per_site(head) * res["sites"] / (res["kern_ms"] * 1e-3) / 1e9
@@ -746,6 +815,7 @@ def main():
         "serving": serving,
         "fp32_accuracy": accuracy,
         "string_length": slen,
+        "string_ic": string_ic,
     }
     print(json.dumps(line), flush=True)
     if ws > 1:
