@@ -12,9 +12,9 @@ cudaError_t launch_ah_step_f32(const Geom& g, const Fields<float, 5>& f, const S
 }
 
 cudaError_t launch_ah_tiled_f32(const Geom& g, const Fields<float, 5>& f, const StepCoef& c, const DiagOut& d,
-                                bool diag, int chunk, cudaStream_t st)
+                                bool diag, int chunk, cudaStream_t st, bool allow_vec)
 {
-    return launch_tiled_t<float, 1>(g, f, c, d, diag, chunk, st);
+    return launch_tiled_t<float, 1>(g, f, c, d, diag, chunk, st, allow_vec);
 }
 
 cudaError_t launch_divergence_f32(const Geom& g, const float* tx, const float* ty, const float* tz, const StepCoef& c,

@@ -36,6 +36,7 @@ struct BatchJob {
     int ns;                 // scalars: 1 (AH) or 2 (Moore)
     int diag;               // record diagnostics at this step
     int chunk;
+    int vec;                // 16-byte staging (tiled_vec_ok)
     int tiles_z, tiles_y;
     int items;              // tiles_z * tiles_y * x-chunks
     int item_begin;         // first work item of this job in the step
@@ -67,9 +68,9 @@ __device__ __forceinline__ void run_item(unsigned char* smem_raw, const BatchJob
 {
     TiledSmem<float, NS>& sm = *reinterpret_cast<TiledSmem<float, NS>*>(smem_raw);
     if constexpr (NS == 1) {
-        tiled_tile<float, 1, DIAG>(sm, J.g, f5, J.c, J.ch, J.d, bx, by, bz, J.chunk, part);
+        tiled_tile<float, 1, DIAG>(sm, J.g, f5, J.c, J.ch, J.d, bx, by, bz, J.chunk, part, J.vec != 0);
     } else {
-        tiled_tile<float, 2, DIAG>(sm, J.g, J.f, J.c, J.ch, J.d, bx, by, bz, J.chunk, part);
+        tiled_tile<float, 2, DIAG>(sm, J.g, J.f, J.c, J.ch, J.d, bx, by, bz, J.chunk, part, J.vec != 0);
     }
 }
 
@@ -425,6 +426,7 @@ int lat_batch_advance(lat_batch* b, int32_t nsteps)
             // on the lattice's own shape only, never on its company, so
             // results do not depend on the mix.
             J.chunk = b->chunk > 0 ? std::min(h->geom.hix - h->geom.lox, b->chunk) : batch_chunk(h->geom);
+            J.vec = h->p.kernel_variant != 2 && tiled_vec_ok(h->geom, J.f) ? 1 : 0;
             const dim3 tg = tiled_grid(h->geom, J.chunk);
             J.tiles_z = (int)tg.x;
             J.tiles_y = (int)tg.y;

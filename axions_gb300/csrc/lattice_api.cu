@@ -195,7 +195,8 @@ static int validate(const lat_params* p)
     LAT_REQUIRE(p->model == LAT_MODEL_AH || p->model == LAT_MODEL_MOORE, "unknown model");
     LAT_REQUIRE(p->precision == LAT_F64 || p->precision == LAT_F32 || p->precision == LAT_F64_FAST,
                 "unknown precision");
-    LAT_REQUIRE(p->kernel_variant == 0 || p->kernel_variant == 1, "unknown kernel_variant");
+    LAT_REQUIRE(p->kernel_variant == 0 || p->kernel_variant == 1 || (p->kernel_variant == 2 && p->precision == LAT_F32),
+                "unknown kernel_variant (2 is for FP32 only)");
     LAT_REQUIRE(p->bc >= LAT_BC_PERIODIC && p->bc <= LAT_BC_ABSORBING, "unknown boundary condition");
     LAT_REQUIRE(p->bc_z >= LAT_BCZ_AS_XY && p->bc_z <= LAT_BCZ_NEUMANN, "unknown bc_z");
     const int kz = bc_z_kind(*p);
@@ -523,7 +524,8 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
                 f.now[c] = (const float*)h->slot(c, tNow);
                 f.past[c] = (float*)h->slot(c, tPast);
             }
-            if (p.kernel_variant == 0) LAT_CKL(launch_ah_tiled_f32(h->geom, f, cf, d, diag, h->chunk, h->stream));
+            if (p.kernel_variant != 1)
+                LAT_CKL(launch_ah_tiled_f32(h->geom, f, cf, d, diag, h->chunk, h->stream, p.kernel_variant == 0));
             else LAT_CKL(launch_ah_step_f32(h->geom, f, cf, d, diag, h->stream));
         }
     } else {
@@ -540,14 +542,15 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
                 f.now[c] = (const float*)h->slot(c, tNow);
                 f.past[c] = (float*)h->slot(c, tPast);
             }
-            if (p.kernel_variant == 0) LAT_CKL(launch_moore_tiled_f32(h->geom, f, cf, d, diag, h->chunk, h->stream));
+            if (p.kernel_variant != 1)
+                LAT_CKL(launch_moore_tiled_f32(h->geom, f, cf, d, diag, h->chunk, h->stream, p.kernel_variant == 0));
             else LAT_CKL(launch_moore_step_f32(h->geom, f, cf, d, diag, h->stream));
         }
     }
     if (absorb) LAT_CKL(launch_absorb_update(h->geom, (int)h->elem, nowv, pastv, h->btt, p.dt * p.dt, h->stream));
     if (diag) {
         // partials written by the step: one per CTA of the kernel that ran
-        const bool tiled = h->elem == 4 && p.kernel_variant == 0;
+        const bool tiled = h->elem == 4 && p.kernel_variant != 1;
         const int used = tiled ? tiled_blocks(h->geom, h->chunk) : h->nblocks;
         LAT_CKL(launch_finalize(h->partials, used, diag_dst, h->stream));
     }

@@ -119,11 +119,12 @@ int default_chunk(const lat_params& p);
 int batch_chunk(const Geom& g);
 // number of CTAs (and diagnostic partials) of the tiled FP32 step
 int tiled_blocks(const Geom&, int chunk);
-// tiled, x-marching FP32 Abelian-Higgs step; `chunk` x-planes per CTA
+// tiled, x-marching FP32 Abelian-Higgs step; `chunk` x-planes per CTA.
+// allow_vec = false keeps the one-element staging copies (kernel_variant 2)
 cudaError_t launch_ah_tiled_f32(const Geom&, const Fields<float, 5>&, const StepCoef&, const DiagOut&, bool diag,
-                                int chunk, cudaStream_t);
+                                int chunk, cudaStream_t, bool allow_vec = true);
 cudaError_t launch_moore_tiled_f32(const Geom&, const Fields<float, 7>&, const StepCoef&, const DiagOut&, bool diag,
-                                   int chunk, cudaStream_t);
+                                   int chunk, cudaStream_t, bool allow_vec = true);
 // divergence of theta on one level into divbuf (used when no previous step stored it)
 cudaError_t launch_divergence_f64(const Geom&, const double* thx, const double* thy, const double* thz,
                                   const StepCoef&, double* out, cudaStream_t);

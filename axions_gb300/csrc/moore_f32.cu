@@ -12,9 +12,9 @@ cudaError_t launch_moore_step_f32(const Geom& g, const Fields<float, 7>& f, cons
 }
 
 cudaError_t launch_moore_tiled_f32(const Geom& g, const Fields<float, 7>& f, const StepCoef& c, const DiagOut& d,
-                                   bool diag, int chunk, cudaStream_t st)
+                                   bool diag, int chunk, cudaStream_t st, bool allow_vec)
 {
-    return launch_tiled_t<float, 2>(g, f, c, d, diag, chunk, st);
+    return launch_tiled_t<float, 2>(g, f, c, d, diag, chunk, st, allow_vec);
 }
 
 }  // namespace lat

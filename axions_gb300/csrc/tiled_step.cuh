@@ -9,7 +9,8 @@
 // every plaquette sine once for each site that uses it.  Here a CTA owns a
 // TZ x TY tile of (z, y) columns and marches along x.  For each x-plane:
 //   * the now-level theta and phi of the tile plus a one-site halo are staged
-//     in shared memory by cp.async, two planes ahead of the compute;
+//     in shared memory by cp.async, two planes ahead of the compute, in
+//     16-byte row chunks where the layout allows (periodic z, nz % 4 == 0);
 //   * every site of the tile plus its low y/z halo evaluates its link data
 //     once: e^{i q_f theta_mu} for each scalar f and direction mu, and the
 //     sines of the plaquettes P_xy, P_xz, P_yz (sin P_yx = -sin P_xy etc.);
@@ -35,6 +36,9 @@ constexpr int TT_HY = TT_Y + 2;
 constexpr int TT_LZ = TT_Z + 1;     // link data: tile + low halo
 constexpr int TT_LY = TT_Y + 1;
 constexpr int TT_STAGES = 3;        // planes i, i+1 in use, i+2 in flight
+constexpr int TT_PZ = 40;           // staged row pitch (elements): 160 B, rows start on 16-byte boundaries
+constexpr int TT_C0 = 3;            // column of staged position hz = 0 (z = k0 - 1); z = k0 is column 4
+constexpr int TT_NQ = TT_PZ / 4;    // 16-byte chunks of a staged row
 
 // link data kept in shared memory for the y/z neighbours:
 // per scalar f: cos/sin(q_f theta_y), cos/sin(q_f theta_z); then sin P_xy, P_xz, P_yz
@@ -49,8 +53,8 @@ struct LinkIdx {
 
 template <class T, int NS>
 struct TiledSmem {
-    T th[TT_STAGES][3][TT_HY][TT_HZ];       // theta_x,y,z of a plane
-    T ph[TT_STAGES][2 * NS][TT_HY][TT_HZ];  // scalar components of a plane
+    T th[TT_STAGES][3][TT_HY][TT_PZ];       // theta_x,y,z of a plane; position (hy, hz) at [hy][hz + TT_C0]
+    T ph[TT_STAGES][2 * NS][TT_HY][TT_PZ];  // scalar components of a plane
     T L[LinkIdx<NS>::count][TT_LY][TT_LZ];  // link data of the current plane
     double red[2][TT_THREADS / 32];
 };
@@ -97,33 +101,95 @@ __device__ __forceinline__ void charged(T theta, T c1, T s1, const Charges<T>& c
     }
 }
 
-// Issue the asynchronous copy of plane `pi` (tile + halo) into stage `b`.
-// The TT_HY x TT_HZ staged positions are spread evenly over the CTA's threads
-// (no warp copies more than two), so no warp arrives late at the barrier.
+// Issue the asynchronous copy of plane `pi` (tile + halo) into stage `b`,
+// one element per copy.  The staged positions are spread evenly over the
+// CTA's threads (no warp copies more than two), so no warp arrives late at
+// the barrier.  Only the positions the tile's in-range sites use are copied:
+// rows j0-1 .. j0+wy and columns k0-1 .. k0+wz (wy, wz the in-range rows and
+// columns of the tile), whose indices wrap at most once.
 template <class T, int NS>
 __device__ __forceinline__ void stage_plane(TiledSmem<T, NS>& sm, int b, const Fields<T, 2 * NS + 3>& f, const Geom& g,
-                                            int pi, int j0, int k0)
+                                            int pi, int j0, int k0, int wy, int wz)
 {
     const int tid = threadIdx.y * TT_Z + threadIdx.x;
     const int base = pi * g.syz;
     for (int q = tid; q < TT_HY * TT_HZ; q += TT_THREADS) {
         const int hy = q / TT_HZ, hz = q - hy * TT_HZ;
+        if (hy > wy + 1 || hz > wz + 1) continue;
         const int s = base + wrap_idx(j0 - 1 + hy, g.ny) * g.nz + wrap_idx(k0 - 1 + hz, g.nz);
 #pragma unroll
-        for (int m = 0; m < 3; ++m) __pipeline_memcpy_async(&sm.th[b][m][hy][hz], f.now[2 * NS + m] + s, sizeof(T));
+        for (int m = 0; m < 3; ++m) __pipeline_memcpy_async(&sm.th[b][m][hy][hz + TT_C0], f.now[2 * NS + m] + s, sizeof(T));
 #pragma unroll
-        for (int c = 0; c < 2 * NS; ++c) __pipeline_memcpy_async(&sm.ph[b][c][hy][hz], f.now[c] + s, sizeof(T));
+        for (int c = 0; c < 2 * NS; ++c) __pipeline_memcpy_async(&sm.ph[b][c][hy][hz + TT_C0], f.now[c] + s, sizeof(T));
     }
     __pipeline_commit();
 }
 
+// 16-byte staging (FP32, periodic z, nz a multiple of 4, 16-byte aligned
+// fields): a staged row is TT_NQ chunks of 4 elements, chunk cq holding
+// z = k0-4+4cq .. k0-1+4cq, which wrap as one piece because nz and the chunk
+// start are multiples of 4.  Threads 64..163 (warps 2-5; warps 0 and 1 carry
+// the halo link data) own one (row, chunk) pair each and copy it for every
+// component.  vec_plan() gives a thread's plane-independent source offset and
+// its destination in a staged component, or dst = -1.
+struct VecPlan {
+    int off;  // row * nz + z within a plane
+    int dst;  // hy * TT_PZ + 4 * cq, or -1
+};
+
+__device__ __forceinline__ VecPlan vec_plan(const Geom& g, int j0, int k0, int wy, int wz)
+{
+    VecPlan vp{0, -1};
+    const int p = threadIdx.y * TT_Z + threadIdx.x - 2 * 32;
+    if (p >= 0 && p < TT_HY * TT_NQ) {
+        const int hy = p / TT_NQ, cq = p - hy * TT_NQ;
+        // rows j0-1 .. j0+wy; columns k0-1 .. k0+wz are chunks 0 .. 1 + wz/4
+        if (hy <= wy + 1 && cq <= 1 + (wz >> 2)) {
+            vp.off = wrap_idx(j0 - 1 + hy, g.ny) * g.nz + wrap_idx(k0 - 4 + 4 * cq, g.nz);
+            vp.dst = hy * TT_PZ + 4 * cq;
+        }
+    }
+    return vp;
+}
+
+template <class T, int NS>
+__device__ __forceinline__ void stage_plane_vec(TiledSmem<T, NS>& sm, int b, const Fields<T, 2 * NS + 3>& f,
+                                                const Geom& g, int pi, const VecPlan& vp)
+{
+    static_assert(sizeof(T) == 4, "16-byte staging is for FP32 fields");
+    if (vp.dst >= 0) {
+        const int s = pi * g.syz + vp.off;
+        T* th = &sm.th[b][0][0][0] + vp.dst;
+        T* ph = &sm.ph[b][0][0][0] + vp.dst;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) __pipeline_memcpy_async(th + m * TT_HY * TT_PZ, f.now[2 * NS + m] + s, 16);
+#pragma unroll
+        for (int c = 0; c < 2 * NS; ++c) __pipeline_memcpy_async(ph + c * TT_HY * TT_PZ, f.now[c] + s, 16);
+    }
+    __pipeline_commit();
+}
+
+// Whether the tiled step may stage by 16-byte copies: FP32 fields, periodic z
+// with nz a multiple of 4 (rows and chunk starts on 16-byte boundaries) and
+// every field pointer 16-byte aligned.
+template <class T, int NC>
+inline bool tiled_vec_ok(const Geom& g, const Fields<T, NC>& f)
+{
+    if (sizeof(T) != 4 || g.loz != 0 || g.hiz != g.nz || (g.nz & 3) != 0) return false;
+    for (int c = 0; c < NC; ++c)
+        if ((reinterpret_cast<uintptr_t>(f.now[c]) & 15) != 0) return false;
+    return true;
+}
+
 // One tile: columns (bx*TZ.., by*TY..) of the evolved region, x-planes
 // [bz*chunk, bz*chunk + chunk).  Called by every thread of the CTA.  With DIAG
-// the CTA's energy and |G| sums are written to part[0], part[1].
+// the CTA's energy and |G| sums are written to part[0], part[1].  `vec`
+// selects the 16-byte staging (only where tiled_vec_ok holds); both stagings
+// fill the same shared-memory positions, so the results are bitwise equal.
 template <class T, int NS, bool DIAG>
 __device__ __forceinline__ void tiled_tile(TiledSmem<T, NS>& sm, const Geom& g, const Fields<T, 2 * NS + 3>& f,
                                            const StepCoefT<T>& c, const Charges<T>& ch, const DiagOut& d, int bx,
-                                           int by, int bz, int chunk, double* part)
+                                           int by, int bz, int chunk, double* part, bool vec)
 {
     using TR = Trig<T>;
     using LI = LinkIdx<NS>;
@@ -165,9 +231,17 @@ __device__ __forceinline__ void tiled_tile(TiledSmem<T, NS>& sm, const Geom& g, 
 #pragma unroll
         for (int cc = 0; cc < 2 * NS; ++cc) vm[cc] = f.now[cc][s];
     }
+    // in-range rows and columns of the tile
+    const int wy = min(TT_Y, g.hiy - j0), wz = min(TT_Z, g.hiz - k0);
+    VecPlan vp{0, -1};
+    if (vec) vp = vec_plan(g, j0, k0, wy, wz);
+    auto stage = [&](int b, int pi) {
+        if (vec) stage_plane_vec<T, NS>(sm, b, f, g, pi, vp);
+        else stage_plane<T, NS>(sm, b, f, g, pi, j0, k0, wy, wz);
+    };
     int cur = 0;
-    stage_plane<T, NS>(sm, 0, f, g, wrap_idx(ib, g.nx), j0, k0);
-    stage_plane<T, NS>(sm, 1, f, g, wrap_idx(ib + 1, g.nx), j0, k0);
+    stage(0, wrap_idx(ib, g.nx));
+    stage(1, wrap_idx(ib + 1, g.nx));
 
     double e_acc = 0.0, g_acc = 0.0;
 
@@ -180,7 +254,7 @@ __device__ __forceinline__ void tiled_tile(TiledSmem<T, NS>& sm, const Geom& g, 
         const int nn = nxt == 2 ? 0 : nxt + 1;
         __pipeline_wait_prior(0);  // planes i and i+1 have landed
         __syncthreads();
-        if (i + 1 < ie) stage_plane<T, NS>(sm, nn, f, g, wrap_idx(i + 2, g.nx), j0, k0);
+        if (i + 1 < ie) stage(nn, wrap_idx(i + 2, g.nx));
         // the own site's level n-1, loaded now so that the link phase covers
         // the memory latency
         const int s = (i * g.ny + jj) * g.nz + kk;
@@ -198,10 +272,10 @@ __device__ __forceinline__ void tiled_tile(TiledSmem<T, NS>& sm, const Geom& g, 
         // ---- link data of one staged position (ly, lz) of the current plane
         auto links = [&](int ly, int lz, T* cyq, T* syq, T* czq, T* szq, T& sxy, T& sxz, T& syz, T* cxq, T* sxq,
                          T* cpo) {
-            const T tx = sm.th[cur][0][ly][lz], tyv = sm.th[cur][1][ly][lz], tzv = sm.th[cur][2][ly][lz];
-            const T tyxp = sm.th[nxt][1][ly][lz], tzxp = sm.th[nxt][2][ly][lz];
-            const T txyp = sm.th[cur][0][ly + 1][lz], tzyp = sm.th[cur][2][ly + 1][lz];
-            const T txzp = sm.th[cur][0][ly][lz + 1], tyzp = sm.th[cur][1][ly][lz + 1];
+            const T tx = sm.th[cur][0][ly][lz + TT_C0], tyv = sm.th[cur][1][ly][lz + TT_C0], tzv = sm.th[cur][2][ly][lz + TT_C0];
+            const T tyxp = sm.th[nxt][1][ly][lz + TT_C0], tzxp = sm.th[nxt][2][ly][lz + TT_C0];
+            const T txyp = sm.th[cur][0][ly + 1][lz + TT_C0], tzyp = sm.th[cur][2][ly + 1][lz + TT_C0];
+            const T txzp = sm.th[cur][0][ly][lz + 1 + TT_C0], tyzp = sm.th[cur][1][ly][lz + 1 + TT_C0];
             T c1, s1;
             TR::sincos(tyv, &s1, &c1);
 #pragma unroll
@@ -257,8 +331,8 @@ __device__ __forceinline__ void tiled_tile(TiledSmem<T, NS>& sm, const Geom& g, 
 
         T v[2 * NS];
 #pragma unroll
-        for (int cc = 0; cc < 2 * NS; ++cc) v[cc] = sm.ph[cur][cc][hy][hz];
-        const T tx = sm.th[cur][0][hy][hz], tyv = sm.th[cur][1][hy][hz], tzv = sm.th[cur][2][hy][hz];
+        for (int cc = 0; cc < 2 * NS; ++cc) v[cc] = sm.ph[cur][cc][hy][hz + TT_C0];
+        const T tx = sm.th[cur][0][hy][hz + TT_C0], tyv = sm.th[cur][1][hy][hz + TT_C0], tzv = sm.th[cur][2][hy][hz + TT_C0];
         if (active) {
             const T sPxy_ym = sm.L[LI::pxy][hy - 1][hz], sPyz_ym = sm.L[LI::pyz][hy - 1][hz];
             const T sPxz_zm = sm.L[LI::pxz][hy][hz - 1], sPyz_zm = sm.L[LI::pyz][hy][hz - 1];
@@ -279,11 +353,11 @@ __device__ __forceinline__ void tiled_tile(TiledSmem<T, NS>& sm, const Geom& g, 
 #pragma unroll
             for (int q = 0; q < NS; ++q) {
                 const T re = v[2 * q], imv = v[2 * q + 1];
-                const T rexp = sm.ph[nxt][2 * q][hy][hz], imxp = sm.ph[nxt][2 * q + 1][hy][hz];
-                const T reyp = sm.ph[cur][2 * q][hy + 1][hz], imyp = sm.ph[cur][2 * q + 1][hy + 1][hz];
-                const T reym = sm.ph[cur][2 * q][hy - 1][hz], imym = sm.ph[cur][2 * q + 1][hy - 1][hz];
-                const T rezp = sm.ph[cur][2 * q][hy][hz + 1], imzp = sm.ph[cur][2 * q + 1][hy][hz + 1];
-                const T rezm = sm.ph[cur][2 * q][hy][hz - 1], imzm = sm.ph[cur][2 * q + 1][hy][hz - 1];
+                const T rexp = sm.ph[nxt][2 * q][hy][hz + TT_C0], imxp = sm.ph[nxt][2 * q + 1][hy][hz + TT_C0];
+                const T reyp = sm.ph[cur][2 * q][hy + 1][hz + TT_C0], imyp = sm.ph[cur][2 * q + 1][hy + 1][hz + TT_C0];
+                const T reym = sm.ph[cur][2 * q][hy - 1][hz + TT_C0], imym = sm.ph[cur][2 * q + 1][hy - 1][hz + TT_C0];
+                const T rezp = sm.ph[cur][2 * q][hy][hz + 1 + TT_C0], imzp = sm.ph[cur][2 * q + 1][hy][hz + 1 + TT_C0];
+                const T rezm = sm.ph[cur][2 * q][hy][hz - 1 + TT_C0], imzm = sm.ph[cur][2 * q + 1][hy][hz - 1 + TT_C0];
                 const T rexm = vm[2 * q], imxm = vm[2 * q + 1];
                 const T cym = sm.L[LI::cy(q)][hy - 1][hz], sym = sm.L[LI::sy(q)][hy - 1][hz];
                 const T czm = sm.L[LI::cz(q)][hy][hz - 1], szm = sm.L[LI::sz(q)][hy][hz - 1];
@@ -342,7 +416,7 @@ __device__ __forceinline__ void tiled_tile(TiledSmem<T, NS>& sm, const Geom& g, 
             }
             T divNow = 0;
             if (DIAG || d.store_div) {
-                const T tym = sm.th[cur][1][hy - 1][hz], tzm = sm.th[cur][2][hy][hz - 1];
+                const T tym = sm.th[cur][1][hy - 1][hz + TT_C0], tzm = sm.th[cur][2][hy][hz - 1 + TT_C0];
                 divNow = (tx - txm_prev) * c.inv_dx2 + (tyv - tym) * c.inv_dy2 + (tzv - tzm) * c.inv_dz2;
             }
             if constexpr (DIAG) {
@@ -427,13 +501,13 @@ __device__ __forceinline__ void tiled_tile(TiledSmem<T, NS>& sm, const Geom& g, 
 template <class T, int NS, bool DIAG>
 __global__ void __launch_bounds__(TT_THREADS, NS == 1 ? 4 : 3)
 tiled_step_kernel(const Geom g, const Fields<T, 2 * NS + 3> f, const StepCoefT<T> c, const Charges<T> ch,
-                  const DiagOut d, const int chunk)
+                  const DiagOut d, const int chunk, const int vec)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TiledSmem<T, NS>& sm = *reinterpret_cast<TiledSmem<T, NS>*>(smem_raw);
     const int blk = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
     tiled_tile<T, NS, DIAG>(sm, g, f, c, ch, d, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, chunk,
-                            DIAG ? d.partials + 2 * blk : nullptr);
+                            DIAG ? d.partials + 2 * blk : nullptr, vec != 0);
 }
 
 inline dim3 tiled_grid(const Geom& g, int chunk)
@@ -449,7 +523,7 @@ inline int small_int_power(double q)
 
 template <class T, int NS>
 cudaError_t launch_tiled_t(const Geom& g, const Fields<T, 2 * NS + 3>& f, const StepCoef& c64, const DiagOut& d,
-                           bool diag, int chunk, cudaStream_t st)
+                           bool diag, int chunk, cudaStream_t st, bool allow_vec = true)
 {
     const StepCoefT<T> c = coef_as<T>(c64);
     Charges<T> ch;
@@ -472,8 +546,9 @@ cudaError_t launch_tiled_t(const Geom& g, const Fields<T, 2 * NS + 3>& f, const 
     }
     const dim3 grid = tiled_grid(g, chunk);
     const dim3 block(TT_Z, TT_Y);
-    if (diag) tiled_step_kernel<T, NS, true><<<grid, block, smem, st>>>(g, f, c, ch, d, chunk);
-    else tiled_step_kernel<T, NS, false><<<grid, block, smem, st>>>(g, f, c, ch, d, chunk);
+    const int vec = allow_vec && tiled_vec_ok(g, f) ? 1 : 0;
+    if (diag) tiled_step_kernel<T, NS, true><<<grid, block, smem, st>>>(g, f, c, ch, d, chunk, vec);
+    else tiled_step_kernel<T, NS, false><<<grid, block, smem, st>>>(g, f, c, ch, d, chunk, vec);
     return cudaGetLastError();
 }
 

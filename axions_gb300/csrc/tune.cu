@@ -94,7 +94,7 @@ int lat_autotune(lat_handle* h, int32_t trial_steps, lat_tuning* out)
         set_error("lat_autotune: bad argument");
         return LAT_ERR_INVALID;
     }
-    if (h->elem != 4 || h->p.kernel_variant != 0) {  // only the tiled FP32 step has a chunk
+    if (h->elem != 4 || h->p.kernel_variant == 1) {  // only the tiled FP32 step has a chunk
         if (out) {
             out->chunk = h->chunk;
             out->candidates = 0;

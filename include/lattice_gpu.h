@@ -121,7 +121,9 @@ typedef struct lat_params {
     double scaling;        /* scale-factor power; friction = alpha*scaling/tau           */
     double tau0;           /* conformal time at step 0: tau = tau0 + TimeStep*dt (=1)    */
     int32_t energy_form;   /* LAT_ENERGY_*                                               */
-    int32_t kernel_variant;/* 0: default kernels; 1: one-pass FP64 stencil (for checks)  */
+    int32_t kernel_variant;/* 0: default kernels; 1: one-pass stencils (for checks);
+                              2 (FP32): the tiled step staging one element per copy
+                              instead of 16-byte row chunks (for checks)                 */
     int32_t bc_z;          /* LAT_BCZ_*: boundary of the z axis (0: the same as bc)        */
     int32_t reserved_i;
     double reserved[3];

@@ -295,13 +295,16 @@ def test_strict_non_power_of_two_spacing(lattice_mod, oracle_mod):
 
 
 @pytest.mark.parametrize("bc", [0, 1])
-def test_fp32_tiled_kernel_odd_sizes(lattice_mod, bc):
+@pytest.mark.parametrize("sides", [(70, 29, 45), (70, 29, 44), (10, 3, 4)])
+def test_fp32_tiled_kernel_odd_sizes(lattice_mod, bc, sides):
     """The tiled FP32 kernel (x-march, shared-memory staging) on sides that are
     not multiples of its tile (32 x 8) or of its x-chunk, periodic and fixed
     boundaries: it must track the FP64 path, and the one-pass FP32 kernel, to
-    FP32 accuracy."""
+    FP32 accuracy.  Periodic nz = 44 and nz = 4 take the 16-byte staging; the
+    10 x 3 x 4 lattice is narrower than the tile on both y and z."""
     from axions_gb300.params import ENERGY_EVOLUTION, F32, make_params
-    p = make_params(0, nx=70, ny=29, nz=45, d=0.5, dt=0.1, lam=2.0, g=1.0, damped_nt=3, dampFac=0.5, alpha=3.0,
+    nx, ny, nz = sides
+    p = make_params(0, nx=nx, ny=ny, nz=nz, d=0.5, dt=0.1, lam=2.0, g=1.0, damped_nt=3, dampFac=0.5, alpha=3.0,
                     energy_form=ENERGY_EVOLUTION, bc=bc)
     ic = lattice_mod.random_phase_ic(p, 23)
     res = {}
@@ -351,3 +354,35 @@ def test_fp32_tiled_moore(lattice_mod, bc, charges, current):
         assert l2 < 3e-6 and mx < 3e-5, (name, mx, l2)
         np.testing.assert_allclose([x[1] for x in d], [x[1] for x in res["f64"][1]], rtol=1e-5)
         np.testing.assert_allclose([x[2] for x in d], [x[2] for x in res["f64"][1]], rtol=1e-4)
+
+
+@pytest.mark.parametrize("model", [0, 1])
+@pytest.mark.parametrize("sides", [(70, 29, 44), (33, 17, 32), (40, 12, 100), (24, 20, 36), (10, 3, 4), (9, 5, 8)])
+def test_fp32_tiled_vector_staging_is_bitwise_the_element_staging(lattice_mod, model, sides):
+    """With periodic z and nz a multiple of 4 the tiled FP32 step stages its
+    planes in 16-byte row chunks; kernel_variant 2 stages one element per
+    copy.  Both fill the same shared-memory positions and the arithmetic is
+    the same, so fields and diagnostics are bitwise equal.  The sides cover a
+    partial last z tile, one tile wrapping at both ends, four tiles, a right
+    edge cut to the lattice, and lattices narrower than the tile (nz = 4,
+    ny = 3), whose halo indices wrap within one period."""
+    from axions_gb300.params import ENERGY_EVOLUTION, F32, MODEL_MOORE, make_params
+    nx, ny, nz = sides
+    if model == 0:
+        p = make_params(0, nx=nx, ny=ny, nz=nz, d=0.5, dt=0.1, lam=2.0, g=1.0, damped_nt=3, dampFac=0.5, alpha=3.0,
+                        energy_form=ENERGY_EVOLUTION, precision=F32)
+    else:
+        p = make_params(MODEL_MOORE, nx=nx, ny=ny, nz=nz, d=0.5, dt=0.1, lam=2.0, lambda2=2.0, lambda12=0.5, eta=1.0,
+                        eta2=1.0, q1=2.0, q2=1.0, g=1.0, damped_nt=3, dampFac=0.5, alpha=3.0,
+                        energy_form=ENERGY_EVOLUTION, precision=F32)
+    ic = lattice_mod.random_phase_ic(p, 31, independent=model == 1)
+    out = []
+    for variant in (0, 2):
+        q = p.copy()
+        q.kernel_variant = variant
+        with lattice_mod.Lattice(q) as lat:
+            lat.set_state(ic, ic, 0)
+            d = lat.advance(11, diag_every=3)
+            out.append((lat.get_slots(), d))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert out[0][1] == out[1][1]
