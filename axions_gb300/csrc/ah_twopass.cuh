@@ -70,13 +70,13 @@ __global__ void __launch_bounds__(BLOCK) ah_links_kernel(const Geom g, const dou
     const double txyp = TX[s + n.yp], tzyp = TZ[s + n.yp];
     const double txzp = TX[s + n.zp], tyzp = TY[s + n.zp];
     double sv, cv;
-    sincos(tx, &sv, &cv);
+    dsincos(tx, &sv, &cv);
     L[L_CX * N + s] = cv;
     L[L_SX * N + s] = sv;
-    sincos(ty, &sv, &cv);
+    dsincos(ty, &sv, &cv);
     L[L_CY * N + s] = cv;
     L[L_SY * N + s] = sv;
-    sincos(tz, &sv, &cv);
+    dsincos(tz, &sv, &cv);
     L[L_CZ * N + s] = cv;
     L[L_SZ * N + s] = sv;
     // plaquette angles, summed in the reference's order (mpi_evolution.cpp:471-487)
@@ -84,24 +84,24 @@ __global__ void __launch_bounds__(BLOCK) ah_links_kernel(const Geom g, const dou
     const double Pxz = tx + tzxp - txzp - tz;
     const double Pyz = ty + tzyp - tyzp - tz;
     if constexpr (DIAG) {
-        sincos(Pxy, &sv, &cv);
+        dsincos(Pxy, &sv, &cv);
         L[L_PXY * N + s] = sv;
         L[L_CPXY * N + s] = cv;
-        sincos(Pxz, &sv, &cv);
+        dsincos(Pxz, &sv, &cv);
         L[L_PXZ * N + s] = sv;
         L[L_CPXZ * N + s] = cv;
-        sincos(Pyz, &sv, &cv);
+        dsincos(Pyz, &sv, &cv);
         L[L_PYZ * N + s] = sv;
         L[L_CPYZ * N + s] = cv;
     } else {
-        L[L_PXY * N + s] = sin(Pxy);
-        L[L_PXZ * N + s] = sin(Pxz);
-        L[L_PYZ * N + s] = sin(Pyz);
+        L[L_PXY * N + s] = dsin(Pxy);
+        L[L_PXZ * N + s] = dsin(Pxz);
+        L[L_PYZ * N + s] = dsin(Pyz);
     }
     if constexpr (STRICT) {
-        L[L_PYX * N + s] = sin(ty + txyp - tyxp - tx);
-        L[L_PZX * N + s] = sin(tz + txzp - tzxp - tx);
-        L[L_PZY * N + s] = sin(tz + tyzp - tzyp - ty);
+        L[L_PYX * N + s] = dsin(ty + txyp - tyxp - tx);
+        L[L_PZX * N + s] = dsin(tz + txzp - tzxp - tx);
+        L[L_PZY * N + s] = dsin(tz + tyzp - tzyp - ty);
     }
 }
 

@@ -1,6 +1,10 @@
-// Deterministic reduction of per-block diagnostic partials and the
-// double <-> float conversions of the FP32 path.
-#include "lattice_internal.cuh"
+// Deterministic reduction of per-block diagnostic partials, the
+// double <-> float conversions of the FP32 path, and lat_dtrig_eval (the FP64
+// step's sine and cosine on given arguments, for checks).
+#include <string>
+
+#include "dtrig.cuh"
+#include "lattice_handle.hpp"
 
 namespace lat {
 
@@ -51,6 +55,21 @@ __global__ void f2d_kernel(const float* __restrict__ in, double* __restrict__ ou
         out[q] = (double)in[q];
 }
 
+// the FP64 step's dsin/dsincos and CUDA's sin/cos on the same arguments
+__global__ void dtrig_kernel(const double* __restrict__ x, int64_t n, double* __restrict__ out)
+{
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const double v = x[q];
+        double s, c;
+        dsincos(v, &s, &c);
+        out[q] = dsin(v);
+        out[n + q] = s;
+        out[2 * n + q] = c;
+        out[3 * n + q] = ::sin(v);
+        out[4 * n + q] = ::cos(v);
+    }
+}
+
 inline unsigned grid_for(int64_t n)
 {
     int64_t b = (n + 255) / 256;
@@ -79,3 +98,28 @@ cudaError_t launch_f2d(const float* in, double* out, int64_t n, cudaStream_t st)
 }
 
 }  // namespace lat
+
+using namespace lat;
+
+extern "C" int lat_dtrig_eval(const double* x, int64_t n, double* out)
+{
+    if (!x || !out || n < 0 || n > ((int64_t)1 << 26)) {
+        set_error("lat_dtrig_eval: null pointer or n outside [0, 2^26]");
+        return LAT_ERR_INVALID;
+    }
+    if (n == 0) return LAT_OK;
+    double* d = nullptr;
+    cudaError_t e = cudaMalloc((void**)&d, sizeof(double) * 6 * (size_t)n);
+    if (e == cudaSuccess) e = cudaMemcpy(d, x, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        dtrig_kernel<<<grid_for(n), 256>>>(d, n, d + n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + n, sizeof(double) * 5 * (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        set_error(std::string("lat_dtrig_eval: ") + cudaGetErrorString(e));
+        return LAT_ERR_CUDA;
+    }
+    return LAT_OK;
+}

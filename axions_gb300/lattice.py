@@ -32,7 +32,7 @@ EXPORTS = [
     "lat_ah_step_f64_noalloc",
     "lat_batch_create", "lat_batch_destroy", "lat_batch_add", "lat_batch_remove", "lat_batch_size",
     "lat_batch_kernel_launches", "lat_batch_set_chunk", "lat_batch_advance", "lat_batch_take_diags",
-    "lat_random_phase_ic_device", "lat_boost_ic_device", "lat_loop_collision_ic_device", "lat_philox4x32_10", "lat_autotune", "lat_get_tuning", "lat_set_tuning",
+    "lat_random_phase_ic_device", "lat_boost_ic_device", "lat_loop_collision_ic_device", "lat_philox4x32_10", "lat_dtrig_eval", "lat_autotune", "lat_get_tuning", "lat_set_tuning",
     "lat_tune_cache_save", "lat_tune_cache_load", "lat_footprint_bytes",
     "lat_server_create", "lat_server_submit", "lat_server_poll", "lat_server_wait", "lat_server_diags",
     "lat_server_get_stats", "lat_server_destroy",
@@ -118,6 +118,7 @@ def load_library(path: Path | None = None):
     L.lat_boost_ic_device.argtypes = [vp, vp, vp, P(ctypes.c_int64)]
     L.lat_loop_collision_ic_device.argtypes = [vp, vp, vp, P(ctypes.c_int64)]
     L.lat_philox4x32_10.argtypes = [u32p, u32p, u32p]
+    L.lat_dtrig_eval.argtypes = [dp, ctypes.c_int64, dp]
     L.lat_autotune.argtypes = [vp, ctypes.c_int32, P(LatTuning)]
     L.lat_get_tuning.argtypes = [vp, P(LatTuning)]
     L.lat_set_tuning.argtypes = [vp, P(LatTuning)]
@@ -169,6 +170,15 @@ def philox4x32_10(counter, key):
     out = (ctypes.c_uint32 * 4)()
     _check("lat_philox4x32_10", load_library().lat_philox4x32_10(c, k, out))
     return list(out)
+
+
+def dtrig_eval(x):
+    """The FP64 step's sine and cosine at the doubles x, on the current GPU.
+    Returns (sin, sincos_sin, sincos_cos, cuda_sin, cuda_cos) as arrays."""
+    x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+    out = np.empty(5 * x.size, dtype=np.float64)
+    _check("lat_dtrig_eval", load_library().lat_dtrig_eval(_dp(x), x.size, _dp(out)))
+    return tuple(out.reshape(5, x.size))
 
 
 def tune_cache_save(path) -> None:

@@ -366,6 +366,14 @@ int lat_loop_collision_ic_device(lat_handle* h, const lat_string_profile* prof, 
 /* The generator on the host (checks, reproduction of device ICs). */
 int lat_philox4x32_10(const uint32_t counter[4], const uint32_t key[2], uint32_t out[4]);
 
+/* The FP64 step's sine and cosine (a table-driven reduction to |r| <= pi/512,
+ * within about two ulps) evaluated on the current device at n host arguments x, for
+ * checks: out (5*n doubles, host) receives sin(x) from the sine alone, then
+ * sin(x) and cos(x) from the joint sincos, then CUDA's sin(x) and cos(x).
+ * No counterpart in the reference, whose step calls libm's sin and cos
+ * (mpi_evolution.cpp:418-487).  n <= 2^26. */
+int lat_dtrig_eval(const double* x, int64_t n, double* out);
+
 /* ---- tuning of the tiled FP32 step ------------------------------------------------
  * chunk = x-planes each CTA of the tiled FP32 step marches through.  New
  * handles start with the value tuned for their shape in this process (or

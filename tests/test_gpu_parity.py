@@ -5,11 +5,11 @@ Tolerances (FP64 path):
   * fields: normwise, max|d|/max|ref| <= 1e-12 and ||d||_2/||ref||_2 <= 1e-12
     over the whole state, and ||d||_2/||ref||_2 <= 1e-12 for every field
     (component) on its own.  (A single field's largest site difference over its
-    own largest value reaches ~1.1e-12 after 300 chaotic steps: the GPU's
-    sin/cos differ from libm's in the last bit for some arguments, and the
-    dynamics amplify it.)
-    The GPU's sin/cos differ from libm's in the last bit for some arguments, so
-    element-wise equality is not possible; normwise agreement is the bar.
+    own largest value reaches ~1.1e-12 after 300 chaotic steps: the FP64
+    step's table-driven sin/cos differ from libm's in the last bits (at most
+    3 ulps) for some arguments, and the dynamics amplify it.)
+    Element-wise equality is therefore not possible; normwise agreement is the
+    bar.
   * energy and summed Gauss deviation: relative 1e-12 (different summation
     order on top of the above).
   * string detection on identical fields: bit-exact (same double operations,
