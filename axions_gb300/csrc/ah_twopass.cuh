@@ -30,12 +30,27 @@ enum LinkSlot {
     L_COUNT
 };
 
+// x * p for an exact power of two p = 2^e.  When x and the result are normal
+// numbers the product only moves the exponent field, which integer
+// instructions do off the FP64 pipe (1/64 of the FP32 rate on GB300); zeros,
+// subnormals, Inf/NaN and results outside the normal range take the FP64
+// multiply.  Both give the same double.
+__device__ __forceinline__ double mul_pow2(double x, double p)
+{
+    const long long bx = __double_as_longlong(x);
+    const int ex = (int)(bx >> 52) & 0x7ff;
+    const int e = ((int)(__double_as_longlong(p) >> 52) & 0x7ff) - 1023;
+    const int ey = ex + e;
+    if (ex == 0 || ex == 0x7ff || ey <= 0 || ey >= 0x7ff) return x * p;
+    return __longlong_as_double(bx + ((long long)e << 52));
+}
+
 // a / b where b = spacing^2 or spacing: exact reciprocal multiply when every
 // spacing is a power of two (then a*(1/b) == a/b for all a), else IEEE divide.
 template <bool RECIP>
 __device__ __forceinline__ double sdiv(double a, double b, double inv_b)
 {
-    if constexpr (RECIP) return a * inv_b;
+    if constexpr (RECIP) return mul_pow2(a, inv_b);
     else return a / b;
 }
 
@@ -155,16 +170,17 @@ __global__ void __launch_bounds__(BLOCK) ah_update_kernel(const Geom g, const Fi
             sPzy_m = -L[L_PYZ * N + sym_];
         }
 
+        const double twop0 = mul_pow2(p0, 2.0), twop1 = mul_pow2(p1, 2.0);  // 2 * p0, 2 * p1
         const double phiMagSqr = p0 * p0 + p1 * p1;
         const double pot = c.halfLambda * (phiMagSqr - c.etaSq);
 
         // covariant Laplacian (mpi_evolution.cpp:418-428), c = +1 then c = -1
-        double lap0 = sdiv<RECIP>(cx * p0xp + sx * p1xp - 2 * p0 + cxm * p0xm - sxm_ * p1xm, c.dx2, c.inv_dx2)
-                    + sdiv<RECIP>(cy * p0yp + sy * p1yp - 2 * p0 + cym * p0ym - sym * p1ym, c.dy2, c.inv_dy2)
-                    + sdiv<RECIP>(cz * p0zp + sz * p1zp - 2 * p0 + czm * p0zm - szm_ * p1zm, c.dz2, c.inv_dz2);
-        double lap1 = sdiv<RECIP>(cx * p1xp - sx * p0xp - 2 * p1 + cxm * p1xm + sxm_ * p0xm, c.dx2, c.inv_dx2)
-                    + sdiv<RECIP>(cy * p1yp - sy * p0yp - 2 * p1 + cym * p1ym + sym * p0ym, c.dy2, c.inv_dy2)
-                    + sdiv<RECIP>(cz * p1zp - sz * p0zp - 2 * p1 + czm * p1zm + szm_ * p0zm, c.dz2, c.inv_dz2);
+        double lap0 = sdiv<RECIP>(cx * p0xp + sx * p1xp - twop0 + cxm * p0xm - sxm_ * p1xm, c.dx2, c.inv_dx2)
+                    + sdiv<RECIP>(cy * p0yp + sy * p1yp - twop0 + cym * p0ym - sym * p1ym, c.dy2, c.inv_dy2)
+                    + sdiv<RECIP>(cz * p0zp + sz * p1zp - twop0 + czm * p0zm - szm_ * p1zm, c.dz2, c.inv_dz2);
+        double lap1 = sdiv<RECIP>(cx * p1xp - sx * p0xp - twop1 + cxm * p1xm + sxm_ * p0xm, c.dx2, c.inv_dx2)
+                    + sdiv<RECIP>(cy * p1yp - sy * p0yp - twop1 + cym * p1ym + sym * p0ym, c.dy2, c.inv_dy2)
+                    + sdiv<RECIP>(cz * p1zp - sz * p0zp - twop1 + czm * p1zm + szm_ * p0zm, c.dz2, c.inv_dz2);
         double tt0 = lap0 - pot * p0;
         double tt1 = lap1 - pot * p1;
         if (c.fric != 0) {
@@ -243,11 +259,11 @@ __global__ void __launch_bounds__(BLOCK) ah_update_kernel(const Geom g, const Fi
         if (d.store_div) reinterpret_cast<double*>(d.divbuf)[s] = divNow;
 
         if (d.write) {  // in-place update of the past slot (mpi_evolution.cpp:432,499-501)
-            f.past[0][s] = 2 * p0 - q0 + c.dt2 * tt0;
-            f.past[1][s] = 2 * p1 - q1 + c.dt2 * tt1;
-            f.past[2][s] = 2 * tx - qx + c.dt2 * ttx;
-            f.past[3][s] = 2 * ty - qy + c.dt2 * tty;
-            f.past[4][s] = 2 * tz - qz + c.dt2 * ttz;
+            f.past[0][s] = twop0 - q0 + c.dt2 * tt0;
+            f.past[1][s] = twop1 - q1 + c.dt2 * tt1;
+            f.past[2][s] = mul_pow2(tx, 2.0) - qx + c.dt2 * ttx;
+            f.past[3][s] = mul_pow2(ty, 2.0) - qy + c.dt2 * tty;
+            f.past[4][s] = mul_pow2(tz, 2.0) - qz + c.dt2 * ttz;
         }
     }
     if constexpr (DIAG) block_sum2_store(e_site, g_site, d.partials);
