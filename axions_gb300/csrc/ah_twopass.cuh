@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(BLOCK) ah_links_kernel(const Geom g, const dou
 }
 
 template <bool STRICT, bool DIAG, bool RECIP>
-__global__ void __launch_bounds__(BLOCK) ah_update_kernel(const Geom g, const Fields<double, 5> f,
+__global__ void __launch_bounds__(BLOCK, 2) ah_update_kernel(const Geom g, const Fields<double, 5> f,
                                                           const double* __restrict__ L, const int N, const StepCoef c,
                                                           const DiagOut d)
 {
@@ -219,7 +219,9 @@ __global__ void __launch_bounds__(BLOCK) ah_update_kernel(const Geom g, const Fi
 
         if constexpr (DIAG) {
             // energy density and Gauss deviation of the now level
-            // (evolution.cpp:322-334,377-427; mpi_evolution.cpp:509-532)
+            // (evolution.cpp:322-334,377-427; mpi_evolution.cpp:509-532).  Each
+            // divisor other than dt occurs once per site, so cdiv's host
+            // reciprocal replaces the division's own (the same doubles).
             const double cPxy = L[L_CPXY * N + s], cPxz = L[L_CPXZ * N + s], cPyz = L[L_CPYZ * N + s];
             const double pt0 = tdiv<STRICT>(p0 - q0, c.dt, c.inv_dt);
             const double pt1 = tdiv<STRICT>(p1 - q1, c.dt, c.inv_dt);
@@ -233,18 +235,20 @@ __global__ void __launch_bounds__(BLOCK) ah_update_kernel(const Geom g, const Fi
             if (d.energy_form == LAT_ENERGY_MPI) {
                 const double a0 = (tx - qx) / c.dt, a1 = (ty - qy) / c.dt, a2 = (tz - qz) / c.dt;
                 tdc = 0.5 * (a0 * a0 + a1 * a1 + a2 * a2);
-                fc = (1 - cPxy) / c.gxy2 + (1 - cPxz) / c.gxz2 + (1 - cPyz) / c.gyz2;
+                fc = cdiv(1 - cPxy, c.gxy2, c.inv_gxy2) + cdiv(1 - cPxz, c.gxz2, c.inv_gxz2)
+                   + cdiv(1 - cPyz, c.gyz2, c.inv_gyz2);
             }
             if (c.g != 0) {
                 const double divPast = reinterpret_cast<const double*>(d.divbuf)[s];
                 const double divThetat = (divNow - divPast) / c.dt;
-                gauss = divThetat / c.g - c.twog * (p1 * pt0 - p0 * pt1);
+                gauss = cdiv(divThetat, c.g, c.inv_g) - c.twog * (p1 * pt0 - p0 * pt1);
                 if (d.energy_form != LAT_ENERGY_MPI) {
-                    const double a0 = (tx - qx) / c.gdtdx, a1 = (ty - qy) / c.gdtdy, a2 = (tz - qz) / c.gdtdz;
+                    const double a0 = cdiv(tx - qx, c.gdtdx, c.inv_gdtdx), a1 = cdiv(ty - qy, c.gdtdy, c.inv_gdtdy),
+                                 a2 = cdiv(tz - qz, c.gdtdz, c.inv_gdtdz);
                     tdc = 0.5 * (a0 * a0 + a1 * a1 + a2 * a2);
-                    const double Fxy = (1 - cPxy) / c.gxy2;
-                    const double Fxz = (1 - cPxz) / c.gxz2;
-                    const double Fyz = (1 - cPyz) / c.gyz2;
+                    const double Fxy = cdiv(1 - cPxy, c.gxy2, c.inv_gxy2);
+                    const double Fxz = cdiv(1 - cPxz, c.gxz2, c.inv_gxz2);
+                    const double Fyz = cdiv(1 - cPyz, c.gyz2, c.inv_gyz2);
                     fc = Fxy + Fxz + Fyz;
                 }
             }
