@@ -54,13 +54,15 @@ __device__ __forceinline__ double sdiv(double a, double b, double inv_b)
     else return a / b;
 }
 
-// a / dt.  STRICT: IEEE divide.  Fast: q = a*r corrected by one residual step
-// (Markstein), which returns the correctly rounded quotient except in rare
-// cases where it is one ulp off.
+// a / dt.  STRICT: IEEE divide; a zero dividend (every site of the first step
+// from an initial condition with equal levels) returns a * (1/b), the same
+// +-0, instead of entering the division's slow path.  Fast: q = a*r corrected
+// by one residual step (Markstein), which returns the correctly rounded
+// quotient except in rare cases where it is one ulp off.
 template <bool STRICT>
 __device__ __forceinline__ double tdiv(double a, double b, double inv_b)
 {
-    if constexpr (STRICT) return a / b;
+    if constexpr (STRICT) return is_zero(a) ? a * inv_b : a / b;
     else {
         const double q = a * inv_b;
         const double r = fma(-q, b, a);
@@ -233,14 +235,15 @@ __global__ void __launch_bounds__(BLOCK, 2) ah_update_kernel(const Geom g, const
             const double pz1 = sdiv<RECIP>(p1 - czm * p1zm - szm_ * p0zm, c.dz, c.inv_dz);
             double tdc = 0, fc = 0, gauss = 0;
             if (d.energy_form == LAT_ENERGY_MPI) {
-                const double a0 = (tx - qx) / c.dt, a1 = (ty - qy) / c.dt, a2 = (tz - qz) / c.dt;
+                const double a0 = tdiv<true>(tx - qx, c.dt, c.inv_dt), a1 = tdiv<true>(ty - qy, c.dt, c.inv_dt),
+                             a2 = tdiv<true>(tz - qz, c.dt, c.inv_dt);
                 tdc = 0.5 * (a0 * a0 + a1 * a1 + a2 * a2);
                 fc = cdiv(1 - cPxy, c.gxy2, c.inv_gxy2) + cdiv(1 - cPxz, c.gxz2, c.inv_gxz2)
                    + cdiv(1 - cPyz, c.gyz2, c.inv_gyz2);
             }
             if (c.g != 0) {
                 const double divPast = reinterpret_cast<const double*>(d.divbuf)[s];
-                const double divThetat = (divNow - divPast) / c.dt;
+                const double divThetat = tdiv<true>(divNow - divPast, c.dt, c.inv_dt);
                 gauss = cdiv(divThetat, c.g, c.inv_g) - c.twog * (p1 * pt0 - p0 * pt1);
                 if (d.energy_form != LAT_ENERGY_MPI) {
                     const double a0 = cdiv(tx - qx, c.gdtdx, c.inv_gdtdx), a1 = cdiv(ty - qy, c.gdtdy, c.inv_gdtdy),

@@ -49,15 +49,19 @@ struct Trig<float> {
 // (Markstein's theorem; P. Markstein, IBM J. Res. Dev. 34(1), 1990, and the
 // Handbook of Floating-Point Arithmetic, ch. 4).  So the double is the IEEE
 // quotient, at five FP64 instructions instead of a full division's reciprocal
-// refinement.  |a| or |b| outside [2^-400, 2^401) (zeros, subnormals,
-// Inf/NaN, and wherever quotient or residual could leave the normal range)
-// take the IEEE division.
+// refinement.  A zero a returns a*y (the IEEE quotient +-0); otherwise |a|
+// or |b| outside [2^-400, 2^401) (subnormals, Inf/NaN, and wherever quotient
+// or residual could leave the normal range) take the IEEE division.
+__device__ __forceinline__ bool is_zero(double a) { return (__double_as_longlong(a) << 1) == 0; }
+
 __device__ __forceinline__ double cdiv(double a, double b, double y)
 {
     constexpr unsigned lo = 1023 - 400, span = 800;  // biased exponents lo .. lo + span
     const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7ffu;
     const unsigned eb = ((unsigned)__double2hiint(b) >> 20) & 0x7ffu;
-    if (ea - lo > span || eb - lo > span) return a / b;
+    if (eb - lo > span) return a / b;
+    if (is_zero(a)) return __dmul_rn(a, y);
+    if (ea - lo > span) return a / b;
     double q = __dmul_rn(a, y);
     q = __fma_rn(__fma_rn(-q, b, a), y, q);
     return __fma_rn(__fma_rn(-q, b, a), y, q);
