@@ -350,9 +350,10 @@ def ensemble_jobs(njobs: int, n: int):
 def measure_ensemble(njobs: int, n: int, steps: int, diag_every: int, tick: int):
     """Runs/hour of an ensemble: batched (all lattices in the same launches,
     one CUDA graph per tick) against the same jobs run one after another
-    through the single-lattice path.  Both are timed twice: stepping only
-    (state resident) and end to end (host IC generation, upload, stepping,
-    diagnostics, download of the final fields)."""
+    through the single-lattice path, in the same FP32 form and (sampled) in
+    the plain FP64 form.  Each is timed twice: stepping only (state resident)
+    and end to end (IC generation, stepping, diagnostics, download of the
+    final fields)."""
     import numpy as np
     import torch
 
@@ -413,6 +414,30 @@ def measure_ensemble(njobs: int, n: int, steps: int, diag_every: int, tick: int)
     })
     out["speedup"] = out["batched"]["runs_per_hour"] / out["sequential"]["runs_per_hour"]
     out["speedup_e2e"] = out["batched"]["runs_per_hour_e2e"] / out["sequential"]["runs_per_hour_e2e"]
+    # The same jobs run one after another through the plain path (FP64 strict,
+    # the form the FP32/batched forms are built beside), sampled on two jobs.
+    t_step = t_total = 0.0
+    sampled = jobs[:2]
+    for p, seed in sampled:
+        q = p.copy()
+        q.precision = 0
+        t0 = time.perf_counter()
+        lat = lattice.Lattice(q)
+        lat.random_phase_ic_device(seed)
+        torch.cuda.synchronize()
+        s0 = time.perf_counter()
+        lat.advance(steps, diag_every)
+        t_step += time.perf_counter() - s0
+        lat.get_state()
+        lat.close()
+        t_total += time.perf_counter() - t0
+    if sampled:
+        k = len(sampled)
+        out["sequential_plain_f64"] = {"runs_per_hour": k / t_step * 3600, "runs_per_hour_e2e": k / t_total * 3600,
+                                       "sampled_runs": k, "precision": "f64 strict (the plain path)"}
+        out["speedup_vs_plain_f64"] = out["batched"]["runs_per_hour"] / out["sequential_plain_f64"]["runs_per_hour"]
+        out["speedup_vs_plain_f64_e2e"] = (out["batched"]["runs_per_hour_e2e"]
+                                           / out["sequential_plain_f64"]["runs_per_hour_e2e"])
     # The reference's own way to run an ensemble: one program invocation per
     # job (run_mpi_evol.sh, submit_job.sh).  Timed with the drop-in program on
     # a few jobs; each invocation creates its CUDA context, draws its mt19937
