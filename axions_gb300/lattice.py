@@ -303,11 +303,19 @@ class Lattice:
         past = np.ascontiguousarray(st[:, time_step % 2, :])
         self.set_state(now, past, time_step)
 
-    def get_state(self):
-        now = np.empty((self.ncomp, self.N), dtype=np.float64)
-        past = np.empty((self.ncomp, self.N), dtype=np.float64)
-        _check("lat_get_state", self.L.lat_get_state(self.h, _dp(now), _dp(past)))
-        return now, past
+    def get_state(self, now: np.ndarray | None = None, past: np.ndarray | None = None):
+        """Download (now, past) as float64 arrays of shape (ncomp, N).  Arrays
+        passed in (C-contiguous float64 of that shape, e.g. views of pinned
+        buffers reused across calls) receive the levels; others are allocated."""
+        out = []
+        for a in (now, past):
+            if a is None:
+                a = np.empty((self.ncomp, self.N), dtype=np.float64)
+            elif a.dtype != np.float64 or not a.flags.c_contiguous or a.size != self.ncomp * self.N:
+                raise ValueError("get_state: output arrays must be C-contiguous float64 of ncomp*N elements")
+            out.append(a)
+        _check("lat_get_state", self.L.lat_get_state(self.h, _dp(out[0]), _dp(out[1])))
+        return out[0].reshape(self.ncomp, self.N), out[1].reshape(self.ncomp, self.N)
 
     def get_slots(self) -> np.ndarray:
         n = self.time_step
