@@ -26,7 +26,7 @@ EXPORTS = [
     "lat_version", "lat_last_error", "lat_params_init", "lat_random_phase_ic", "lat_create", "lat_destroy",
     "lat_set_stream", "lat_get_params", "lat_num_components", "lat_time_step", "lat_device_bytes",
     "lat_kernel_launches",
-    "lat_set_state", "lat_get_state", "lat_step", "lat_step_diag", "lat_advance", "lat_diagnostics",
+    "lat_set_state", "lat_get_state", "lat_step", "lat_step_diag", "lat_advance", "lat_run", "lat_diagnostics",
     "lat_detect_crossings", "lat_winding", "lat_string_length", "lat_string_length_points",
     "lat_snapshot_doubles", "lat_snapshot_begin", "lat_snapshot_wait", "lat_host_alloc", "lat_host_free",
     "lat_ah_step_f64_noalloc",
@@ -90,6 +90,8 @@ def load_library(path: Path | None = None):
     L.lat_step.argtypes = [vp, ctypes.c_int32]
     L.lat_step_diag.argtypes = [vp, P(LatDiag)]
     L.lat_advance.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, P(LatDiag), ctypes.c_int64, P(ctypes.c_int64)]
+    L.lat_run.argtypes = [vp, dp, dp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, P(LatDiag), ctypes.c_int64,
+                          P(ctypes.c_int64), dp, dp]
     L.lat_diagnostics.argtypes = [vp, P(LatDiag)]
     L.lat_detect_crossings.argtypes = [vp, ctypes.c_int32, dp, ctypes.c_int64, P(ctypes.c_int64)]
     L.lat_winding.argtypes = [vp, ctypes.c_int32, P(ctypes.c_int8), P(ctypes.c_int64)]
@@ -344,6 +346,31 @@ class Lattice:
         cnt = ctypes.c_int64(0)
         _check("lat_advance", self.L.lat_advance(self.h, int(nsteps), int(diag_every), buf, int(cap), ctypes.byref(cnt)))
         return [(buf[q].time_step, buf[q].energy, buf[q].gauss_abs_sum) for q in range(cnt.value)]
+
+    def run(self, now: np.ndarray, past: np.ndarray | None, time_step: int, nsteps: int, diag_every: int = 0,
+            now_out: np.ndarray | None = None, past_out: np.ndarray | None = None):
+        """set_state + advance + get_state in one call (lat_run), with the copies
+        overlapping the steps where the step allows it.  Returns (diagnostics,
+        now_out, past_out); output arrays passed in (C-contiguous float64 of
+        ncomp*N elements, e.g. pinned buffers) are filled, others allocated."""
+        now = np.ascontiguousarray(now, dtype=np.float64).reshape(self.ncomp, self.N)
+        past = now if past is None else np.ascontiguousarray(past, dtype=np.float64).reshape(self.ncomp, self.N)
+        outs = []
+        for a in (now_out, past_out):
+            if a is None:
+                a = np.empty((self.ncomp, self.N), dtype=np.float64)
+            elif a.dtype != np.float64 or not a.flags.c_contiguous or a.size != self.ncomp * self.N:
+                raise ValueError("run: output arrays must be C-contiguous float64 of ncomp*N elements")
+            outs.append(a)
+        cap = 0
+        if diag_every > 0:
+            cap = sum(1 for n in range(time_step, time_step + nsteps) if n % diag_every == 0)
+        buf = (LatDiag * max(cap, 1))()
+        cnt = ctypes.c_int64(0)
+        _check("lat_run", self.L.lat_run(self.h, _dp(now), _dp(past), int(time_step), int(nsteps), int(diag_every),
+                                         buf, int(cap), ctypes.byref(cnt), _dp(outs[0]), _dp(outs[1])))
+        diags = [(buf[q].time_step, buf[q].energy, buf[q].gauss_abs_sum) for q in range(cnt.value)]
+        return diags, outs[0].reshape(self.ncomp, self.N), outs[1].reshape(self.ncomp, self.N)
 
     def diagnostics(self) -> LatDiag:
         d = LatDiag()

@@ -10,9 +10,10 @@ path is the headline; the FP32 form is measured in the same run.
 Reported (one JSON line on rank 0):
   value        site-updates/s with the state resident in HBM (CUDA events on the
                library's stream around the K timed steps);
-  e2e          the same metric through the C ABI with host buffers: upload of
-               the state from pinned memory, the K steps (diagnostics copied
-               back at their cadence) and download of the final state, all
+  e2e          the same metric through the C ABI with host buffers: one
+               lat_run call (upload of the state from pinned memory, the K
+               steps, the diagnostics and the download of the final state,
+               its copies overlapping the steps where the step allows), all
                inside the timed region;
   roofline     dominant kernel (the step kernel): algorithmic bytes per
                site-update x sites / its average launch time, against the
@@ -296,7 +297,7 @@ def measure_gpu(n: int, precision: str, steps: int, warmup: int, ws: int, local:
     plain = [t for t, k in zip(per, kinds) if k == "plain"] or per
     kern_ms = statistics.median(plain)
 
-    # end to end through the C ABI with host buffers (pinned), timed the same way
+    # end to end through the C ABI with host buffers (pinned): one lat_run call
     nc, N = lat.ncomp, lat.N
     pin_now = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
     pin_past = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
@@ -309,10 +310,8 @@ def measure_gpu(n: int, precision: str, steps: int, warmup: int, ws: int, local:
     e0 = time.perf_counter()
     e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e_start.record(stream)
-    lat.set_state(pin_now.numpy(), pin_past.numpy(), 0)
-    diags = lat.advance(steps, DIAG_EVERY)
-    lat.L.lat_get_state(lat.h, out_now.numpy().ctypes.data_as(lattice.ctypes.POINTER(lattice.ctypes.c_double)),
-                        out_past.numpy().ctypes.data_as(lattice.ctypes.POINTER(lattice.ctypes.c_double)))
+    diags, _, _ = lat.run(pin_now.numpy(), pin_past.numpy(), 0, steps, DIAG_EVERY, now_out=out_now.numpy(),
+                          past_out=out_past.numpy())
     e_end.record(stream)
     torch.cuda.synchronize(dev)
     e2e_wall = time.perf_counter() - e0
