@@ -475,10 +475,13 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
 {
     const lat_params& p = h->p;
     const int tNow = (int)((h->n + 1) % 2), tPast = (int)(h->n % 2);
-    // periodic/fixed walls: nothing but the passes touches the levels
-    const bool twopass = p.model == LAT_MODEL_AH && h->elem == 8 && h->links && p.bc <= LAT_BC_FIXED &&
-                         bc_z_kind(p) <= LAT_BC_FIXED;
-    if (wait_ev && !twopass) {
+    // The two-pass FP64 Abelian-Higgs step with periodic or fixed walls (where
+    // nothing but its passes touches the levels) launches the links pass, then
+    // the divergence if needed and the update pass: only the links pass runs
+    // before wait_ev.  Any other step waits at its start.
+    const bool split = p.model == LAT_MODEL_AH && h->elem == 8 && h->links && p.bc <= LAT_BC_FIXED &&
+                       bc_z_kind(p) <= LAT_BC_FIXED;
+    if (wait_ev && !split) {
         LAT_CK(cudaStreamWaitEvent(h->stream, wait_ev, 0));
         wait_ev = nullptr;
     }
@@ -512,8 +515,8 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
     d.charge_current = p.moore_current == LAT_MOORE_CURRENT_CHARGE;
     d.write = write ? 1 : 0;
     const int th0 = h->ncomp - 3;
-    // divergence of the past level's theta for this step's Gauss term (the
-    // two-pass step launches it between its passes, which do not touch it)
+    // divergence of the past level's theta for this step's Gauss term (a split
+    // step launches it between its passes, which do not touch it)
     auto divergence = [&]() -> int {
         if (!(diag && p.g != 0 && !h->div_valid)) return LAT_OK;
         if (h->elem == 8)
@@ -524,7 +527,6 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
                                          (const float*)h->slot(th0 + 2, tPast), cf, (float*)h->divbuf, h->stream));
         return LAT_OK;
     };
-    const bool split = twopass;  // divergence between the two passes
     if (!split && (rc = divergence())) return rc;
     if (p.model == LAT_MODEL_AH) {
         if (h->elem == 8) {
