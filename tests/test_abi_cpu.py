@@ -97,3 +97,17 @@ def test_no_device_is_reported_not_faked(L):
     p = make_params(0, n=8)
     h = ctypes.c_void_p()
     assert L.lat_create(ctypes.byref(p), ctypes.byref(h)) == LAT_ERR_NODEVICE
+
+
+def test_new_entry_points_reject_bad_arguments_before_device(L):
+    """lat_run and lat_dtrig_eval check their arguments before any CUDA call."""
+    from axions_gb300.params import LAT_ERR_INVALID, LAT_OK
+    dp = ctypes.POINTER(ctypes.c_double)
+    buf = np.zeros(8)
+    x = buf.ctypes.data_as(dp)
+    cnt = ctypes.c_int64(0)
+    assert L.lat_run(None, x, x, 0, 1, 0, None, 0, ctypes.byref(cnt), x, x) == LAT_ERR_INVALID
+    assert L.lat_last_error()
+    assert L.lat_dtrig_eval(x, -1, x) == LAT_ERR_INVALID
+    assert L.lat_dtrig_eval(None, 1, x) == LAT_ERR_INVALID
+    assert L.lat_dtrig_eval(x, 0, x) == LAT_OK   # nothing to do: no device needed
