@@ -30,21 +30,6 @@ enum LinkSlot {
     L_COUNT
 };
 
-// x * p for an exact power of two p = 2^e.  When x and the result are normal
-// numbers the product only moves the exponent field, which integer
-// instructions do off the FP64 pipe (1/64 of the FP32 rate on GB300); zeros,
-// subnormals, Inf/NaN and results outside the normal range take the FP64
-// multiply.  Both give the same double.
-__device__ __forceinline__ double mul_pow2(double x, double p)
-{
-    const long long bx = __double_as_longlong(x);
-    const int ex = (int)(bx >> 52) & 0x7ff;
-    const int e = ((int)(__double_as_longlong(p) >> 52) & 0x7ff) - 1023;
-    const int ey = ex + e;
-    if (ex == 0 || ex == 0x7ff || ey <= 0 || ey >= 0x7ff) return x * p;
-    return __longlong_as_double(bx + ((long long)e << 52));
-}
-
 // a / b where b = spacing^2 or spacing: exact reciprocal multiply when every
 // spacing is a power of two (then a*(1/b) == a/b for all a), else IEEE divide.
 template <bool RECIP>

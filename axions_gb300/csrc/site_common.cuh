@@ -2,6 +2,7 @@
 #pragma once
 
 #include "dtrig.cuh"
+#include "fp64_exact.cuh"
 #include "lattice_internal.cuh"
 
 namespace lat {
@@ -41,31 +42,6 @@ struct Trig<float> {
     static __device__ __forceinline__ float cos(float x) { return __cosf(reduce(x)); }
     static __device__ __forceinline__ void sincos(float x, float* s, float* c) { __sincosf(reduce(x), s, c); }
 };
-
-// a / b for a divisor b whose reciprocal y = RN(1/b) was computed on the host:
-// q = a*y, then two residual corrections q += (a - b*q)*y with exact FMA
-// residuals.  The first makes q a faithful quotient; from a faithful q and
-// |y - 1/b| < 2^-53 |1/b|, the second returns the correctly rounded a / b
-// (Markstein's theorem; P. Markstein, IBM J. Res. Dev. 34(1), 1990, and the
-// Handbook of Floating-Point Arithmetic, ch. 4).  So the double is the IEEE
-// quotient, at five FP64 instructions instead of a full division's reciprocal
-// refinement.  A zero a returns a*y (the IEEE quotient +-0); otherwise |a|
-// or |b| outside [2^-400, 2^401) (subnormals, Inf/NaN, and wherever quotient
-// or residual could leave the normal range) take the IEEE division.
-__device__ __forceinline__ bool is_zero(double a) { return (__double_as_longlong(a) << 1) == 0; }
-
-__device__ __forceinline__ double cdiv(double a, double b, double y)
-{
-    constexpr unsigned lo = 1023 - 400, span = 800;  // biased exponents lo .. lo + span
-    const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7ffu;
-    const unsigned eb = ((unsigned)__double2hiint(b) >> 20) & 0x7ffu;
-    if (eb - lo > span) return a / b;
-    if (is_zero(a)) return __dmul_rn(a, y);
-    if (ea - lo > span) return a / b;
-    double q = __dmul_rn(a, y);
-    q = __fma_rn(__fma_rn(-q, b, a), y, q);
-    return __fma_rn(__fma_rn(-q, b, a), y, q);
-}
 
 // a / b.  FP64 divides (the reference's rounding); FP32 multiplies by the
 // reciprocal computed once on the host.
