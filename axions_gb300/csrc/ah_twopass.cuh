@@ -30,6 +30,31 @@ enum LinkSlot {
     L_COUNT
 };
 
+// Base address of every link-data slot.  The host forms them from the
+// buffer and the site count in 64-bit arithmetic: an int slot*N + s offset
+// would pass 2^31 above 143,165,576 sites (15 slots), where a kernel would
+// write at a wrapped offset.  Inside one slot the site index s < 2^31.
+template <class P>
+struct LinkSlotsT {
+    P p[L_COUNT];
+};
+using LinkSlots = LinkSlotsT<double* __restrict__>;
+using LinkSlotsC = LinkSlotsT<const double* __restrict__>;
+
+inline LinkSlots link_slots(double* L, long long N)
+{
+    LinkSlots s;
+    for (int q = 0; q < L_COUNT; ++q) s.p[q] = L + (size_t)q * (size_t)N;
+    return s;
+}
+
+inline LinkSlotsC link_slots_c(const double* L, long long N)
+{
+    LinkSlotsC s;
+    for (int q = 0; q < L_COUNT; ++q) s.p[q] = L + (size_t)q * (size_t)N;
+    return s;
+}
+
 // a / b where b = spacing^2 or spacing: exact reciprocal multiply when every
 // spacing is a power of two (then a*(1/b) == a/b for all a), else IEEE divide.
 template <bool RECIP>
@@ -58,8 +83,7 @@ __device__ __forceinline__ double tdiv(double a, double b, double inv_b)
 template <bool STRICT, bool DIAG>
 __global__ void __launch_bounds__(BLOCK) ah_links_kernel(const Geom g, const double* __restrict__ TX,
                                                          const double* __restrict__ TY,
-                                                         const double* __restrict__ TZ, double* __restrict__ L,
-                                                         const int N)
+                                                         const double* __restrict__ TZ, const LinkSlots L)
 {
     const int k = (int)(blockIdx.x * BZ + threadIdx.x);
     const int j = (int)(blockIdx.y * BY + threadIdx.y);
@@ -73,43 +97,43 @@ __global__ void __launch_bounds__(BLOCK) ah_links_kernel(const Geom g, const dou
     const double txzp = TX[s + n.zp], tyzp = TY[s + n.zp];
     double sv, cv;
     dsincos(tx, &sv, &cv);
-    L[L_CX * N + s] = cv;
-    L[L_SX * N + s] = sv;
+    L.p[L_CX][s] = cv;
+    L.p[L_SX][s] = sv;
     dsincos(ty, &sv, &cv);
-    L[L_CY * N + s] = cv;
-    L[L_SY * N + s] = sv;
+    L.p[L_CY][s] = cv;
+    L.p[L_SY][s] = sv;
     dsincos(tz, &sv, &cv);
-    L[L_CZ * N + s] = cv;
-    L[L_SZ * N + s] = sv;
+    L.p[L_CZ][s] = cv;
+    L.p[L_SZ][s] = sv;
     // plaquette angles, summed in the reference's order (mpi_evolution.cpp:471-487)
     const double Pxy = tx + tyxp - txyp - ty;
     const double Pxz = tx + tzxp - txzp - tz;
     const double Pyz = ty + tzyp - tyzp - tz;
     if constexpr (DIAG) {
         dsincos(Pxy, &sv, &cv);
-        L[L_PXY * N + s] = sv;
-        L[L_CPXY * N + s] = cv;
+        L.p[L_PXY][s] = sv;
+        L.p[L_CPXY][s] = cv;
         dsincos(Pxz, &sv, &cv);
-        L[L_PXZ * N + s] = sv;
-        L[L_CPXZ * N + s] = cv;
+        L.p[L_PXZ][s] = sv;
+        L.p[L_CPXZ][s] = cv;
         dsincos(Pyz, &sv, &cv);
-        L[L_PYZ * N + s] = sv;
-        L[L_CPYZ * N + s] = cv;
+        L.p[L_PYZ][s] = sv;
+        L.p[L_CPYZ][s] = cv;
     } else {
-        L[L_PXY * N + s] = dsin(Pxy);
-        L[L_PXZ * N + s] = dsin(Pxz);
-        L[L_PYZ * N + s] = dsin(Pyz);
+        L.p[L_PXY][s] = dsin(Pxy);
+        L.p[L_PXZ][s] = dsin(Pxz);
+        L.p[L_PYZ][s] = dsin(Pyz);
     }
     if constexpr (STRICT) {
-        L[L_PYX * N + s] = dsin(ty + txyp - tyxp - tx);
-        L[L_PZX * N + s] = dsin(tz + txzp - tzxp - tx);
-        L[L_PZY * N + s] = dsin(tz + tyzp - tzyp - ty);
+        L.p[L_PYX][s] = dsin(ty + txyp - tyxp - tx);
+        L.p[L_PZX][s] = dsin(tz + txzp - tzxp - tx);
+        L.p[L_PZY][s] = dsin(tz + tyzp - tzyp - ty);
     }
 }
 
 template <bool STRICT, bool DIAG, bool RECIP>
 __global__ void __launch_bounds__(BLOCK, 2) ah_update_kernel(const Geom g, const Fields<double, 5> f,
-                                                          const double* __restrict__ L, const int N, const StepCoef c,
+                                                          const LinkSlotsC L, const StepCoef c,
                                                           const DiagOut d)
 {
     const int k = g.loz + (int)(blockIdx.x * BZ + threadIdx.x);
@@ -132,29 +156,29 @@ __global__ void __launch_bounds__(BLOCK, 2) ah_update_kernel(const Geom g, const
         const double tx = f.now[2][s], ty = f.now[3][s], tz = f.now[4][s];
         const double qx = f.past[2][s], qy = f.past[3][s], qz = f.past[4][s];
 
-        const double cx = L[L_CX * N + s], sx = L[L_SX * N + s];
-        const double cy = L[L_CY * N + s], sy = L[L_SY * N + s];
-        const double cz = L[L_CZ * N + s], sz = L[L_SZ * N + s];
-        const double cxm = L[L_CX * N + sxm], sxm_ = L[L_SX * N + sxm];
-        const double cym = L[L_CY * N + sym_], sym = L[L_SY * N + sym_];
-        const double czm = L[L_CZ * N + szm], szm_ = L[L_SZ * N + szm];
-        const double sPxy = L[L_PXY * N + s], sPxz = L[L_PXZ * N + s], sPyz = L[L_PYZ * N + s];
-        const double sPxy_m = L[L_PXY * N + sym_], sPxz_m = L[L_PXZ * N + szm], sPyz_m = L[L_PYZ * N + szm];
+        const double cx = L.p[L_CX][s], sx = L.p[L_SX][s];
+        const double cy = L.p[L_CY][s], sy = L.p[L_SY][s];
+        const double cz = L.p[L_CZ][s], sz = L.p[L_SZ][s];
+        const double cxm = L.p[L_CX][sxm], sxm_ = L.p[L_SX][sxm];
+        const double cym = L.p[L_CY][sym_], sym = L.p[L_SY][sym_];
+        const double czm = L.p[L_CZ][szm], szm_ = L.p[L_SZ][szm];
+        const double sPxy = L.p[L_PXY][s], sPxz = L.p[L_PXZ][s], sPyz = L.p[L_PYZ][s];
+        const double sPxy_m = L.p[L_PXY][sym_], sPxz_m = L.p[L_PXZ][szm], sPyz_m = L.p[L_PYZ][szm];
         double sPyx, sPzx, sPzy, sPyx_m, sPzx_m, sPzy_m;
         if constexpr (STRICT) {
-            sPyx = L[L_PYX * N + s];
-            sPzx = L[L_PZX * N + s];
-            sPzy = L[L_PZY * N + s];
-            sPyx_m = L[L_PYX * N + sxm];
-            sPzx_m = L[L_PZX * N + sxm];
-            sPzy_m = L[L_PZY * N + sym_];
+            sPyx = L.p[L_PYX][s];
+            sPzx = L.p[L_PZX][s];
+            sPzy = L.p[L_PZY][s];
+            sPyx_m = L.p[L_PYX][sxm];
+            sPzx_m = L.p[L_PZX][sxm];
+            sPzy_m = L.p[L_PZY][sym_];
         } else {
             sPyx = -sPxy;
             sPzx = -sPxz;
             sPzy = -sPyz;
-            sPyx_m = -L[L_PXY * N + sxm];
-            sPzx_m = -L[L_PXZ * N + sxm];
-            sPzy_m = -L[L_PYZ * N + sym_];
+            sPyx_m = -L.p[L_PXY][sxm];
+            sPzx_m = -L.p[L_PXZ][sxm];
+            sPzy_m = -L.p[L_PYZ][sym_];
         }
 
         const double twop0 = mul_pow2(p0, 2.0), twop1 = mul_pow2(p1, 2.0);  // 2 * p0, 2 * p1
@@ -209,7 +233,7 @@ __global__ void __launch_bounds__(BLOCK, 2) ah_update_kernel(const Geom g, const
             // (evolution.cpp:322-334,377-427; mpi_evolution.cpp:509-532).  Each
             // divisor other than dt occurs once per site, so cdiv's host
             // reciprocal replaces the division's own (the same doubles).
-            const double cPxy = L[L_CPXY * N + s], cPxz = L[L_CPXZ * N + s], cPyz = L[L_CPYZ * N + s];
+            const double cPxy = L.p[L_CPXY][s], cPxz = L.p[L_CPXZ][s], cPyz = L.p[L_CPYZ][s];
             const double pt0 = tdiv<STRICT>(p0 - q0, c.dt, c.inv_dt);
             const double pt1 = tdiv<STRICT>(p1 - q1, c.dt, c.inv_dt);
             const double px0 = sdiv<RECIP>(p0 - cxm * p0xm + sxm_ * p1xm, c.dx, c.inv_dx);
@@ -266,7 +290,9 @@ template <bool STRICT>
 cudaError_t launch_ah_twopass(const Geom& g, const Fields<double, 5>& f, double* L, const StepCoef& c,
                               const DiagOut& d, bool diag, bool recip, cudaStream_t st, int phase = 3)
 {
-    const int N = g.nx * g.syz;
+    const long long N = (long long)g.nx * g.syz;
+    const LinkSlots Lw = link_slots(L, N);
+    const LinkSlotsC Lr = link_slots_c(L, N);
     Geom all = g;
     all.lox = all.loy = all.loz = 0;
     all.hix = g.nx;
@@ -274,19 +300,19 @@ cudaError_t launch_ah_twopass(const Geom& g, const Fields<double, 5>& f, double*
     all.hiz = g.nz;
     const dim3 block(BZ, BY);
     if (phase & 1) {
-        if (diag) ah_links_kernel<STRICT, true><<<site_grid(all), block, 0, st>>>(g, f.now[2], f.now[3], f.now[4], L, N);
-        else ah_links_kernel<STRICT, false><<<site_grid(all), block, 0, st>>>(g, f.now[2], f.now[3], f.now[4], L, N);
+        if (diag) ah_links_kernel<STRICT, true><<<site_grid(all), block, 0, st>>>(g, f.now[2], f.now[3], f.now[4], Lw);
+        else ah_links_kernel<STRICT, false><<<site_grid(all), block, 0, st>>>(g, f.now[2], f.now[3], f.now[4], Lw);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
     if (!(phase & 2)) return cudaSuccess;
     const dim3 grid = site_grid(g);
     if (diag) {
-        if (recip) ah_update_kernel<STRICT, true, true><<<grid, block, 0, st>>>(g, f, L, N, c, d);
-        else ah_update_kernel<STRICT, true, false><<<grid, block, 0, st>>>(g, f, L, N, c, d);
+        if (recip) ah_update_kernel<STRICT, true, true><<<grid, block, 0, st>>>(g, f, Lr, c, d);
+        else ah_update_kernel<STRICT, true, false><<<grid, block, 0, st>>>(g, f, Lr, c, d);
     } else {
-        if (recip) ah_update_kernel<STRICT, false, true><<<grid, block, 0, st>>>(g, f, L, N, c, d);
-        else ah_update_kernel<STRICT, false, false><<<grid, block, 0, st>>>(g, f, L, N, c, d);
+        if (recip) ah_update_kernel<STRICT, false, true><<<grid, block, 0, st>>>(g, f, Lr, c, d);
+        else ah_update_kernel<STRICT, false, false><<<grid, block, 0, st>>>(g, f, Lr, c, d);
     }
     return cudaGetLastError();
 }

@@ -189,7 +189,11 @@ int lat_params_init(lat_params* p, int32_t model)
     return LAT_OK;
 }
 
-static int validate(const lat_params* p)
+}  // extern "C"
+
+// Checks shared by every entry point that takes a parameter block (also the
+// allocation-free step, noalloc.cu).
+int lat::validate_params(const lat_params* p)
 {
     LAT_REQUIRE(p, "null params");
     LAT_REQUIRE(p->abi_version == LAT_ABI_VERSION, "lat_params.abi_version mismatch");
@@ -211,7 +215,10 @@ static int validate(const lat_params* p)
     const int64_t mxy = p->bc == LAT_BC_PERIODIC ? 2 : 3, mz = kz == LAT_BC_PERIODIC ? 2 : 3;
     LAT_REQUIRE(p->nx >= mxy && p->ny >= mxy && p->nz >= mz, "lattice sides too small for the boundary condition");
     LAT_REQUIRE(p->nx <= 65535 + (p->bc == LAT_BC_PERIODIC ? 0 : 2), "nx above 65535 (grid z-dimension limit)");
-    LAT_REQUIRE(p->nx * p->ny * p->nz < ((int64_t)1 << 31) - 1, "nx*ny*nz must be below 2^31");
+    // each product is formed only once its factors are known to keep it in int64
+    LAT_REQUIRE(p->ny < ((int64_t)1 << 31) && p->nz < ((int64_t)1 << 31) && p->ny * p->nz < ((int64_t)1 << 31) - 1 &&
+                    p->nx * (p->ny * p->nz) < ((int64_t)1 << 31) - 1,
+                "nx*ny*nz must be below 2^31");
     LAT_REQUIRE(p->dx > 0 && p->dy > 0 && p->dz > 0 && p->dt > 0, "spacings and dt must be positive");
     LAT_REQUIRE(std::isfinite(p->tau0) && p->tau0 > 0, "tau0 must be positive");
     LAT_REQUIRE(p->energy_form == LAT_ENERGY_EVOLUTION || p->energy_form == LAT_ENERGY_MPI, "unknown energy_form");
@@ -219,6 +226,10 @@ static int validate(const lat_params* p)
                 "unknown moore_current");
     return LAT_OK;
 }
+
+extern "C" {
+
+static int validate(const lat_params* p) { return validate_params(p); }
 
 // Device bytes lat_create allocates for `p` (the same terms as below).
 static int64_t footprint(const lat_params& p)

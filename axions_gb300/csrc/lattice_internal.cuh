@@ -76,6 +76,8 @@ inline StepCoefT<R> coef_as(const StepCoef& c)
 }
 
 StepCoef make_coef(const lat_params& p, int64_t n);
+// LAT_OK or LAT_ERR_INVALID (with the message set) for a parameter block
+int validate_params(const lat_params* p);
 Geom make_geom(const lat_params& p);
 // LAT_BC_* of the z axis (bc_z, or the same as bc)
 int bc_z_kind(const lat_params& p);

@@ -38,6 +38,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cmath>
 
@@ -75,6 +76,7 @@ constexpr int CHAIN_ERR_UNION = 1;     // union-find retry bound reached
 constexpr int CHAIN_ERR_RESTART = 2;   // no remaining member where one must be
 constexpr int CHAIN_ERR_LINK = 3;      // the link graph is not symmetric, or a walk outran its component
 constexpr int CHAIN_ERR_BARRIER = 4;   // a grid barrier wait gave up
+constexpr long long kDefaultWaitPolls = 1LL << 24;
 
 struct ChainDev {
     ChainGeom g;
@@ -114,6 +116,8 @@ struct ChainDev {
     int* slot_j;              // [2][grid]
     int* slot_min;            // [2][grid]
     unsigned* bar;            // [2] arrivals, generation
+    long long wait_polls;     // polls of a barrier wait before it gives up
+    unsigned missing;         // arrivals a barrier waits for that never come (0; > 0 only to test the bound)
     int* counters;            // [0] roots, [1] queue head, [2] error
     double* out;              // [2] L0, L1
 };
@@ -591,23 +595,29 @@ __global__ void __launch_bounds__(32) sum_kernel(const ChainDev c)
 // cooperative walk over all crossings (any lattice)
 // ---------------------------------------------------------------------------
 // Grid barrier for a cooperative launch (all CTAs resident).  The wait is
-// bounded: after about a second it records CHAIN_ERR_BARRIER and every CTA
-// leaves at its next barrier.  Returns false once an error is recorded.
-__device__ bool grid_barrier(unsigned* bar, int* err)
+// bounded: a CTA polls the generation word at most `polls` times (the host's
+// default, 2^24 polls, is about a second), then records CHAIN_ERR_BARRIER; a
+// CTA that sees the error recorded stops waiting too, and every CTA leaves at
+// its barrier.  `missing` arrivals are added to the count the barrier waits
+// for: none in normal use; a test sets one, an arrival that never comes, to
+// make every wait run out.  Returns false once an error is recorded.
+__device__ bool grid_barrier(unsigned* bar, int* err, long long polls, unsigned missing)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned* vgen = bar + 1;
+        volatile int* verr = err;
         const unsigned gen = *vgen;
         __threadfence();
-        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+        if (atomicAdd(bar, 1u) == gridDim.x + missing - 1) {
             atomicExch(bar, 0u);
             __threadfence();
             atomicAdd(bar + 1, 1u);
         } else {
             long long spins = 0;
             while (*vgen == gen) {
-                if (++spins > (1LL << 24)) {
+                if (*verr != 0) break;
+                if (++spins > polls) {
                     atomicExch(err, CHAIN_ERR_BARRIER);
                     break;
                 }
@@ -682,7 +692,7 @@ __global__ void __launch_bounds__(EX_T) walk_coop_kernel(const ChainDev c)
                 c.slot_min[sl] = (int)mn;
             }
         }
-        if (!grid_barrier(c.bar, &c.counters[2])) return;
+        if (!grid_barrier(c.bar, &c.counters[2], c.wait_polls, c.missing)) return;
         if (wid == 0) {
             best = c.g.cutoff;
             bj = -1;
@@ -814,6 +824,11 @@ int grow(void** p, size_t* have, size_t need, int64_t* held)
     if (held) *held += (int64_t)want;
     return LAT_OK;
 }
+
+// Bound of the cooperative walk's barrier waits and the test's missing
+// arrivals (lat_set_chain_wait).  Process-wide.
+std::atomic<long long> g_wait_polls{kDefaultWaitPolls};
+std::atomic<unsigned> g_missing{0};
 
 // CTAs of the cooperative walk: all resident at once (at most one per SM), at
 // most one per EX_T crossings
@@ -957,6 +972,8 @@ int chain_length_run(const ChainGeom& g, const double* d_xyz, int64_t M, int spl
     CH_CK(cudaMemsetAsync(c.counters, 0, 4 * sizeof(int), st));
     if (method == LAT_CHAIN_EXHAUSTIVE) {
         CH_CK(cudaMemsetAsync(c.bar, 0, 2 * sizeof(unsigned), st));
+        c.wait_polls = g_wait_polls.load();
+        c.missing = g_missing.load();
         void* args[] = {(void*)&c};
         CH_CK(cudaLaunchCooperativeKernel((const void*)walk_coop_kernel, dim3(grid), dim3(EX_T), args, 0, st));
         ++nl;
@@ -1005,6 +1022,18 @@ int chain_length_run(const ChainGeom& g, const double* d_xyz, int64_t M, int spl
 }
 
 }  // namespace lat
+
+extern "C" int lat_set_chain_wait(int64_t polls, int32_t missing_arrivals)
+{
+    using namespace lat;
+    if (polls < 0 || missing_arrivals < 0 || missing_arrivals > 1024) {
+        set_error("lat_set_chain_wait: polls >= 0 and 0 <= missing_arrivals <= 1024");
+        return LAT_ERR_INVALID;
+    }
+    g_wait_polls.store(polls ? (long long)polls : kDefaultWaitPolls);
+    g_missing.store((unsigned)missing_arrivals);
+    return LAT_OK;
+}
 
 extern "C" int lat_string_length_points(const lat_params* p, const double* xyz, int64_t M, int32_t split,
                                         int32_t method, double* L0, double* L1)

@@ -27,7 +27,7 @@ EXPORTS = [
     "lat_set_stream", "lat_get_params", "lat_num_components", "lat_time_step", "lat_device_bytes",
     "lat_kernel_launches",
     "lat_set_state", "lat_get_state", "lat_step", "lat_step_diag", "lat_advance", "lat_run", "lat_diagnostics",
-    "lat_detect_crossings", "lat_winding", "lat_string_length", "lat_string_length_points",
+    "lat_detect_crossings", "lat_winding", "lat_string_length", "lat_string_length_points", "lat_set_chain_wait",
     "lat_snapshot_doubles", "lat_snapshot_begin", "lat_snapshot_wait", "lat_host_alloc", "lat_host_free",
     "lat_ah_step_f64_noalloc",
     "lat_batch_create", "lat_batch_destroy", "lat_batch_add", "lat_batch_remove", "lat_batch_size",
@@ -104,6 +104,7 @@ def load_library(path: Path | None = None):
     L.lat_host_alloc.restype = vp
     L.lat_host_free.argtypes = [vp]
     L.lat_string_length_points.argtypes = [P(LatParams), dp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, dp, dp]
+    L.lat_set_chain_wait.argtypes = [ctypes.c_int64, ctypes.c_int32]
     L.lat_ah_step_f64_noalloc.argtypes = [P(LatParams), vp, ctypes.c_int64, ctypes.c_int32, vp]
     L.lat_batch_create.argtypes = [ctypes.c_int32, P(vp)]
     L.lat_batch_destroy.argtypes = [vp]

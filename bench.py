@@ -42,13 +42,16 @@ sys.path.insert(0, str(ROOT))
 DIAG_EVERY = 20
 # Workloads: "ah" (AH 512^3, the headline) and "moore" (Moore 768^3 FP32 with FP64 reductions).
 MODEL = {"name": "ah"}
+# Forms: "f64" is the plain FP64 path (two-pass step, fused multiply-adds, LAT_F64_FAST); "f64_strict"
+# the same step in the reference's operation order (LAT_F64); "f32" FP32 fields with FP64 reductions.
+FORMS = ("f64", "f64_strict", "f32")
 # algorithmic bytes per site-update: each field value read at levels n and n-1, written at n+1
-BYTES = {"ah": {"f64": 120, "f64_fast": 120, "f32": 60}, "moore": {"f64": 168, "f64_fast": 168, "f32": 84}}
-KERNEL_NAME = {"f64": "ah_links_kernel + ah_update_kernel (strict FP64 two-pass step)",
-               "f64_fast": "ah_links_kernel + ah_update_kernel (fast FP64 two-pass step)",
+BYTES = {"ah": {"f64": 120, "f64_strict": 120, "f32": 60}, "moore": {"f64": 168, "f64_strict": 168, "f32": 84}}
+KERNEL_NAME = {"f64": "ah_links_kernel + ah_update_kernel (FP64 two-pass step, fused multiply-adds)",
+               "f64_strict": "ah_links_kernel + ah_update_kernel (FP64 two-pass step, reference operation order)",
                "f32": "tiled_step_kernel<float, 1> (FP32 fused tiled step)"}
 KERNEL_NAME_MOORE = {"f64": "moore_step_kernel<double> (one-pass FP64 step)",
-                     "f64_fast": "moore_step_kernel<double> (one-pass FP64 step)",
+                     "f64_strict": "moore_step_kernel<double> (one-pass FP64 step)",
                      "f32": "tiled_step_kernel<float, 2> (FP32 fused tiled step, two scalars)"}
 
 
@@ -60,16 +63,28 @@ def kernel_name(precision: str) -> str:
     return (KERNEL_NAME_MOORE if MODEL["name"] == "moore" else KERNEL_NAME)[precision]
 
 
+def lat_precision(precision: str) -> int:
+    from axions_gb300.params import F32, F64, F64_FAST
+    return {"f64": F64_FAST, "f64_strict": F64, "f32": F32}[precision]
+
+
 def workload_params(n: int, precision: str):
-    from axions_gb300.params import ENERGY_EVOLUTION, F32, F64, F64_FAST, MODEL_MOORE, make_params
-    prec = {"f64": F64, "f64_fast": F64_FAST, "f32": F32}[precision]
+    from axions_gb300.params import ENERGY_EVOLUTION, MODEL_MOORE, make_params
+    prec = lat_precision(precision)
     if MODEL["name"] == "moore":
-        # two scalars with charges 1 and 2, equal vevs, lambda1 = lambda2 = 2, e = 1, radiation era
-        return make_params(MODEL_MOORE, n=n, d=0.5, dt=0.1, lam=2.0, lambda2=2.0, lambda12=0.0, eta=1.0, eta2=1.0,
-                           q1=1.0, q2=2.0, g=1.0, damped_nt=0, dampFac=0.0, alpha=3.0, scaling=1.0, tau0=1.0,
-                           energy_form=ENERGY_EVOLUTION, precision=prec)
+        return moore_params(n, precision)
     return make_params(0, n=n, d=0.5, dt=0.1, lam=2.0, eta=1.0, g=1.0, damped_nt=0, dampFac=0.0, alpha=3.0,
                        scaling=1.0, tau0=1.0, energy_form=ENERGY_EVOLUTION, precision=prec)
+
+
+def moore_params(n: int, precision: str):
+    """Config 3: two scalars with charges 1 and 2, equal vevs, lambda1 =
+    lambda2 = 2, e = 1, dx = 0.5, dt = 0.1, radiation era (PRS friction
+    alpha = 3, a ~ tau, tau0 = 1)."""
+    from axions_gb300.params import ENERGY_EVOLUTION, MODEL_MOORE, make_params
+    return make_params(MODEL_MOORE, n=n, d=0.5, dt=0.1, lam=2.0, lambda2=2.0, lambda12=0.0, eta=1.0, eta2=1.0,
+                       q1=1.0, q2=2.0, g=1.0, damped_nt=0, dampFac=0.0, alpha=3.0, scaling=1.0, tau0=1.0,
+                       energy_form=ENERGY_EVOLUTION, precision=lat_precision(precision))
 
 
 def global_string_params(n: int, precision: str):
@@ -79,7 +94,7 @@ def global_string_params(n: int, precision: str):
     periodic.  (Without damping or friction a random-phase start in a periodic
     box keeps its gradient energy and no network forms.)"""
     from axions_gb300.params import ENERGY_EVOLUTION, F32, F64, make_params
-    prec = {"f64": F64, "f32": F32}[precision]
+    prec = lat_precision(precision)
     return make_params(0, n=n, d=0.25, dt=0.05, lam=1.0, eta=1.0, g=0.0, damped_nt=200, dampFac=0.5, alpha=3.0,
                        scaling=1.0, tau0=1.0, energy_form=ENERGY_EVOLUTION, precision=prec)
 
@@ -189,18 +204,20 @@ def dist_sum(ws: int, x: float, device=None) -> float:
 # ---------------------------------------------------------------------------
 # CPU implementation (the oracle's restatement of the reference arithmetic)
 # ---------------------------------------------------------------------------
-def cpu_rate(n: int, seconds: float, min_steps: int = 2):
-    """Site-updates/s of the CPU implementation on all host cores, on an n^3
-    sample of the workload; steps are run until `seconds` have passed."""
+def cpu_rate(n: int, seconds: float, min_steps: int = 2, warmup: int = 1):
+    """Site-updates/s of the CPU implementation (the oracle's restatement of
+    the reference's arithmetic) on all host cores, on the n^3 workload: one
+    IC, `warmup` untimed steps, then timed steps (energy/Gauss on every 20th,
+    as the workload) until at least `min_steps` steps and `seconds` seconds."""
     from oracle import oracle as O
-    p = workload_params(n, "f64")
+    p = workload_params(n, "f64_strict")
     st = O.random_phase_ic(p, 42)
-    O.step(p, st, 0)  # first touch
+    for q in range(max(warmup, 0)):
+        O.step(p, st, q, diag=q % DIAG_EVERY == 0)
     steps, t0 = 0, time.perf_counter()
     while True:
-        n_step = 1 + steps
-        d = n_step % DIAG_EVERY == 0
-        O.step(p, st, n_step, diag=d)
+        n_step = max(warmup, 0) + steps
+        O.step(p, st, n_step, diag=n_step % DIAG_EVERY == 0)
         steps += 1
         el = time.perf_counter() - t0
         if steps >= min_steps and el >= seconds:
@@ -218,7 +235,7 @@ def load_traffic(precision: str, n: int):
         return None
     try:
         d = json.loads(f.read_text())
-        e = d.get(f"{'moore' if MODEL['name'] == 'moore' else 'ah'}_step_{precision}")
+        e = d.get(f"{MODEL['name']}_step_{precision}")
         if not e:
             return None
         return e["bytes_per_site"] * n ** 3
@@ -236,7 +253,7 @@ def fp64_ceiling(precision: str, res: dict, peaks: dict):
         return None
     try:
         d = json.loads(f.read_text())
-        e = d.get(f"{'moore' if MODEL['name'] == 'moore' else 'ah'}_step_{precision}")
+        e = d.get(f"{MODEL['name']}_step_{precision}")
         if not e or "fp64_inst_per_site" not in e:
             return None
         import torch
@@ -250,7 +267,13 @@ def fp64_ceiling(precision: str, res: dict, peaks: dict):
         return None
 
 
-def measure_gpu(n: int, precision: str, steps: int, warmup: int, ws: int, local: int, peaks: dict):
+def measure_gpu(n: int, precision: str, steps: int, warmup: int, ws: int, local: int, peaks: dict,
+                device_ic: bool = False):
+    """K steps of the workload with the state resident (CUDA events on the
+    library's stream), then the same K steps end to end through lat_run from
+    pinned host buffers.  The IC is the host mt19937 one (mpi_evolution.cpp:
+    287-312), or with device_ic the device Philox one (for the 768^3 Moore
+    lattice, whose host draws would take longer than its steps)."""
     import numpy as np
     import torch
 
@@ -259,10 +282,20 @@ def measure_gpu(n: int, precision: str, steps: int, warmup: int, ws: int, local:
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     p = workload_params(n, precision)
-    ic = lattice.random_phase_ic(p, 42 + local, independent=MODEL["name"] == "moore")
+    moore = MODEL["name"] == "moore"
     lat = lattice.Lattice(p)
     lat.set_stream(stream.cuda_stream)
-    lat.set_state(ic, ic, 0)
+    nc, N = lat.ncomp, lat.N
+    pin_now = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
+    if device_ic:
+        lat.random_phase_ic_device(42 + local, independent=moore)
+        pin_past = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
+        lat.get_state(pin_now.numpy(), pin_past.numpy())
+        del pin_past
+    else:
+        pin_now.numpy()[:] = lattice.random_phase_ic(p, 42 + local, independent=moore)
+        lat.set_state(pin_now.numpy(), None, 0)
+    ic = pin_now.numpy()
 
     def one_step():
         return lat.advance(1, DIAG_EVERY)
@@ -298,11 +331,8 @@ def measure_gpu(n: int, precision: str, steps: int, warmup: int, ws: int, local:
     kern_ms = statistics.median(plain)
 
     # end to end through the C ABI with host buffers (pinned): one lat_run call
-    nc, N = lat.ncomp, lat.N
-    pin_now = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
-    pin_past = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
-    pin_now.numpy()[:] = ic
-    pin_past.numpy()[:] = ic
+    # from the IC (both levels equal)
+    pin_past = pin_now
     out_now = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
     out_past = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
     dist_barrier(ws)
@@ -346,7 +376,7 @@ def ensemble_jobs(njobs: int, n: int):
     return jobs
 
 
-def measure_ensemble(njobs: int, n: int, steps: int, diag_every: int, tick: int):
+def measure_ensemble(njobs: int, n: int, steps: int, diag_every: int, tick: int, extras: bool = True):
     """Runs/hour of an ensemble: batched (all lattices in the same launches,
     one CUDA graph per tick) against the same jobs run one after another
     through the single-lattice path, in the same FP32 form and (sampled) in
@@ -415,15 +445,19 @@ def measure_ensemble(njobs: int, n: int, steps: int, diag_every: int, tick: int)
         "sequential": {"runs_per_hour": njobs / seq_step * 3600, "runs_per_hour_e2e": njobs / seq_total * 3600,
                        "site_updates_per_s": su / seq_step},
     })
+    # like for like: the batch against the same FP32 jobs run one after another
     out["speedup"] = out["batched"]["runs_per_hour"] / out["sequential"]["runs_per_hour"]
     out["speedup_e2e"] = out["batched"]["runs_per_hour_e2e"] / out["sequential"]["runs_per_hour_e2e"]
-    # The same jobs run one after another through the plain path (FP64 strict,
-    # the form the FP32/batched forms are built beside), sampled on two jobs.
+    if not extras:
+        return out
+    # The same jobs run one after another through the plain FP64 path (the
+    # form the FP32/batched forms are built beside), sampled on two jobs: a
+    # precision comparison, not a batching one.
     t_step = t_total = 0.0
     sampled = jobs[:2]
     for p, seed in sampled:
         q = p.copy()
-        q.precision = 0
+        q.precision = lat_precision("f64")
         t0 = time.perf_counter()
         lat = lattice.Lattice(q)
         lat.random_phase_ic_device(seed)
@@ -437,7 +471,7 @@ def measure_ensemble(njobs: int, n: int, steps: int, diag_every: int, tick: int)
     if sampled:
         k = len(sampled)
         out["sequential_plain_f64"] = {"runs_per_hour": k / t_step * 3600, "runs_per_hour_e2e": k / t_total * 3600,
-                                       "sampled_runs": k, "precision": "f64 strict (the plain path)"}
+                                       "sampled_runs": k, "precision": "f64, the plain two-pass path"}
         out["speedup_vs_plain_f64"] = out["batched"]["runs_per_hour"] / out["sequential_plain_f64"]["runs_per_hour"]
         out["speedup_vs_plain_f64_e2e"] = (out["batched"]["runs_per_hour_e2e"]
                                            / out["sequential_plain_f64"]["runs_per_hour_e2e"])
@@ -470,30 +504,42 @@ def measure_ensemble(njobs: int, n: int, steps: int, diag_every: int, tick: int)
     return out
 
 
-def measure_fp32_accuracy(n: int, steps: int, sample_every: int = 100):
-    """FP32 form against the FP64 path on the same seeded IC.  The workload's
-    physics (diagnostics every 20 steps): field L2 drift at the end and the
-    largest relative difference of the energy and of the Gauss residual over the
-    run.  Global strings (the reference's default physics, 128^3, 1000 steps):
-    every 250 steps the total string length by greedy chaining of the crossings
-    (L0 + L1, ic_w_evolution.cpp:961-1087) and the number of crossings.  (With
-    e != 0 the gauge links drift and the reference's detection, which reads phi
-    alone, finds crossings at almost every site after a few hundred steps, so
-    lengths are compared on global strings, as the reference measures them.)"""
+def fp32_vs_fp64(params_fn, n: int, steps: int, diag_every: int, seed: int, independent: bool, check_every: int):
+    """One config run twice from the same initial values: FP32 fields with
+    FP64 reductions, and the plain FP64 path (parity-tested against the
+    oracle).  The IC is the FP32 device IC of `seed` (so both start from the
+    same, float-representable values).  Returns the field L2 drift at the end,
+    the largest relative energy and Gauss differences over the diagnostic
+    steps, and every `check_every` steps the crossing counts and winding
+    totals of each scalar."""
     import numpy as np
 
     from axions_gb300 import lattice
-    out = {"lattice": n, "steps": steps, "diag_every": DIAG_EVERY}
+    p32 = params_fn(n, "f32")
+    nf = 2 if p32.model == 1 else 1
+    ic = None
     runs = {}
-    for prec in ("f64", "f32"):
-        p = workload_params(n, prec)
+    for form in ("f32", "f64"):
+        p = params_fn(n, form)
         with lattice.Lattice(p) as lat:
-            lat.random_phase_ic_device(2026)
-            diags = lat.advance(steps, DIAG_EVERY)
+            if ic is None:
+                lat.random_phase_ic_device(seed, independent=independent)
+                ic = lat.get_state()[0]
+            else:
+                lat.set_state(ic, None, 0)
+            diags, checks = [], []
+            t0 = time.perf_counter()
+            while lat.time_step < steps:
+                k = min(check_every, steps - lat.time_step)
+                diags += lat.advance(k, diag_every)
+                checks.append({"step": lat.time_step,
+                               "crossings": [lat.count_crossings(f) for f in range(nf)],
+                               "winding_abs": [lat.winding(f, want_array=False)[1] for f in range(nf)]})
+            secs = time.perf_counter() - t0
             now, _ = lat.get_state()
-        runs[prec] = (np.array([d[1] for d in diags]), np.array([d[2] for d in diags]), now)
-    e64, g64, f64 = runs["f64"]
-    e32, g32, f32 = runs["f32"]
+        runs[form] = (np.array([d[1] for d in diags]), np.array([d[2] for d in diags]), now, checks, secs)
+    e64, g64, f64, c64, s64 = runs["f64"]
+    e32, g32, f32, c32, s32 = runs["f32"]
 
     def rel(a, b):
         """largest |a-b|/|b| over entries with b != 0 (the Gauss residual of the
@@ -501,12 +547,40 @@ def measure_fp32_accuracy(n: int, steps: int, sample_every: int = 100):
         m = np.abs(b) > 0
         return float(np.max(np.abs(a - b)[m] / np.abs(b)[m])) if m.any() else 0.0
 
-    out.update({
+    ns = 2 * nf
+    return {
+        "lattice": n, "steps": steps, "diag_every": diag_every,
         "field_l2_drift": float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64)),
-        "scalar_l2_drift": float(np.linalg.norm(f32[:2] - f64[:2]) / np.linalg.norm(f64[:2])),
+        "scalar_l2_drift": float(np.linalg.norm(f32[:ns] - f64[:ns]) / np.linalg.norm(f64[:ns])),
         "energy_rel_max": rel(e32, e64), "energy_rel_final": float(abs(e32[-1] - e64[-1]) / abs(e64[-1])),
         "gauss_rel_max": rel(g32, g64), "gauss_rel_final": float(abs(g32[-1] - g64[-1]) / abs(g64[-1])),
-    })
+        "checks_f64": c64, "checks_f32": c32, "f64_s": s64, "f32_s": s32,
+        "speedup_f32": s64 / s32,
+    }
+
+
+def measure_fp32_accuracy(n: int, steps: int, moore_n: int, moore_steps: int):
+    """FP32 forms against the FP64 path, per config.
+    Config 2 (Abelian-Higgs n^3, radiation era, diagnostics every 20) and
+    config 3's physics (Moore, charges 1 and 2, radiation era, both scalars'
+    crossings every 50 steps; at moore_n^3, the largest lattice whose FP64 run
+    fits the benchmark's time): field L2 drift, energy and Gauss residual, and
+    crossing counts and winding totals.  With e != 0 the gauge links drift and
+    the reference's detection, which reads phi alone, finds crossings at almost
+    every site after a few hundred steps, so a greedy-chained string length of
+    these fields is not meaningful (and would chain ~10^8 crossings of one
+    percolating cluster); the total string length is compared on global
+    strings (the reference's default physics, 128^3, 1000 steps): every 250
+    steps L0 + L1 by greedy chaining (ic_w_evolution.cpp:961-1087) and the
+    number of crossings."""
+    import numpy as np
+
+    from axions_gb300 import lattice
+    out = {"config2": fp32_vs_fp64(workload_params, n, steps, DIAG_EVERY, 2026, False, 250)}
+    out["config2"]["string_length"] = "not meaningful at e != 0 (about one crossing per site); see global_strings"
+    out["config3"] = fp32_vs_fp64(moore_params, moore_n, moore_steps, 50, 2027, True, 500)
+    out["config3"]["string_length"] = "not meaningful at e != 0 (about one crossing per site); see global_strings"
+    out["config3"]["note"] = f"config 3 physics at {moore_n}^3 (the configured 768^3 x 1500 FP64 run takes ~10 min)"
     gn, gsteps, gevery = 128, 1000, 250
     lens = {}
     for prec in ("f64", "f32"):
@@ -522,11 +596,13 @@ def measure_fp32_accuracy(n: int, steps: int, sample_every: int = 100):
         lens[prec] = (np.array(L), np.array(M))
     l64, c64 = lens["f64"]
     l32, c32 = lens["f32"]
+    m = l64 > 0
     out["global_strings"] = {
         "physics": GLOBAL_STRINGS, "lattice": gn, "steps": gsteps,
         "every": gevery,
         "string_length_f64": l64.tolist(), "string_length_f32": l32.tolist(),
-        "string_length_rel_max": rel(l32, l64), "crossings_f64": c64.tolist(), "crossings_f32": c32.tolist()}
+        "string_length_rel_max": float(np.max(np.abs(l32 - l64)[m] / l64[m])) if m.any() else 0.0,
+        "crossings_f64": c64.tolist(), "crossings_f32": c32.tolist()}
     return out
 
 
@@ -688,6 +764,30 @@ def measure_serving(njobs: int, rate: float, budget_gb: float, tick: int, seed: 
             "gpu_busy_frac": st.busy_s / st.wall_s, "peak_hbm_gb": st.peak_bytes / (1 << 30)}
 
 
+def bench_config(n: int, precision: str, ws: int) -> dict:
+    """The `config` of the JSON line, the same for both arms."""
+    return {"workload": workload_name(n), "model": "moore" if MODEL["name"] == "moore" else "abelian-higgs",
+            "lattice": n, "precision": precision, "diag_every": DIAG_EVERY,
+            "l2": f"inputs larger than L2 ({2 * BYTES[MODEL['name']]['f64'] / 3 * n ** 3 / 1e9:.1f} GB FP64 state)",
+            "parallelism": "replicas" if ws > 1 else "single"}
+
+
+def form_entry(res: dict, form: str, n: int, units: float, t_ms: float, steps: int, hbm: float, peaks: dict,
+               head_ms: float | None) -> dict:
+    ach = bytes_per_site(form) * res["sites"] / (res["kern_ms"] * 1e-3) / 1e9
+    e = {"value": units / (t_ms * 1e-3), "ms_per_step": t_ms / steps, "dtype": "f32" if form == "f32" else "f64",
+         "kernel_ms": res["kern_ms"], "kernel": kernel_name(form),
+         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                      "traffic": load_traffic(form, n), "bytes_per_site": bytes_per_site(form),
+                      "fp64_pipe": fp64_ceiling(form, res, peaks)},
+         "e2e": {"value": units / (res["e2e_ms"] * 1e-3), "unit": "site-updates/s",
+                 "h2d_bytes_per_step": res["e2e_h2d"], "d2h_bytes_per_step": res["e2e_d2h"]},
+         "clocks": res["clocks"], "gpu_launches": res["launches"]}
+    if head_ms:
+        e["speedup_vs_headline"] = head_ms / res["total_ms"]
+    return e
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -695,24 +795,33 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--model", choices=["ah", "moore"], default="ah",
-                    help="ah: Abelian-Higgs 512^3 (headline); moore: Moore model 768^3")
+                    help="ah: Abelian-Higgs 512^3 (headline); moore: Moore model 768^3 as the headline")
     ap.add_argument("--n", type=int, default=None, help="lattice side (default 512 for ah, 768 for moore)")
-    ap.add_argument("--cpu-n", type=int, default=256, help="side of the CPU sample lattice")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--precision", choices=["f64", "f64_fast", "f32"], default="f64",
+    ap.add_argument("--cpu-n", type=int, default=None, help="side of the CPU lattice (default: the workload's)")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--precision", choices=list(FORMS), default="f64",
                     help="form of the headline number (the workload's plain path is f64)")
-    ap.add_argument("--no-fp32", action="store_true", help="measure only the headline form")
+    ap.add_argument("--no-forms", "--no-fp32", action="store_true", help="measure only the headline form")
+    ap.add_argument("--no-moore", action="store_true", help="skip the Moore 768^3 FP32 form (config 3)")
+    ap.add_argument("--moore-n", type=int, default=768)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--ensemble-jobs", type=int, default=64)
     ap.add_argument("--ensemble-n", type=int, default=128)
     ap.add_argument("--ensemble-steps", type=int, default=500)
+    ap.add_argument("--ensemble-small", type=str, default="64,32", help="further ensemble sides (like for like only)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
-    ap.add_argument("--serving-jobs", type=int, default=120, help="jobs in the Poisson stream (workload: 2000)")
+    ap.add_argument("--serving-jobs", type=int, default=120,
+                    help="jobs in the Poisson stream (a sample of the configured 2000)")
     ap.add_argument("--serving-rate", type=float, default=4.0, help="mean arrivals per second")
+    ap.add_argument("--serving-saturated-jobs", type=int, default=240,
+                    help="jobs of a second stream arriving faster than the GPU serves them (0: skip)")
+    ap.add_argument("--serving-saturated-rate", type=float, default=60.0)
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy study")
-    ap.add_argument("--accuracy-n", type=int, default=256, help="lattice side of the accuracy study (workload: 512)")
+    ap.add_argument("--accuracy-n", type=int, default=512, help="lattice side of config 2's accuracy run")
     ap.add_argument("--accuracy-steps", type=int, default=1000)
+    ap.add_argument("--accuracy-moore-n", type=int, default=256, help="lattice side of config 3's accuracy run")
+    ap.add_argument("--accuracy-moore-steps", type=int, default=1500)
     ap.add_argument("--no-length", action="store_true", help="skip the string-length measurement")
     ap.add_argument("--no-ic", action="store_true", help="skip the string initial-condition measurement")
     ap.add_argument("--ic-n", type=int, default=401)
@@ -723,37 +832,36 @@ def main():
     args = ap.parse_args()
     ws, rank, local = dist_env()
     MODEL["name"] = args.model
-    n = args.n if args.n else (768 if args.model == "moore" else 512)
+    n = args.n if args.n else (args.moore_n if args.model == "moore" else 512)
+    cpu_n = args.cpu_n or n
     steps, warmup = args.steps, max(args.warmup, 0)
 
     if args.impl == "reference":
+        # the reference's arithmetic on the host cores (the oracle's restatement,
+        # pinned bit-exact against reference builds): the same workload, lattice
+        # and step count; rank 0 alone under torchrun
         if rank != 0:
             return
-        rates = []
-        from oracle import oracle as O  # noqa: F401
-        for _ in range(warmup):
-            cpu_rate(args.cpu_n, 0.0, min_steps=1)
-        t0 = time.perf_counter()
-        r, cores, ns, el = cpu_rate(args.cpu_n, 0.0, min_steps=steps)
-        rates.append(r)
+        MODEL["name"] = "ah"
+        r, cores, ns, el = cpu_rate(cpu_n, 0.0, min_steps=steps, warmup=warmup)
         line = {"impl": "reference", "metric": "site-updates/s", "value": r, "unit": "site-updates/s",
-                "n_gpus": args.gpus, "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * el / ns,
+                "n_gpus": args.gpus, "steps": ns, "warmup": warmup, "ms_per_step": 1e3 * el / ns,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic: seeded uniform-phase IC (mt19937)",
-                "config": {"workload": workload_name(n), "lattice": n, "sample_lattice": args.cpu_n,
-                           "model": "abelian-higgs", "parallelism": "replicas"},
+                "data": "synthetic: seeded uniform-phase IC (mt19937, mpi_evolution.cpp:287-312)",
+                "config": bench_config(cpu_n, "f64", args.gpus),
                 "cpu_baseline": {"value": r, "unit": "site-updates/s", "cores": cores, "kind": "port",
-                                 "sample": f"{args.cpu_n}^3 lattice of the same physics, {ns} steps"},
+                                 "sample": f"the {cpu_n}^3 workload itself, {ns} steps after {warmup} warm-up "
+                                           f"steps, {el:.1f} s"},
                 "e2e": {"value": r, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
 
     # CPU baseline before the first CUDA call (rank 0, one GPU only)
     cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu:
-        r, cores, ns, el = cpu_rate(args.cpu_n, args.cpu_seconds)
+    if rank == 0 and ws == 1 and not args.no_cpu and args.model == "ah":
+        r, cores, ns, el = cpu_rate(cpu_n, args.cpu_seconds, warmup=1)
         cpu = {"value": r, "unit": "site-updates/s", "cores": cores, "kind": "port",
-               "sample": f"{args.cpu_n}^3 lattice of the same physics, {ns} steps in {el:.1f} s"}
+               "sample": f"the {cpu_n}^3 workload itself, {ns} steps in {el:.1f} s after 1 warm-up step"}
 
     t_start = time.perf_counter()
     import torch
@@ -768,40 +876,59 @@ def main():
     peak_src = "measured" if hbm else "fallback"
     hbm = hbm or 6800.0
 
+    def note(leg, t0):
+        print(f"bench: {leg} done in {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
+
     head = args.precision
-    res = measure_gpu(n, head, steps, warmup, ws, local, peaks)
+    dev_ic = args.model == "moore"
+    res = measure_gpu(n, head, steps, warmup, ws, local, peaks, device_ic=dev_ic)
     t_max = dist_max(ws, res["total_ms"], dev)
     units = dist_sum(ws, float(res["sites"]) * steps, dev)
     e2e_max = dist_max(ws, res["e2e_ms"], dev)
     forms = {}
-    for form in ([] if args.no_fp32 else [f for f in ("f64", "f64_fast", "f32") if f != head]):
-        r2 = measure_gpu(n, form, steps, warmup, ws, local, peaks)
+    for form in ([] if args.no_forms else [f for f in FORMS if f != head]):
+        r2 = measure_gpu(n, form, steps, warmup, ws, local, peaks, device_ic=dev_ic)
         t2 = dist_max(ws, r2["total_ms"], dev)
-        ach2 = bytes_per_site(form) * r2["sites"] / (r2["kern_ms"] * 1e-3) / 1e9
-        forms[form] = {"value": units / (t2 * 1e-3), "ms_per_step": t2 / steps,
-                       "dtype": "f32" if form == "f32" else "f64", "kernel_ms": r2["kern_ms"],
-                       "roofline": {"bound": "hbm", "achieved": ach2, "peak": hbm, "unit": "GB/s",
-                                    "frac": ach2 / hbm, "traffic": load_traffic(form, n),
-                                    "fp64_pipe": fp64_ceiling(form, r2, peaks)},
-                       "speedup_vs_f64": res["total_ms"] / r2["total_ms"]}
-    def note(leg, t0):
-        print(f"bench: {leg} done in {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
-
+        r2["e2e_ms"] = dist_max(ws, r2["e2e_ms"], dev)
+        forms[form] = form_entry(r2, form, n, units, t2, steps, hbm, peaks, res["total_ms"])
     note("headline and forms", t_start)
+    moore = None
+    if args.model == "ah" and not args.no_moore:
+        t_leg = time.perf_counter()
+        MODEL["name"] = "moore"
+        rm = measure_gpu(args.moore_n, "f32", steps, warmup, ws, local, peaks, device_ic=True)
+        tm = dist_max(ws, rm["total_ms"], dev)
+        rm["e2e_ms"] = dist_max(ws, rm["e2e_ms"], dev)
+        um = dist_sum(ws, float(rm["sites"]) * steps, dev)
+        moore = form_entry(rm, "f32", args.moore_n, um, tm, steps, hbm, peaks, None)
+        moore["config"] = bench_config(args.moore_n, "f32", ws)
+        moore["data"] = "synthetic: seeded independent uniform phases per scalar (device Philox-4x32-10)"
+        MODEL["name"] = "ah"
+        note("moore", t_leg)
     t_leg = time.perf_counter()
     ensemble = None
     if not args.no_ensemble:
         ensemble = measure_ensemble(args.ensemble_jobs, args.ensemble_n, args.ensemble_steps, DIAG_EVERY, 50)
+        ensemble["smaller"] = {}
+        for side in [int(x) for x in args.ensemble_small.split(",") if x.strip()]:
+            ensemble["smaller"][str(side)] = measure_ensemble(args.ensemble_jobs, side, args.ensemble_steps,
+                                                              DIAG_EVERY, 50, extras=False)
     note("ensemble", t_leg)
     t_leg = time.perf_counter()
-    serving = None
+    serving = serving_sat = None
     if not args.no_serving:
         serving = measure_serving(args.serving_jobs, args.serving_rate, 96.0, 25)
+        serving["note"] = f"a {args.serving_jobs}-job sample of the configured 2000-job stream"
+        if args.serving_saturated_jobs > 0:
+            serving_sat = measure_serving(args.serving_saturated_jobs, args.serving_saturated_rate, 96.0, 25,
+                                          seed=4343)
+            serving_sat["note"] = "arrivals faster than the GPU serves them: the engine's own throughput"
     note("serving", t_leg)
     t_leg = time.perf_counter()
     accuracy = None
     if not args.no_accuracy and args.model == "ah":
-        accuracy = measure_fp32_accuracy(args.accuracy_n, args.accuracy_steps)
+        accuracy = measure_fp32_accuracy(args.accuracy_n, args.accuracy_steps, args.accuracy_moore_n,
+                                         args.accuracy_moore_steps)
     note("accuracy", t_leg)
     t_leg = time.perf_counter()
     slen = None
@@ -816,17 +943,14 @@ def main():
     note("string initial conditions", t_leg)
     if rank != 0:
         return
+    MODEL["name"] = args.model
     achieved = bytes_per_site(head) * res["sites"] / (res["kern_ms"] * 1e-3) / 1e9
     line = {
         "metric": "site-updates/s", "value": units / (t_max * 1e-3), "unit": "site-updates/s", "n_gpus": ws,
         "steps": steps, "warmup": warmup, "ms_per_step": t_max / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if head == "f32" else "f64",
         "data": "synthetic: seeded uniform-phase IC (mt19937, mpi_evolution.cpp:287-312)",
-        "config": {"workload": workload_name(n), "model": "moore" if args.model == "moore" else "abelian-higgs",
-                   "lattice": n, "precision": head,
-                   "diag_every": DIAG_EVERY,
-                   "l2": f"inputs larger than L2 ({2 * bytes_per_site(head) / 3 * n ** 3 / 1e9:.1f} GB state)",
-                   "parallelism": "replicas" if ws > 1 else "single"},
+        "config": bench_config(n, head, ws),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": load_traffic(head, n), "peak_source": peak_src,
                      "kernel": kernel_name(head), "kernel_ms": res["kern_ms"],
@@ -836,11 +960,11 @@ def main():
                 "h2d_bytes_per_step": res["e2e_h2d"], "d2h_bytes_per_step": res["e2e_d2h"]},
         "gpu_launches": res["launches"],
         "clocks": res["clocks"],
-        "fp32": forms.get("f32"),
-        "f64_fast": forms.get("f64_fast"),
-        "f64": forms.get("f64"),
+        "forms": forms,
+        "moore": moore,
         "ensemble": ensemble,
         "serving": serving,
+        "serving_saturated": serving_sat,
         "fp32_accuracy": accuracy,
         "string_length": slen,
         "string_ic": string_ic,

@@ -280,6 +280,16 @@ int lat_string_length(lat_handle* h, int32_t field, int32_t split, int32_t metho
 int lat_string_length_points(const lat_params* p, const double* xyz, int64_t M, int32_t split, int32_t method,
                              double* L0, double* L1);
 
+/* Bound of the device-side waits of LAT_CHAIN_EXHAUSTIVE (the grid barrier of
+ * its cooperative walk, which stands in for the reference's OpenMP region per
+ * step, ic_w_evolution.cpp:985-1040): a wait polls at most `polls` times
+ * (0: the default, 2^24 polls, about a second), then the walk stops and the
+ * call returns LAT_ERR_TIMEOUT with the device still usable.
+ * missing_arrivals > 0 makes every barrier wait for that many arrivals that
+ * never come, so that a test can make the bound run out; 0 in normal use.
+ * Process-wide; affects later calls. */
+int lat_set_chain_wait(int64_t polls, int32_t missing_arrivals);
+
 /* ---- asynchronous snapshots ------------------------------------------------------
  * The reference writes its field dumps (gifData |phi|^2 volumes,
  * evolution.cpp:1423-1441, mooreEvol.cpp:700-718; finalField) from host arrays
@@ -492,12 +502,14 @@ int lat_server_destroy(lat_server* s);
 /* Largest lattice (sites) lat_ah_step_f64_noalloc accepts: 64^3. */
 #define LAT_NOALLOC_MAX_SITES 262144
 
-/* Advance `nsteps` Abelian-Higgs steps (strict FP64, the same kernels and
- * results as lat_step on a LAT_F64 handle) on fields the caller owns, without
- * allocating any device memory.  No counterpart in the reference: it exists for
- * callers that cannot let a library allocate, e.g. a host application that
- * owns all device memory through its own pool or a fixed budget, or a tight
- * stepping loop that cannot afford cudaMalloc's synchronisation of the device.
+/* Advance `nsteps` Abelian-Higgs FP64 steps on fields the caller owns, without
+ * allocating any device memory: the same kernels and the same doubles as
+ * lat_step on a handle with the same parameters (p->precision LAT_F64 or
+ * LAT_F64_FAST, kernel_variant 0, periodic or fixed walls).  No counterpart in
+ * the reference: it exists for callers that cannot let a library allocate,
+ * e.g. a host application that owns all device memory through its own pool or
+ * a fixed budget, or a tight stepping loop that cannot afford cudaMalloc's
+ * synchronisation of the device.
  *   fields     device pointer, [5 components][2 slots][nx*ny*nz] doubles in the
  *              reference's slot layout (slot (n+1)%2 holds level n, slot n%2
  *              level n-1; mpi_evolution.cpp:62,370-371); updated in place.
@@ -507,10 +519,12 @@ int lat_server_destroy(lat_server* s);
  * The step's per-site scratch (link data) lives in a fixed array inside the
  * library, LAT_NOALLOC_MAX_SITES*15 doubles (31.5 MiB), held by every GPU that
  * loads the library until the process exits.  Larger lattices are rejected
- * with LAT_ERR_INVALID.  The first call on a device looks up that array's
- * device address (make it before any stream capture).  All calls on a device
- * share the array, so calls whose work overlaps on the GPU (different streams,
- * threads or processes sharing the context) race; serialise them. */
+ * with LAT_ERR_INVALID.  The first call in a CUDA context (per device, and
+ * again after cudaDeviceReset or in another context the caller makes current)
+ * looks up that array's device address; make that call before any stream
+ * capture.  All calls on a device share the array, so calls whose work
+ * overlaps on the GPU (different streams, threads or processes sharing the
+ * context) race; serialise them. */
 int lat_ah_step_f64_noalloc(const lat_params* p, double* fields, int64_t time_step, int32_t nsteps,
                             void* stream);
 

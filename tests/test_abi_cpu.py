@@ -111,3 +111,44 @@ def test_new_entry_points_reject_bad_arguments_before_device(L):
     assert L.lat_dtrig_eval(x, -1, x) == LAT_ERR_INVALID
     assert L.lat_dtrig_eval(None, 1, x) == LAT_ERR_INVALID
     assert L.lat_dtrig_eval(x, 0, x) == LAT_OK   # nothing to do: no device needed
+
+
+def test_large_fp64_lattices_are_accepted_with_64_bit_link_offsets(L):
+    """The two-pass FP64 step addresses its 15 link-data slots through base
+    pointers formed in 64-bit arithmetic, so a lattice whose 15*N passes 2^31
+    (528x528x520 = 144,967,680 sites) is valid and its footprint counts the
+    link data in full."""
+    from axions_gb300.params import make_params
+    L.lat_footprint_bytes.restype = ctypes.c_int64
+    p = make_params(0, nx=528, ny=528, nz=520)
+    N = 528 * 528 * 520
+    assert 15 * N > 2 ** 31
+    b = L.lat_footprint_bytes(ctypes.byref(p))
+    fields_div_links = 5 * 2 * N * 8 + N * 8 + 15 * N * 8
+    assert fields_div_links < b < fields_div_links + 64 * 2 ** 20
+
+
+def test_side_products_cannot_wrap(L):
+    """nx*ny*nz is formed only after each factor is bounded: sides whose
+    product would overflow int64 are rejected, not wrapped into range."""
+    from axions_gb300.params import LAT_ERR_INVALID, make_params
+    L.lat_footprint_bytes.restype = ctypes.c_int64
+    for nx, ny, nz in ((2, 2 ** 40, 2 ** 40), (4, 2 ** 62, 4), (65535, 2 ** 31 - 2, 2), (1000, 1000, 2148)):
+        p = make_params(0, nx=nx, ny=ny, nz=nz)
+        assert L.lat_footprint_bytes(ctypes.byref(p)) == LAT_ERR_INVALID, (nx, ny, nz)
+
+
+def test_noalloc_validates_before_any_device_call(L):
+    """The allocation-free step runs the library's parameter checks (and its
+    own) before it touches CUDA, so bad blocks are rejected without a GPU."""
+    from axions_gb300.params import BC_NEUMANN, F32, LAT_ERR_INVALID, MODEL_MOORE, make_params
+    buf = np.zeros(8)
+    x = ctypes.c_void_p(buf.ctypes.data)
+    bad = [dict(precision=F32), dict(model=MODEL_MOORE), dict(bc=BC_NEUMANN), dict(tau0=0.0),
+           dict(tau0=float("nan")), dict(ny=2 ** 40, nz=2 ** 40), dict(kernel_variant=1), dict(nx=65, ny=64, nz=64)]
+    for kw in bad:
+        p = make_params(0, n=8)
+        for k, v in kw.items():
+            setattr(p, k, v)
+        assert L.lat_ah_step_f64_noalloc(ctypes.byref(p), x, 0, 1, None) == LAT_ERR_INVALID, kw
+        assert L.lat_last_error()

@@ -65,3 +65,16 @@ def test_reference_arm_under_torchrun_prints_once_on_rank_0():
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["unit"] == "site-updates/s" and d["higher_is_better"] is True
     assert d["e2e"]["value"] == d["value"] and d["cpu_baseline"]["kind"] == "port"
+
+
+def test_reference_arm_runs_the_same_config_as_ours():
+    """The reference arm times the workload itself: its `config` is the one
+    the GPU arm prints for the same lattice."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "2", "--warmup", "1",
+                        "--cpu-n", "10"], cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][0])
+    assert d["config"] == bench.bench_config(10, "f64", 1)
+    assert d["steps"] == 2 and d["warmup"] == 1 and "10^3 workload itself" in d["cpu_baseline"]["sample"]

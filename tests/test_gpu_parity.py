@@ -126,6 +126,141 @@ def test_config1_physics_64cubed_300_steps(lattice_mod, oracle_mod):
     lat.close()
 
 
+def _detect_loop(step_block, detect, nt, diag_every, det_every, nfields=1, det_from=0):
+    """mpi_evolution.cpp:354-789 (moore_mpi_evolution.cpp:592-849) at a
+    config's cadence: at each step n >= det_from with n % det_every == 0, while
+    the stringsExist latch is set, detect the crossings of the now level of
+    each field (the latch drops after the first empty frame of field 0); then
+    step, with energy/Gauss on every diag_every-th step."""
+    diags, frames, exist = [], [], True
+    n0 = 0
+    while n0 < nt:
+        if n0 >= det_from and exist:
+            xyz = [detect(n0, fld) for fld in range(nfields)]
+            frames.append(xyz)
+            exist = len(xyz[0]) > 0
+        k = min(det_every, nt - n0)
+        diags += step_block(n0, k, diag_every)
+        n0 += k
+    return diags, frames
+
+
+def _oracle_run(oracle_mod, p, seed, nt, diag_every, det_every, independent=False):
+    st = oracle_mod.random_phase_ic(p, seed, independent=independent)
+
+    def block(n0, k, de):
+        return [tuple(r) for r in oracle_mod.evolve(p, st, n0, k, diag_every=de)]
+
+    nf = 2 if p.model == 1 else 1
+    diags, frames = _detect_loop(block, lambda n, f: oracle_mod.detect(p, st, n, f), nt, diag_every, det_every, nf)
+    return st, diags, frames
+
+
+def _gpu_vs_oracle(lattice_mod, oracle_mod, ref, p, seed, nt, diag_every, det_every, precision, label,
+                   independent=False):
+    """The GPU loop against the oracle's (`ref`).  Bars: whole state max-norm
+    and L2 and every field's L2 <= 1e-12; energies <= 1e-12 and summed Gauss
+    deviations <= 1e-10 relative; crossing frames with equal counts, at least
+    99.99 % of coordinates within 1e-9 and all within 1e-3 (a root of the
+    bilinear quadratic moves by up to ~sqrt of the field difference where the
+    quadratic is nearly degenerate), and bit-exact crossings of the final level
+    when the GPU is given the oracle's own fields.  Each field's own max-norm
+    is printed: the table-driven sine/cosine (at most 3 ulps from libm) and
+    the chaotic dynamics let it pass 1e-12 where a component is small."""
+    st, ref_diags, ref_frames = ref
+    q = p.copy()
+    q.precision = precision
+    lat = lattice_mod.Lattice(q)
+    lat.set_state(lattice_mod.random_phase_ic(p, seed, independent), None, 0)
+
+    def block(n0, k, de):
+        assert lat.time_step == n0
+        return lat.advance(k, diag_every=de)
+
+    nf = 2 if p.model == 1 else 1
+    diags, frames = _detect_loop(block, lambda n, f: lat.detect(f), nt, diag_every, det_every, nf)
+    gpu = lat.get_slots()
+    # identical fields: the oracle's final state on the GPU, detected there
+    lat.set_slots(st, nt)
+    same = [np.array_equal(lat.detect(f), oracle_mod.detect(p, st, nt, f)) for f in range(nf)]
+    lat.close()
+    nc = gpu.shape[0]
+    mx, l2 = normwise(gpu, st)
+    a2, b2 = gpu.reshape(nc, -1), st.reshape(nc, -1)
+    per_max = [float(np.abs(a2[c] - b2[c]).max() / np.abs(b2[c]).max()) for c in range(nc)]
+    per_l2 = [float(np.linalg.norm(a2[c] - b2[c]) / np.linalg.norm(b2[c])) for c in range(nc)]
+    e_rel = max(abs(a[1] - b[1]) / abs(b[1]) for a, b in zip(diags, ref_diags))
+    g_pairs = [(a[2], b[2]) for a, b in zip(diags, ref_diags) if b[2] != 0]
+    g_rel = max(abs(a - b) / abs(b) for a, b in g_pairs) if g_pairs else 0.0
+    counts = [[len(x) for x in fr] for fr in frames]
+    ref_counts = [[len(x) for x in fr] for fr in ref_frames]
+    d = [np.abs(a - b).ravel() for fa, fb in zip(frames, ref_frames) for a, b in zip(fa, fb)
+         if len(a) == len(b) and len(b)]
+    d = np.concatenate(d) if d else np.zeros(1)
+    far = float(np.mean(d > 1e-9))
+    print(f"{label} precision={precision}: state max {mx:.3e} l2 {l2:.3e}; per-field max "
+          + " ".join(f"{v:.2e}" for v in per_max) + "; per-field l2 " + " ".join(f"{v:.2e}" for v in per_l2)
+          + f"; energy {e_rel:.2e} gauss {g_rel:.2e}; crossings {counts}; max |dxyz| {d.max():.2e}, "
+          f"fraction > 1e-9 {far:.2e}; identical-field detection bit-exact {same}")
+    assert_fields_close(gpu, st)
+    assert [x[0] for x in diags] == [x[0] for x in ref_diags] == list(range(0, nt, diag_every))
+    assert e_rel <= TOL
+    assert g_rel <= 1e-10
+    assert counts == ref_counts
+    assert d.max() <= 1e-3 and far <= 1e-4
+    assert all(same)
+
+
+@pytest.fixture(scope="module")
+def config1_oracle(oracle_mod):
+    """Config 1 on the oracle: Abelian-Higgs 128^3 periodic, lambda=2, e=1,
+    eta=1, dx=0.5, dt=0.1, Minkowski, seeded random phases; 300 steps,
+    energy/Gauss every 10, detection every 50."""
+    from axions_gb300.params import ENERGY_EVOLUTION, make_params
+    p = make_params(0, n=128, d=0.5, dt=0.1, lam=2.0, eta=1.0, g=1.0, damped_nt=0, dampFac=0.0, alpha=0.0,
+                    energy_form=ENERGY_EVOLUTION)
+    return p, _oracle_run(oracle_mod, p, 42, 300, 10, 50)
+
+
+@pytest.mark.parametrize("precision", [0, 2], ids=["f64", "f64_fast"])
+def test_config1_at_its_own_size(lattice_mod, oracle_mod, config1_oracle, precision):
+    """Config 1 at its own size (128^3 x 300 steps, energy/Gauss every 10,
+    detection every 50 with the stringsExist latch) against the oracle."""
+    p, ref = config1_oracle
+    _gpu_vs_oracle(lattice_mod, oracle_mod, ref, p, 42, 300, 10, 50, precision, "config1 128^3x300")
+
+
+@pytest.mark.parametrize("precision", [0, 2], ids=["f64", "f64_fast"])
+def test_config2_physics_128cubed_1000_steps(lattice_mod, oracle_mod, precision):
+    """Config 2's physics (radiation era a ~ tau from tau0 = 1, PRS friction
+    alpha = 3, lambda=2, e=1, dx=0.5, dt=0.1) for its 1000 steps with
+    diagnostics every 20, on 128^3 (the oracle cannot run 512^3 x 1000 in a
+    test; its FP32 errors at 512^3 are measured against the FP64 path by the
+    benchmark); detection every 100."""
+    from axions_gb300.params import ENERGY_EVOLUTION, make_params
+    p = make_params(0, n=128, d=0.5, dt=0.1, lam=2.0, eta=1.0, g=1.0, damped_nt=0, dampFac=0.0, alpha=3.0,
+                    scaling=1.0, tau0=1.0, energy_form=ENERGY_EVOLUTION)
+    ref = _ORACLE_CACHE.get("c2") or _ORACLE_CACHE.setdefault("c2", _oracle_run(oracle_mod, p, 2026, 1000, 20, 100))
+    _gpu_vs_oracle(lattice_mod, oracle_mod, ref, p, 2026, 1000, 20, 100, precision, "config2 physics 128^3x1000")
+
+
+def test_config3_physics_moore_fp64_64cubed_1500_steps(lattice_mod, oracle_mod):
+    """Config 3's physics in FP64 (Moore: charges 1 and 2, lambda1 = lambda2
+    = 2, e = 1, eta = 1, dx = 0.5, dt = 0.1, radiation era, independent
+    phases) for its 1500 steps on 64^3, with both scalars' crossings every 50
+    steps and energy/Gauss every 50."""
+    from axions_gb300.params import ENERGY_EVOLUTION, MODEL_MOORE, make_params
+    p = make_params(MODEL_MOORE, n=64, d=0.5, dt=0.1, lam=2.0, lambda2=2.0, lambda12=0.0, eta=1.0, eta2=1.0,
+                    q1=1.0, q2=2.0, g=1.0, damped_nt=0, dampFac=0.0, alpha=3.0, scaling=1.0, tau0=1.0,
+                    energy_form=ENERGY_EVOLUTION)
+    ref = _oracle_run(oracle_mod, p, 3033, 1500, 50, 50, independent=True)
+    _gpu_vs_oracle(lattice_mod, oracle_mod, ref, p, 3033, 1500, 50, 50, 0, "config3 physics moore 64^3x1500",
+                   independent=True)
+
+
+_ORACLE_CACHE = {}
+
+
 def test_prs_moore_48cubed(lattice_mod, oracle_mod):
     """Moore model, charges 1 and 2, PRS friction, independent phases, 100 steps."""
     from axions_gb300.params import MODEL_MOORE, make_params
@@ -258,6 +393,33 @@ def test_twopass_strict_bitwise_equals_onepass(lattice_mod):
         lat.close()
     assert np.array_equal(res[0][0], res[1][0])
     assert res[0][1] == res[1][1]
+
+
+def test_twopass_strict_bitwise_equals_onepass_above_int32_link_offsets(lattice_mod):
+    """528 x 528 x 520 = 144,967,680 sites: the link data's 15 slots span
+    15 * N > 2^31 doubles, so a 32-bit slot * N + s offset would wrap.  The
+    strict two-pass step (link-slot base pointers formed in 64 bits) must give
+    bitwise the doubles of the one-pass kernel, which has no link data, over a
+    diagnostic step and a plain step."""
+    torch = pytest.importorskip("torch")
+    from axions_gb300.params import ENERGY_EVOLUTION, make_params
+    if torch.cuda.get_device_properties(0).total_memory < 80 * 2 ** 30:
+        pytest.skip("needs ~45 GB of device memory")
+    p = make_params(0, nx=528, ny=528, nz=520, d=0.5, dt=0.1, lam=2.0, g=1.0, damped_nt=0, alpha=3.0,
+                    energy_form=ENERGY_EVOLUTION)
+    assert 15 * p.N > 2 ** 31
+    res = []
+    for variant in (0, 1):
+        q = p.copy()
+        q.kernel_variant = variant
+        with lattice_mod.Lattice(q) as lat:
+            lat.random_phase_ic_device(99)
+            d = lat.advance(2, diag_every=2)
+            res.append((lat.get_state(), d))
+    (a_now, a_past), da = res[0]
+    (b_now, b_past), db = res[1]
+    assert da == db and np.isfinite(da[0][1])
+    assert np.array_equal(a_now, b_now) and np.array_equal(a_past, b_past)
 
 
 @pytest.mark.parametrize("d", [0.5, 0.35])

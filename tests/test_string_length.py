@@ -159,3 +159,33 @@ def test_moore_second_field(lattice_mod, oracle_mod):
         got = lat.string_length(field, True)
         assert got[:2] == want
     lat.close()
+
+
+def test_cooperative_walk_barrier_wait_is_bounded(lattice_mod, oracle_mod):
+    """The exhaustive walk's grid barrier waits a bounded number of polls.
+    With one barrier arrival that never comes and a bound of 1000 polls, the
+    call returns LAT_ERR_TIMEOUT at once (no fault, no trap), and the device
+    stays usable: the same call with the default bound then gives the
+    reference's lengths."""
+    import time
+
+    from axions_gb300.params import LAT_ERR_TIMEOUT
+    z = load_golden("ref_icw_len_fixed")
+    p = params_from_json(z["params"])
+    st = oracle_mod.icfunc_random_ic(p, int(z["seed"]))
+    xyz = oracle_mod.detect(p, st, 0, 0)
+    assert len(xyz) > 0
+    L = lattice_mod.load_library()
+    assert L.lat_set_chain_wait(1000, 1) == 0
+    try:
+        t0 = time.perf_counter()
+        with pytest.raises(lattice_mod.LatticeError) as ei:
+            lattice_mod.string_length_points(p, xyz, True, lattice_mod.CHAIN_EXHAUSTIVE)
+        elapsed = time.perf_counter() - t0
+    finally:
+        assert L.lat_set_chain_wait(0, 0) == 0
+    assert ei.value.code == LAT_ERR_TIMEOUT and "barrier" in str(ei.value)
+    assert elapsed < 2.0, elapsed
+    L0, L1 = lattice_mod.string_length_points(p, xyz, True, lattice_mod.CHAIN_EXHAUSTIVE)
+    assert (L0, L1) == (z["L0"][0], z["L1"][0])
+    assert L.lat_set_chain_wait(-1, 0) < 0 and L.lat_set_chain_wait(0, -1) < 0
