@@ -667,3 +667,347 @@ extern "C" int lat_loop_collision_ic_device(lat_handle* h, const lat_string_prof
     if (off_table) *off_table = (int64_t)off_host;
     return LAT_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Perturbed straight strings (initialConditions.cpp:113-668): one level of
+// fields, written into both slots.
+//   "simple sine" (:488-668): per site, the straight string offset along x by
+//     eps*sin(Omega z)/Omega, Omega = 2 pi/(dz (nz-1)).
+//   "NG sine" (:113-486): a Nambu-Goto sine wave.  Per (x, z) column with
+//     z >= 0 a golden-section search (to 1e-6 in the string parameter, every
+//     trial point's z(sigma) a 1001-point trapezoid integral) finds the
+//     closest string point; the sites of the column follow from it, and the
+//     reference mirrors them onto the columns with z < 0.  Here one thread
+//     searches one column, and a second kernel evaluates every site from the
+//     column whose write the reference's loop leaves last (its own, or the
+//     mirrored one), so the result does not depend on an order of writes.
+// The arithmetic follows the reference operation by operation (this unit is
+// compiled with -fmad=false; pow(v, 2) is v*v, the correctly rounded square),
+// with CUDA's sin, cos and sqrt.
+// ---------------------------------------------------------------------------
+namespace lat {
+
+namespace {
+
+constexpr int NG_NELLIP = 1001;  // N_ellipint (initialConditions.cpp:45)
+constexpr double NG_TOL = 1e-6;  // tol (:44)
+
+// both slots of the five components: c[0..4] slot 0, c[5..9] slot 1
+template <class T>
+struct Out10 {
+    T* c[10];
+};
+
+struct SineArgs {
+    int nx, ny, nz, x0, y0, z0;
+    double dx, dy, dz, g, eps, Omega, pi, gr;
+    Profile pr;
+};
+
+__device__ __forceinline__ double sq(double v) { return v * v; }
+
+// z(sigma)*Omega: trapezoid rule with the phase shifted by -pi/2 (:189-198)
+__device__ double ng_ellip(const SineArgs& q, double sigma)
+{
+    double e = 0;
+    for (int j = 0; j < NG_NELLIP; j++) {
+        const double trap_fac = (j == 0 || j == NG_NELLIP - 1) ? 0.5 : 1;
+        const double theta = j * q.Omega * sigma / (NG_NELLIP - 1) - q.pi / 2;
+        e += trap_fac * sqrt(1 - sq(q.eps * sin(theta))) * q.Omega * sigma / (NG_NELLIP - 1);
+    }
+    return e;
+}
+
+__device__ double ng_dist2(const SineArgs& q, double sigma, double x, double z)
+{
+    const double e = ng_ellip(q, sigma);
+    return sq(x - q.eps * cos(q.Omega * sigma - q.pi / 2) / q.Omega) + sq(z - e / q.Omega);
+}
+
+// one column (i, k = z0 + kk): xs, zs, xs_sigma, zs_sigma, paraVecMag, normal_dist
+__global__ void ng_column_kernel(const SineArgs q, double* __restrict__ col, int ncol)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncol) return;
+    const int i = c % q.nx, k = q.z0 + c / q.nx;
+    const double x = (i - q.x0) * q.dx, z = (k - q.z0) * q.dz;
+    double a = -2 * q.pi / q.Omega, b = 2 * q.pi / q.Omega;
+    double sigma1 = b - (b - a) / q.gr, sigma2 = a + (b - a) / q.gr;
+    double d1 = ng_dist2(q, sigma1, x, z), d2 = ng_dist2(q, sigma2, x, z);
+    double tolTest = 1, sigma = 0;
+    while (tolTest > NG_TOL) {  // (b - a) shrinks by 1/gr per pass: ends after ~40 passes
+        if (d1 < d2) b = sigma2;
+        else a = sigma1;
+        sigma1 = b - (b - a) / q.gr;
+        sigma2 = a + (b - a) / q.gr;
+        d1 = ng_dist2(q, sigma1, x, z);
+        d2 = ng_dist2(q, sigma2, x, z);
+        tolTest = b - a;
+        if (tolTest <= NG_TOL) sigma = d1 > d2 ? sigma2 : sigma1;
+    }
+    const double xs = q.eps * cos(q.Omega * sigma - q.pi / 2) / q.Omega;
+    const double zs = ng_ellip(q, sigma) / q.Omega;
+    const double xs_sigma = -q.eps * sin(q.Omega * sigma - q.pi / 2);
+    const double zs_sigma = sqrt(1 - sq(q.eps * sin(q.Omega * sigma - q.pi / 2)));
+    const double paraVecMag = sqrt(sq(xs_sigma) + sq(zs_sigma));
+    col[0 * (size_t)ncol + c] = xs;
+    col[1 * (size_t)ncol + c] = zs;
+    col[2 * (size_t)ncol + c] = xs_sigma;
+    col[3 * (size_t)ncol + c] = zs_sigma;
+    col[4 * (size_t)ncol + c] = paraVecMag;
+    col[5 * (size_t)ncol + c] = (zs_sigma * (x - xs) - xs_sigma * (z - zs)) / paraVecMag;
+}
+
+// the reference's direct values at (i, j, k), k >= z0 (:438-467): phi0, phi1, A0, A1, A2
+__device__ int ng_direct(const SineArgs& q, const double* __restrict__ col, int ncol, int i, int j, int k, double v[5])
+{
+    const int c = (k - q.z0) * q.nx + i;
+    const double xs = col[c], zs = col[(size_t)ncol + c], xs_sigma = col[2 * (size_t)ncol + c];
+    const double zs_sigma = col[3 * (size_t)ncol + c], paraVecMag = col[4 * (size_t)ncol + c];
+    const double normal_dist = col[5 * (size_t)ncol + c];
+    const double x = (i - q.x0) * q.dx, y = (j - q.y0) * q.dy, z = (k - q.z0) * q.dz;
+    const double distance = sqrt(sq(x - xs) + sq(y) + sq(z - zs));
+    double phiMag, AMag;
+    const int off = profile_at(q.pr, distance, phiMag, AMag);
+    if (normal_dist == 0) {
+        v[0] = 0;
+        v[3] = 0;
+    } else {
+        v[0] = phiMag * normal_dist / distance;
+        v[3] = AMag * normal_dist / sq(distance);
+    }
+    if (y == 0) {
+        v[1] = 0;
+        v[2] = 0;
+        v[4] = 0;
+    } else {
+        v[1] = phiMag * y / distance;
+        v[2] = -AMag * zs_sigma * y / (sq(distance) * paraVecMag);
+        v[4] = AMag * xs_sigma * y / (sq(distance) * paraVecMag);
+    }
+    return off;
+}
+
+// Site (i, j, k) as the reference leaves it.  Its loop over k >= z0 (outer),
+// i, j writes (i, j, k) and then the mirror site (nx-1-i, j, nz-1-k) with
+// phi0 and A1 negated (A2 onto (nx-1-i, j, nz-2-k), negated, for k < nz-1).
+// A site gets at most one direct and one mirrored write per field; the later
+// in loop order, (k, i, direct before mirror), stays.
+template <class T>
+__global__ void ng_fill_kernel(const SineArgs q, const double* __restrict__ col, int ncol, long long N, Out10<T> o,
+                               unsigned long long* off)
+{
+    for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < N; s += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(s % q.nz);
+        const long long r = s / q.nz;
+        const int j = (int)(r % q.ny), i = (int)(r / q.ny);
+        double dv[5] = {0, 0, 0, 0, 0}, mv[5];
+        const bool direct = k >= q.z0;
+        if (direct) count_off(off, ng_direct(q, col, ncol, i, j, k, dv));
+        double out[5] = {0, 0, 0, 0, 0};
+        // phi0, phi1, A0, A1: direct at key (k, i); mirror from column (nx-1-i, nz-1-k) at key (nz-1-k, nx-1-i)
+        const int km = q.nz - 1 - k, im = q.nx - 1 - i;
+        const bool mirror = km >= q.z0;
+        const bool mirror_last = mirror && (!direct || km > k || (km == k && im >= i));
+        if (mirror_last) {
+            ng_direct(q, col, ncol, im, j, km, mv);
+            out[0] = -mv[0];
+            out[1] = mv[1];
+            out[2] = mv[2];
+            out[3] = -mv[3];
+        } else if (direct) {
+            out[0] = dv[0];
+            out[1] = dv[1];
+            out[2] = dv[2];
+            out[3] = dv[3];
+        }
+        // A2: mirror from column (nx-1-i, nz-2-k), written while k_src <= nz-2
+        const int k2 = q.nz - 2 - k;
+        const bool mirror2 = k2 >= q.z0;
+        if (mirror2 && (!direct || k2 > k || (k2 == k && im >= i))) {
+            ng_direct(q, col, ncol, im, j, k2, mv);
+            out[4] = -mv[4];
+        } else if (direct) {
+            out[4] = dv[4];
+        }
+        // link columns d*g*A (:482-486), both slots
+        const double v5[5] = {out[0], out[1], q.dx * q.g * out[2], q.dy * q.g * out[3], q.dz * q.g * out[4]};
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+            o.c[c][s] = (T)v5[c];
+            o.c[5 + c][s] = (T)v5[c];
+        }
+    }
+}
+
+template <class T>
+__global__ void simple_sine_kernel(const SineArgs q, long long N, Out10<T> o, unsigned long long* off)
+{
+    for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < N; s += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(s % q.nz);
+        const long long r = s / q.nz;
+        const int j = (int)(r % q.ny), i = (int)(r / q.ny);
+        const double x = (i - q.x0) * q.dx, y = (j - q.y0) * q.dy, z = (k - q.z0) * q.dz;
+        const double xdist = x - q.eps * sin(q.Omega * z) / q.Omega;
+        const double distance = sqrt(xdist * xdist + y * y);
+        double phiMag, AMag, ph0, ph1, A0, A1;
+        count_off(off, profile_at(q.pr, distance, phiMag, AMag));
+        if (xdist == 0) {
+            ph0 = 0;
+            A1 = 0;
+        } else {
+            ph0 = phiMag * xdist / distance;
+            A1 = AMag * xdist / sq(distance);
+        }
+        if (y == 0) {
+            ph1 = 0;
+            A0 = 0;
+        } else {
+            ph1 = phiMag * y / distance;
+            A0 = -AMag * y / sq(distance);
+        }
+        const double v5[5] = {ph0, ph1, q.dx * q.g * A0, q.dy * q.g * A1, q.dz * q.g * 0.0};
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+            o.c[c][s] = (T)v5[c];
+            o.c[5 + c][s] = (T)v5[c];
+        }
+    }
+}
+
+}  // namespace
+
+}  // namespace lat
+
+namespace lat {
+
+namespace {
+
+template <class T>
+Out10<T> both_slots(lat_handle* h)
+{
+    Out10<T> o;
+    for (int t = 0; t < 2; ++t)
+        for (int c = 0; c < 5; ++c) o.c[5 * t + c] = (T*)h->slot(c, t);
+    return o;
+}
+
+template <class T>
+void sine_launch(lat_handle* h, const SineArgs& q, bool ng, const double* col, int ncol, unsigned long long* off)
+{
+    const int threads = 256;
+    long long blocks = ((long long)h->N + threads - 1) / threads;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (ng) ng_fill_kernel<T><<<(unsigned)blocks, threads, 0, h->stream>>>(q, col, ncol, h->N, both_slots<T>(h), off);
+    else simple_sine_kernel<T><<<(unsigned)blocks, threads, 0, h->stream>>>(q, h->N, both_slots<T>(h), off);
+}
+
+// Shared by the two sine families: checks, the table on the device, the
+// launches, the off-table count.
+int sine_ic_device(lat_handle* h, const lat_string_profile* prof, double eps, int64_t* off_table, bool ng,
+                   const char* fn)
+{
+    if (!h || !prof || !prof->phi || !prof->A) {
+        set_error(std::string(fn) + ": null argument");
+        return LAT_ERR_INVALID;
+    }
+    const lat_params& p = h->p;
+    if (p.model != LAT_MODEL_AH) {
+        set_error(std::string(fn) + ": Abelian-Higgs handles only");
+        return LAT_ERR_INVALID;
+    }
+    if (p.nx < 2 || p.ny < 2 || p.nz < 2 || prof->m < 2 || !(prof->h > 0)) {
+        set_error(std::string(fn) + ": sides >= 2, a profile of m >= 2 points and h > 0");
+        return LAT_ERR_INVALID;
+    }
+    if (!(eps >= 0 && eps < 1)) {
+        set_error(std::string(fn) + ": eps must lie in [0, 1)");
+        return LAT_ERR_INVALID;
+    }
+    SineArgs q;
+    q.nx = (int)p.nx;
+    q.ny = (int)p.ny;
+    q.nz = (int)p.nz;
+    q.x0 = (q.nx - 1) / 2;
+    q.y0 = (q.ny - 1) / 2;
+    q.z0 = (q.nz - 1) / 2;
+    q.dx = p.dx;
+    q.dy = p.dy;
+    q.dz = p.dz;
+    q.g = p.g;
+    q.eps = eps;
+    q.pi = 4 * std::atan(1.0);           // initialConditions.cpp:40
+    q.gr = 0.5 * (1 + std::sqrt(5.0));   // :50
+    if (ng) {
+        // Omega of a string periodic over dz*nz (:143-160), on the host with the reference's libm
+        double e = 0;
+        for (int j = 0; j < NG_NELLIP; j++) {
+            const double trap_fac = (j == 0 || j == NG_NELLIP - 1) ? 0.5 : 1;
+            const double theta = j * 2 * q.pi / (NG_NELLIP - 1);
+            e += trap_fac * std::sqrt(1 - std::pow(eps * std::sin(theta), 2)) * 2 * q.pi / (NG_NELLIP - 1);
+        }
+        q.Omega = e / (p.dz * (double)p.nz);
+    } else {
+        q.Omega = 2 * q.pi / (p.dz * (double)(p.nz - 1));   // :510
+    }
+    q.pr.m = prof->m;
+    q.pr.a = prof->h;
+    q.pr.winding = prof->winding;
+    q.pr.g = p.g;
+    const int ncol = ng ? q.nx * (q.nz - q.z0) : 0;
+
+    cudaError_t e = cudaSetDevice(h->device);
+    const size_t tab = sizeof(double) * (size_t)prof->m;
+    const size_t need = 2 * tab + sizeof(double) * 6 * (size_t)ncol + 64;
+    char* scratch = nullptr;
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&scratch, need, h->stream);
+    if (e != cudaSuccess) {
+        set_error(std::string(fn) + ": " + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? LAT_ERR_NOMEM : LAT_ERR_CUDA;
+    }
+    double* S0 = (double*)scratch;
+    double* S1 = S0 + prof->m;
+    double* col = S1 + prof->m;
+    unsigned long long* off = (unsigned long long*)(col + 6 * (size_t)ncol);
+    q.pr.S0 = S0;
+    q.pr.S1 = S1;
+    unsigned long long off_host = 0;
+    e = cudaMemcpyAsync(S0, prof->phi, tab, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(S1, prof->A, tab, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(off, 0, sizeof(unsigned long long), h->stream);
+    if (e == cudaSuccess) {
+        if (ng) ng_column_kernel<<<(ncol + 127) / 128, 128, 0, h->stream>>>(q, col, ncol);
+        if (h->elem == 8) sine_launch<double>(h, q, ng, col, ncol, off);
+        else sine_launch<float>(h, q, ng, col, ncol, off);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&off_host, off, sizeof(off_host), cudaMemcpyDeviceToHost, h->stream);
+    const cudaError_t ef = cudaFreeAsync(scratch, h->stream);
+    if (e == cudaSuccess) e = ef;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+        set_error(std::string(fn) + ": " + cudaGetErrorString(e));
+        return LAT_ERR_CUDA;
+    }
+    h->n = 0;
+    h->bc_level = -1;
+    h->div_valid = false;
+    h->launches += ng ? 2 : 1;
+    if (off_table) *off_table = (int64_t)off_host;
+    return LAT_OK;
+}
+
+}  // namespace
+
+}  // namespace lat
+
+extern "C" int lat_ng_sine_ic_device(lat_handle* h, const lat_string_profile* prof, double eps, int64_t* off_table)
+{
+    return lat::sine_ic_device(h, prof, eps, off_table, true, "lat_ng_sine_ic_device");
+}
+
+extern "C" int lat_simple_sine_ic_device(lat_handle* h, const lat_string_profile* prof, double eps,
+                                         int64_t* off_table)
+{
+    return lat::sine_ic_device(h, prof, eps, off_table, false, "lat_simple_sine_ic_device");
+}

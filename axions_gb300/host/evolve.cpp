@@ -218,6 +218,9 @@ Params::Params(Program prog)
         v["v1y"] = "0.5499090833947008";
         v["v1z"] = "0";
         for (const char* k : {"pos1s", "pos1a", "pos2s", "pos2a", "v1s", "v1a", "v2s", "v2a"}) v[k] = "";
+        // NG sine and simple sine (initialConditions.cpp:113-668): the sine
+        // amplitude, which the reference reads from standard input
+        v["eps"] = "";
         break;
     case Program::SingleSemiAnalytic:
         // singleSemiAnalytic.cpp:19-33; ic_type 0 starts from eta*tanh(r/2),
@@ -884,6 +887,50 @@ void string_ic_table(Params& q, const std::string& dir, StringIc kind, int form,
     }
 }
 
+// A perturbed straight string (initialConditions.cpp:113-668, "NG sine" or
+// "simple sine") built on the GPU from Data/SOR_Fields.txt (sor_file
+// overrides): one level, column-major [5][N].
+void sine_ic_table(Params& q, const std::string& dir, bool ng, std::vector<double>& tab)
+{
+    if (q.str("eps").empty()) fail("ic_type = \"" + q.str("ic_type") + "\" needs eps=<amplitude in [0, 1)>");
+    const int64_t m = q.integer("SORnx");
+    std::vector<double> prof;
+    std::string file = q.str("sor_file");
+    if (file.empty()) file = "Data/SOR_Fields.txt";
+    read_table(dir + "/" + file, 2, m, prof);
+    lat_params p;
+    check(lat_params_init(&p, LAT_MODEL_AH), "lat_params_init");
+    p.nx = q.integer("nx");
+    p.ny = q.integer("ny");
+    p.nz = q.integer("nz");
+    p.dx = q.num("dx");
+    p.dy = q.num("dy");
+    p.dz = q.num("dz");
+    p.dt = q.num("dt");
+    p.g = q.num("g");
+    p.precision = LAT_F64;
+    lat_handle* h = nullptr;
+    check(lat_create(&p, &h), "lat_create");
+    lat_string_profile sp;
+    sp.phi = prof.data();
+    sp.A = prof.data() + m;
+    sp.m = m;
+    sp.h = q.num("SORa");
+    sp.winding = q.num("n");
+    int64_t off = 0;
+    const int rc = ng ? lat_ng_sine_ic_device(h, &sp, q.num("eps"), &off)
+                      : lat_simple_sine_ic_device(h, &sp, q.num("eps"), &off);
+    if (rc != LAT_OK) {
+        lat_destroy(h);
+        check(rc, ng ? "lat_ng_sine_ic_device" : "lat_simple_sine_ic_device");
+    }
+    const int64_t N = p.nx * p.ny * p.nz;
+    tab.assign((size_t)5 * N, 0.0);
+    check(lat_get_state(h, tab.data(), nullptr), "lat_get_state");
+    lat_destroy(h);
+    if (off) std::cout << "Off straight string solution grid at " << off << " site evaluations" << std::endl;
+}
+
 // initialConditions.cpp:670-708 ("random"): per site in linear order phi_re,
 // phi_im from normal_distribution<double>(mean, stdev) over
 // default_random_engine(seed); the link columns are dmu*g*A with A = 0.
@@ -918,13 +965,16 @@ int run_initial_conditions(Params& q)
     } else if (type == "boost" || type == "loop collision") {
         string_ic_table(q, dir, type == "boost" ? StringIc::Boost : StringIc::LoopCollision, LAT_IC_FORM_FILE, tab);
         rows = 2 * N;
+    } else if (type == "NG sine" || type == "simple sine") {
+        sine_ic_table(q, dir, type == "NG sine", tab);
     } else if (type == "convert") {
         cols = (int)q.integer("cols");
         rows = q.integer("levels") * N;
         if (q.str("ic_in").empty()) fail("ic_type = convert needs ic_in");
         read_table(dir + "/Data/" + q.str("ic_in"), cols, rows, tab);
     } else {
-        fail("ic_type: this program provides \"random\", \"boost\", \"loop collision\" and \"convert\"");
+        fail("ic_type: this program provides \"random\", \"NG sine\", \"simple sine\", \"boost\", "
+             "\"loop collision\" and \"convert\"");
     }
     if (ends_with(out, ".bin")) write_table_bin(out, cols, rows, tab.data());
     else write_table_text(out, cols, rows, tab.data(), digits);

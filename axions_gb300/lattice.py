@@ -32,7 +32,8 @@ EXPORTS = [
     "lat_ah_step_f64_noalloc",
     "lat_batch_create", "lat_batch_destroy", "lat_batch_add", "lat_batch_remove", "lat_batch_size",
     "lat_batch_kernel_launches", "lat_batch_set_chunk", "lat_batch_advance", "lat_batch_take_diags",
-    "lat_random_phase_ic_device", "lat_boost_ic_device", "lat_loop_collision_ic_device", "lat_philox4x32_10", "lat_dtrig_eval", "lat_autotune", "lat_get_tuning", "lat_set_tuning",
+    "lat_random_phase_ic_device", "lat_boost_ic_device", "lat_loop_collision_ic_device",
+    "lat_ng_sine_ic_device", "lat_simple_sine_ic_device", "lat_philox4x32_10", "lat_dtrig_eval", "lat_autotune", "lat_get_tuning", "lat_set_tuning",
     "lat_tune_cache_save", "lat_tune_cache_load", "lat_footprint_bytes",
     "lat_server_create", "lat_server_submit", "lat_server_poll", "lat_server_wait", "lat_server_diags",
     "lat_server_get_stats", "lat_server_destroy",
@@ -120,6 +121,8 @@ def load_library(path: Path | None = None):
     L.lat_random_phase_ic_device.argtypes = [vp, ctypes.c_uint64, ctypes.c_int32]
     L.lat_boost_ic_device.argtypes = [vp, vp, vp, P(ctypes.c_int64)]
     L.lat_loop_collision_ic_device.argtypes = [vp, vp, vp, P(ctypes.c_int64)]
+    L.lat_ng_sine_ic_device.argtypes = [vp, vp, ctypes.c_double, P(ctypes.c_int64)]
+    L.lat_simple_sine_ic_device.argtypes = [vp, vp, ctypes.c_double, P(ctypes.c_int64)]
     L.lat_philox4x32_10.argtypes = [u32p, u32p, u32p]
     L.lat_dtrig_eval.argtypes = [dp, ctypes.c_int64, dp]
     L.lat_autotune.argtypes = [vp, ctypes.c_int32, P(LatTuning)]
@@ -272,6 +275,20 @@ class Lattice:
         off = ctypes.c_int64(0)
         _check("lat_loop_collision_ic_device",
                self.L.lat_loop_collision_ic_device(self.h, ctypes.byref(prof), ctypes.byref(c), ctypes.byref(off)))
+        del keep
+        return int(off.value)
+
+    def sine_string_ic_device(self, phi, A, h: float, eps: float, kind: str = "NG sine",
+                              winding: float = 1.0) -> int:
+        """A straight string perturbed by a sine wave (initialConditions.cpp
+        "NG sine" :113-486 or "simple sine" :488-668, amplitude eps) from the
+        profile table (phi, A) with spacing h, built on the GPU into both slots;
+        state at TimeStep 0.  Returns the number of evaluations beyond the table."""
+        from .params import string_profile
+        fn = {"NG sine": "lat_ng_sine_ic_device", "simple sine": "lat_simple_sine_ic_device"}[kind]
+        prof, keep = string_profile(phi, A, h, winding)
+        off = ctypes.c_int64(0)
+        _check(fn, getattr(self.L, fn)(self.h, ctypes.byref(prof), float(eps), ctypes.byref(off)))
         del keep
         return int(off.value)
 

@@ -331,8 +331,9 @@ def measure_gpu(n: int, precision: str, steps: int, warmup: int, ws: int, local:
     kern_ms = statistics.median(plain)
 
     # end to end through the C ABI with host buffers (pinned): one lat_run call
-    # from the IC (both levels equal)
-    pin_past = pin_now
+    # from the IC (both levels equal, in two buffers as a caller holds them)
+    pin_past = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
+    pin_past.numpy()[:] = pin_now.numpy()
     out_now = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
     out_past = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
     dist_barrier(ws)

@@ -387,6 +387,21 @@ typedef struct lat_loop_collision_ic {
 
 int lat_loop_collision_ic_device(lat_handle* h, const lat_string_profile* prof, const lat_loop_collision_ic* c,
                                  int64_t* off_table);
+/* Straight strings perturbed by a sine wave of amplitude eps in [0, 1) (the
+ * value the reference reads from standard input), built on the device from
+ * the profile table into both slots of an Abelian-Higgs handle (one level, as
+ * the reference's Data/ic.txt); time step 0.  Sides >= 2.
+ *   lat_ng_sine_ic_device     "NG sine", initialConditions.cpp:113-486: a
+ *       Nambu-Goto sine wave along z, Omega set so that it is periodic over
+ *       dz*nz; per (x, z) column with z >= 0 a golden-section search to 1e-6
+ *       for the closest string point; the z < 0 half mirrored as the
+ *       reference's loop leaves it.
+ *   lat_simple_sine_ic_device "simple sine", :488-668: the straight string
+ *       offset along x by eps*sin(Omega z)/Omega, Omega = 2 pi/(dz (nz-1)).
+ * off_table (may be null) receives the evaluations beyond the table. */
+int lat_ng_sine_ic_device(lat_handle* h, const lat_string_profile* prof, double eps, int64_t* off_table);
+int lat_simple_sine_ic_device(lat_handle* h, const lat_string_profile* prof, double eps, int64_t* off_table);
+
 /* The generator on the host (checks, reproduction of device ICs). */
 int lat_philox4x32_10(const uint32_t counter[4], const uint32_t key[2], uint32_t out[4]);
 

@@ -180,6 +180,28 @@ static void friction_of(const lat_params* p, int64_t n, double* damp, double* fr
 #define TH(m, t, s) ST(2 + (m), t, s)
 #define PH(c, t, s) ST(c, t, s)
 
+/* Sensitivity probe (test infrastructure): with orc_set_trig_perturbation(f)
+ * and f > 0, the sine and cosine of the step, the diagnostics and the
+ * boundaries return glibc's value moved by one ulp for a fraction f of their
+ * arguments (chosen by a hash of the argument's bits, so the choice does not
+ * depend on threads or order).  f = 0 (the default) leaves every value as the
+ * reference's. */
+static double g_trig_perturb = 0.0;
+void orc_set_trig_perturbation(double frac) { g_trig_perturb = frac; }
+static inline double trig_bump(double x, double y)
+{
+    uint64_t z;
+    memcpy(&z, &x, 8);
+    z += 0x9e3779b97f4a7c15ULL;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    z ^= z >> 31;
+    if ((double)(z >> 11) * (1.0 / 9007199254740992.0) >= g_trig_perturb) return y;
+    return nextafter(y, (z & 1) ? INFINITY : -INFINITY);
+}
+static inline double psin(double x) { const double y = sin(x); return g_trig_perturb > 0 ? trig_bump(x, y) : y; }
+static inline double pcos(double x) { const double y = cos(x); return g_trig_perturb > 0 ? trig_bump(x, y) : y; }
+
 static void neumann_pair(double* st, int64_t N, int tNow, int mu, int64_t b0, int64_t i0, int64_t b1, int64_t i1)
 {
     const int c[2] = {1, -1};
@@ -190,8 +212,8 @@ static void neumann_pair(double* st, int64_t N, int tNow, int mu, int64_t b0, in
     for (int comp = 0; comp < 2; ++comp) {
         const int oc = comp + c[comp];
         const double cc = (double)c[comp];
-        PH(comp, tNow, b0) = cos(TH(mu, tNow, b0)) * PH(comp, tNow, i0) + cc * sin(TH(mu, tNow, b0)) * PH(oc, tNow, i0);
-        PH(comp, tNow, b1) = cos(TH(mu, tNow, i1)) * PH(comp, tNow, i1) - cc * sin(TH(mu, tNow, i1)) * PH(oc, tNow, i1);
+        PH(comp, tNow, b0) = pcos(TH(mu, tNow, b0)) * PH(comp, tNow, i0) + cc * psin(TH(mu, tNow, b0)) * PH(oc, tNow, i0);
+        PH(comp, tNow, b1) = pcos(TH(mu, tNow, i1)) * PH(comp, tNow, i1) - cc * psin(TH(mu, tNow, i1)) * PH(oc, tNow, i1);
     }
 }
 
@@ -210,8 +232,8 @@ static void neumann_pair_moore(const lat_params* p, double* st, int64_t N, int t
         for (int a = 0; a < 2; ++a) {
             const double q = a == 0 ? p->q1 : p->q2;
             const int f = 2 * a + comp, o = 2 * a + comp + c[comp];
-            ST(f, tNow, b0) = cos(q * ST(4 + mu, tNow, b0)) * ST(f, tNow, i0) + cc * sin(q * ST(4 + mu, tNow, b0)) * ST(o, tNow, i0);
-            ST(f, tNow, b1) = cos(q * ST(4 + mu, tNow, i1)) * ST(f, tNow, i1) - cc * sin(q * ST(4 + mu, tNow, i1)) * ST(o, tNow, i1);
+            ST(f, tNow, b0) = pcos(q * ST(4 + mu, tNow, b0)) * ST(f, tNow, i0) + cc * psin(q * ST(4 + mu, tNow, b0)) * ST(o, tNow, i0);
+            ST(f, tNow, b1) = pcos(q * ST(4 + mu, tNow, i1)) * ST(f, tNow, i1) - cc * psin(q * ST(4 + mu, tNow, i1)) * ST(o, tNow, i1);
         }
     }
 }
@@ -268,8 +290,8 @@ static double cov2(const double* st, int64_t N, int tNow, int comp, int mu, int6
     const int c[2] = {1, -1};
     const int oc = comp + c[comp];
     const double cc = (double)c[comp];
-    return (cos(TH(mu, tNow, s)) * PH(comp, tNow, sp) + cc * sin(TH(mu, tNow, s)) * PH(oc, tNow, sp) - 2 * PH(comp, tNow, s)
-            + cos(TH(mu, tNow, sm)) * PH(comp, tNow, sm) - cc * sin(TH(mu, tNow, sm)) * PH(oc, tNow, sm)) / (d * d);
+    return (pcos(TH(mu, tNow, s)) * PH(comp, tNow, sp) + cc * psin(TH(mu, tNow, s)) * PH(oc, tNow, sp) - 2 * PH(comp, tNow, s)
+            + pcos(TH(mu, tNow, sm)) * PH(comp, tNow, sm) - cc * psin(TH(mu, tNow, sm)) * PH(oc, tNow, sm)) / (d * d);
 }
 
 /* one-sided time-space difference at the low face: s0 boundary, s1 = s0 + mu */
@@ -279,8 +301,8 @@ static double near_ts(const double* st, int64_t N, int tNow, int tPast, int comp
     const int c[2] = {1, -1};
     const int oc = comp + c[comp];
     const double cc = (double)c[comp];
-    return (cos(TH(mu, tNow, s0)) * PH(comp, tNow, s1) + cc * sin(TH(mu, tNow, s0)) * PH(oc, tNow, s1) - PH(comp, tNow, s0)
-            - cos(TH(mu, tPast, s0)) * PH(comp, tPast, s1) - cc * sin(TH(mu, tPast, s0)) * PH(oc, tPast, s1)
+    return (pcos(TH(mu, tNow, s0)) * PH(comp, tNow, s1) + cc * psin(TH(mu, tNow, s0)) * PH(oc, tNow, s1) - PH(comp, tNow, s0)
+            - pcos(TH(mu, tPast, s0)) * PH(comp, tPast, s1) - cc * psin(TH(mu, tPast, s0)) * PH(oc, tPast, s1)
             + PH(comp, tPast, s0)) / (dt * d);
 }
 
@@ -292,9 +314,9 @@ static double far_ts(const double* st, int64_t N, int tNow, int tPast, int comp,
     const int c[2] = {1, -1};
     const int oc = comp + c[comp];
     const double cc = (double)c[comp];
-    return (PH(comp, tNow, s0) - cos(TH(mu, tNow, s1)) * PH(comp, tNow, s1) + cc * sin(TH(mu, tNow, s1)) * PH(oc, tNow, s1)
-            - PH(comp, tPast, s0) + cos(TH(mu, tPast, sc)) * PH(comp, tPast, s1)
-            - cc * sin(TH(mu, tPast, s1)) * PH(oc, tPast, s1)) / (dt * d);
+    return (PH(comp, tNow, s0) - pcos(TH(mu, tNow, s1)) * PH(comp, tNow, s1) + cc * psin(TH(mu, tNow, s1)) * PH(oc, tNow, s1)
+            - PH(comp, tPast, s0) + pcos(TH(mu, tPast, sc)) * PH(comp, tPast, s1)
+            - cc * psin(TH(mu, tPast, s1)) * PH(oc, tPast, s1)) / (dt * d);
 }
 
 static double th2(const double* st, int64_t N, int tNow, int m, int64_t sp, int64_t s, int64_t sm, double d)
@@ -473,12 +495,12 @@ static void ah_update(const lat_params* p, double* st, int64_t n)
                 for (int comp = 0; comp < 2; ++comp) {
                     const int oc = comp + c[comp];
                     const double cc = (double)c[comp];
-                    double phixx = (cos(ST(2, tNow, s)) * ST(comp, tNow, ipx) + cc * sin(ST(2, tNow, s)) * ST(oc, tNow, ipx) - 2 * ST(comp, tNow, s)
-                                    + cos(ST(2, tNow, imx)) * ST(comp, tNow, imx) - cc * sin(ST(2, tNow, imx)) * ST(oc, tNow, imx)) / (dx * dx);
-                    double phiyy = (cos(ST(3, tNow, s)) * ST(comp, tNow, ipy) + cc * sin(ST(3, tNow, s)) * ST(oc, tNow, ipy) - 2 * ST(comp, tNow, s)
-                                    + cos(ST(3, tNow, imy)) * ST(comp, tNow, imy) - cc * sin(ST(3, tNow, imy)) * ST(oc, tNow, imy)) / (dy * dy);
-                    double phizz = (cos(ST(4, tNow, s)) * ST(comp, tNow, ipz) + cc * sin(ST(4, tNow, s)) * ST(oc, tNow, ipz) - 2 * ST(comp, tNow, s)
-                                    + cos(ST(4, tNow, imz)) * ST(comp, tNow, imz) - cc * sin(ST(4, tNow, imz)) * ST(oc, tNow, imz)) / (dz * dz);
+                    double phixx = (pcos(ST(2, tNow, s)) * ST(comp, tNow, ipx) + cc * psin(ST(2, tNow, s)) * ST(oc, tNow, ipx) - 2 * ST(comp, tNow, s)
+                                    + pcos(ST(2, tNow, imx)) * ST(comp, tNow, imx) - cc * psin(ST(2, tNow, imx)) * ST(oc, tNow, imx)) / (dx * dx);
+                    double phiyy = (pcos(ST(3, tNow, s)) * ST(comp, tNow, ipy) + cc * psin(ST(3, tNow, s)) * ST(oc, tNow, ipy) - 2 * ST(comp, tNow, s)
+                                    + pcos(ST(3, tNow, imy)) * ST(comp, tNow, imy) - cc * psin(ST(3, tNow, imy)) * ST(oc, tNow, imy)) / (dy * dy);
+                    double phizz = (pcos(ST(4, tNow, s)) * ST(comp, tNow, ipz) + cc * psin(ST(4, tNow, s)) * ST(oc, tNow, ipz) - 2 * ST(comp, tNow, s)
+                                    + pcos(ST(4, tNow, imz)) * ST(comp, tNow, imz) - cc * psin(ST(4, tNow, imz)) * ST(oc, tNow, imz)) / (dz * dz);
                     double phitt = phixx + phiyy + phizz - 0.5 * lambda * (phiMagSqr - eta * eta) * ST(comp, tNow, s);
                     if (fric != 0) {
                         double phit = (ST(comp, tNow, s) - ST(comp, tPast, s)) / dt;
@@ -487,25 +509,25 @@ static void ah_update(const lat_params* p, double* st, int64_t n)
                     ST(comp, tPast, s) = 2 * ST(comp, tNow, s) - ST(comp, tPast, s) + dt * dt * phitt;
                 }
 
-                double curx = cos(ST(2, tNow, s)) * (ST(1, tNow, s) * ST(0, tNow, ipx) - ST(0, tNow, s) * ST(1, tNow, ipx))
-                            + sin(ST(2, tNow, s)) * (ST(0, tNow, s) * ST(0, tNow, ipx) + ST(1, tNow, s) * ST(1, tNow, ipx));
-                double cury = cos(ST(3, tNow, s)) * (ST(1, tNow, s) * ST(0, tNow, ipy) - ST(0, tNow, s) * ST(1, tNow, ipy))
-                            + sin(ST(3, tNow, s)) * (ST(0, tNow, s) * ST(0, tNow, ipy) + ST(1, tNow, s) * ST(1, tNow, ipy));
-                double curz = cos(ST(4, tNow, s)) * (ST(1, tNow, s) * ST(0, tNow, ipz) - ST(0, tNow, s) * ST(1, tNow, ipz))
-                            + sin(ST(4, tNow, s)) * (ST(0, tNow, s) * ST(0, tNow, ipz) + ST(1, tNow, s) * ST(1, tNow, ipz));
+                double curx = pcos(ST(2, tNow, s)) * (ST(1, tNow, s) * ST(0, tNow, ipx) - ST(0, tNow, s) * ST(1, tNow, ipx))
+                            + psin(ST(2, tNow, s)) * (ST(0, tNow, s) * ST(0, tNow, ipx) + ST(1, tNow, s) * ST(1, tNow, ipx));
+                double cury = pcos(ST(3, tNow, s)) * (ST(1, tNow, s) * ST(0, tNow, ipy) - ST(0, tNow, s) * ST(1, tNow, ipy))
+                            + psin(ST(3, tNow, s)) * (ST(0, tNow, s) * ST(0, tNow, ipy) + ST(1, tNow, s) * ST(1, tNow, ipy));
+                double curz = pcos(ST(4, tNow, s)) * (ST(1, tNow, s) * ST(0, tNow, ipz) - ST(0, tNow, s) * ST(1, tNow, ipz))
+                            + psin(ST(4, tNow, s)) * (ST(0, tNow, s) * ST(0, tNow, ipz) + ST(1, tNow, s) * ST(1, tNow, ipz));
 
-                double Fxy_y = (sin(ST(2, tNow, s) + ST(3, tNow, ipx) - ST(2, tNow, ipy) - ST(3, tNow, s))
-                              - sin(ST(2, tNow, imy) + ST(3, tNow, ipxmy) - ST(2, tNow, s) - ST(3, tNow, imy))) / (dy * dy);
-                double Fxz_z = (sin(ST(2, tNow, s) + ST(4, tNow, ipx) - ST(2, tNow, ipz) - ST(4, tNow, s))
-                              - sin(ST(2, tNow, imz) + ST(4, tNow, ipxmz) - ST(2, tNow, s) - ST(4, tNow, imz))) / (dz * dz);
-                double Fyx_x = (sin(ST(3, tNow, s) + ST(2, tNow, ipy) - ST(3, tNow, ipx) - ST(2, tNow, s))
-                              - sin(ST(3, tNow, imx) + ST(2, tNow, imxpy) - ST(3, tNow, s) - ST(2, tNow, imx))) / (dx * dx);
-                double Fyz_z = (sin(ST(3, tNow, s) + ST(4, tNow, ipy) - ST(3, tNow, ipz) - ST(4, tNow, s))
-                              - sin(ST(3, tNow, imz) + ST(4, tNow, ipymz) - ST(3, tNow, s) - ST(4, tNow, imz))) / (dz * dz);
-                double Fzx_x = (sin(ST(4, tNow, s) + ST(2, tNow, ipz) - ST(4, tNow, ipx) - ST(2, tNow, s))
-                              - sin(ST(4, tNow, imx) + ST(2, tNow, imxpz) - ST(4, tNow, s) - ST(2, tNow, imx))) / (dx * dx);
-                double Fzy_y = (sin(ST(4, tNow, s) + ST(3, tNow, ipz) - ST(4, tNow, ipy) - ST(3, tNow, s))
-                              - sin(ST(4, tNow, imy) + ST(3, tNow, imypz) - ST(4, tNow, s) - ST(3, tNow, imy))) / (dy * dy);
+                double Fxy_y = (psin(ST(2, tNow, s) + ST(3, tNow, ipx) - ST(2, tNow, ipy) - ST(3, tNow, s))
+                              - psin(ST(2, tNow, imy) + ST(3, tNow, ipxmy) - ST(2, tNow, s) - ST(3, tNow, imy))) / (dy * dy);
+                double Fxz_z = (psin(ST(2, tNow, s) + ST(4, tNow, ipx) - ST(2, tNow, ipz) - ST(4, tNow, s))
+                              - psin(ST(2, tNow, imz) + ST(4, tNow, ipxmz) - ST(2, tNow, s) - ST(4, tNow, imz))) / (dz * dz);
+                double Fyx_x = (psin(ST(3, tNow, s) + ST(2, tNow, ipy) - ST(3, tNow, ipx) - ST(2, tNow, s))
+                              - psin(ST(3, tNow, imx) + ST(2, tNow, imxpy) - ST(3, tNow, s) - ST(2, tNow, imx))) / (dx * dx);
+                double Fyz_z = (psin(ST(3, tNow, s) + ST(4, tNow, ipy) - ST(3, tNow, ipz) - ST(4, tNow, s))
+                              - psin(ST(3, tNow, imz) + ST(4, tNow, ipymz) - ST(3, tNow, s) - ST(4, tNow, imz))) / (dz * dz);
+                double Fzx_x = (psin(ST(4, tNow, s) + ST(2, tNow, ipz) - ST(4, tNow, ipx) - ST(2, tNow, s))
+                              - psin(ST(4, tNow, imx) + ST(2, tNow, imxpz) - ST(4, tNow, s) - ST(2, tNow, imx))) / (dx * dx);
+                double Fzy_y = (psin(ST(4, tNow, s) + ST(3, tNow, ipz) - ST(4, tNow, ipy) - ST(3, tNow, s))
+                              - psin(ST(4, tNow, imy) + ST(3, tNow, imypz) - ST(4, tNow, s) - ST(3, tNow, imy))) / (dy * dy);
 
                 double tt[3];
                 tt[0] = -2 * g * g * curx - Fxy_y - Fxz_z;
@@ -558,21 +580,21 @@ static void ah_diag(const lat_params* p, const double* st, int64_t n, lat_diag* 
                     const int oc = comp + c[comp];
                     const double cc = (double)c[comp];
                     phit[comp] = (ST(comp, tNow, s) - ST(comp, tPast, s)) / dt;
-                    phix[comp] = (ST(comp, tNow, s) - cos(ST(2, tNow, imx)) * ST(comp, tNow, imx) + cc * sin(ST(2, tNow, imx)) * ST(oc, tNow, imx)) / dx;
-                    phiy[comp] = (ST(comp, tNow, s) - cos(ST(3, tNow, imy)) * ST(comp, tNow, imy) + cc * sin(ST(3, tNow, imy)) * ST(oc, tNow, imy)) / dy;
-                    phiz[comp] = (ST(comp, tNow, s) - cos(ST(4, tNow, imz)) * ST(comp, tNow, imz) + cc * sin(ST(4, tNow, imz)) * ST(oc, tNow, imz)) / dz;
+                    phix[comp] = (ST(comp, tNow, s) - pcos(ST(2, tNow, imx)) * ST(comp, tNow, imx) + cc * psin(ST(2, tNow, imx)) * ST(oc, tNow, imx)) / dx;
+                    phiy[comp] = (ST(comp, tNow, s) - pcos(ST(3, tNow, imy)) * ST(comp, tNow, imy) + cc * psin(ST(3, tNow, imy)) * ST(oc, tNow, imy)) / dy;
+                    phiz[comp] = (ST(comp, tNow, s) - pcos(ST(4, tNow, imz)) * ST(comp, tNow, imz) + cc * psin(ST(4, tNow, imz)) * ST(oc, tNow, imz)) / dz;
                 }
                 double Pxy = ST(2, tNow, s) + ST(3, tNow, ipx) - ST(2, tNow, ipy) - ST(3, tNow, s);
                 double Pxz = ST(2, tNow, s) + ST(4, tNow, ipx) - ST(2, tNow, ipz) - ST(4, tNow, s);
                 double Pyz = ST(3, tNow, s) + ST(4, tNow, ipy) - ST(3, tNow, ipz) - ST(4, tNow, s);
-                double gauss = 0, thetaDotCont, FCont;
+                double gauss = 0, thetaDotCont = 0, FCont = 0;
                 if (mpi_form) {
                     double t0 = (ST(2, tNow, s) - ST(2, tPast, s)) / dt;
                     double t1 = (ST(3, tNow, s) - ST(3, tPast, s)) / dt;
                     double t2 = (ST(4, tNow, s) - ST(4, tPast, s)) / dt;
                     thetaDotCont = 0.5 * (t0 * t0 + t1 * t1 + t2 * t2);
                     double gxy = g * dx * dy, gxz = g * dx * dz, gyz = g * dy * dz;
-                    FCont = (1 - cos(Pxy)) / (gxy * gxy) + (1 - cos(Pxz)) / (gxz * gxz) + (1 - cos(Pyz)) / (gyz * gyz);
+                    FCont = (1 - pcos(Pxy)) / (gxy * gxy) + (1 - pcos(Pxz)) / (gxz * gxz) + (1 - pcos(Pyz)) / (gyz * gyz);
                 }
                 if (g != 0) {
                     double divNow = (ST(2, tNow, s) - ST(2, tNow, imx)) / (dx * dx) + (ST(3, tNow, s) - ST(3, tNow, imy)) / (dy * dy)
@@ -587,9 +609,9 @@ static void ah_diag(const lat_params* p, const double* st, int64_t n, lat_diag* 
                         double t2 = (ST(4, tNow, s) - ST(4, tPast, s)) / (g * dt * dz);
                         thetaDotCont = 0.5 * (t0 * t0 + t1 * t1 + t2 * t2);
                         double gxy = g * dx * dy, gxz = g * dx * dz, gyz = g * dy * dz;
-                        double Fxy = (1 - cos(Pxy)) / (gxy * gxy);
-                        double Fxz = (1 - cos(Pxz)) / (gxz * gxz);
-                        double Fyz = (1 - cos(Pyz)) / (gyz * gyz);
+                        double Fxy = (1 - pcos(Pxy)) / (gxy * gxy);
+                        double Fxz = (1 - pcos(Pxz)) / (gxz * gxz);
+                        double Fyz = (1 - pcos(Pyz)) / (gyz * gyz);
                         FCont = Fxy + Fxz + Fyz;
                     }
                 } else if (!mpi_form) {
@@ -660,9 +682,9 @@ static void moore_update(const lat_params* p, double* st, int64_t n)
                         double lap[3];
                         for (int m = 0; m < 3; ++m) {
                             const int64_t pp = nb[m][0], mm = nb[m][1];
-                            lap[m] = (cos(qf * ST(TH(m), tNow, s)) * ST(PH(f, comp), tNow, pp) + cc * sin(qf * ST(TH(m), tNow, s)) * ST(PH(f, oc), tNow, pp)
+                            lap[m] = (pcos(qf * ST(TH(m), tNow, s)) * ST(PH(f, comp), tNow, pp) + cc * psin(qf * ST(TH(m), tNow, s)) * ST(PH(f, oc), tNow, pp)
                                       - 2 * ST(PH(f, comp), tNow, s)
-                                      + cos(qf * ST(TH(m), tNow, mm)) * ST(PH(f, comp), tNow, mm) - cc * sin(qf * ST(TH(m), tNow, mm)) * ST(PH(f, oc), tNow, mm)) / d2[m];
+                                      + pcos(qf * ST(TH(m), tNow, mm)) * ST(PH(f, comp), tNow, mm) - cc * psin(qf * ST(TH(m), tNow, mm)) * ST(PH(f, oc), tNow, mm)) / d2[m];
                         }
                         double pot = (f == 0) ? (0.5 * l1 * (mag[0] - e1 * e1) + 0.5 * l12 * (mag[1] - e2 * e2))
                                               : (0.5 * l2 * (mag[1] - e2 * e2) + 0.5 * l12 * (mag[0] - e1 * e1));
@@ -681,25 +703,25 @@ static void moore_update(const lat_params* p, double* st, int64_t n)
                     double cf[2];
                     for (int f = 0; f < 2; ++f) {
                         const double qf = q[f];
-                        double v = cos(qf * ST(TH(m), tNow, s)) * (ST(PH(f, 1), tNow, s) * ST(PH(f, 0), tNow, pp) - ST(PH(f, 0), tNow, s) * ST(PH(f, 1), tNow, pp))
-                                 + sin(qf * ST(TH(m), tNow, s)) * (ST(PH(f, 0), tNow, s) * ST(PH(f, 0), tNow, pp) + ST(PH(f, 1), tNow, s) * ST(PH(f, 1), tNow, pp));
+                        double v = pcos(qf * ST(TH(m), tNow, s)) * (ST(PH(f, 1), tNow, s) * ST(PH(f, 0), tNow, pp) - ST(PH(f, 0), tNow, s) * ST(PH(f, 1), tNow, pp))
+                                 + psin(qf * ST(TH(m), tNow, s)) * (ST(PH(f, 0), tNow, s) * ST(PH(f, 0), tNow, pp) + ST(PH(f, 1), tNow, s) * ST(PH(f, 1), tNow, pp));
                         cf[f] = charge ? qf * v : v;
                     }
                     cur[m] = cf[0] + cf[1];
                 }
 
-                double Fxy_y = (sin(ST(TH(0), tNow, s) + ST(TH(1), tNow, ipx) - ST(TH(0), tNow, ipy) - ST(TH(1), tNow, s))
-                              - sin(ST(TH(0), tNow, imy) + ST(TH(1), tNow, ipxmy) - ST(TH(0), tNow, s) - ST(TH(1), tNow, imy))) / (dy * dy);
-                double Fxz_z = (sin(ST(TH(0), tNow, s) + ST(TH(2), tNow, ipx) - ST(TH(0), tNow, ipz) - ST(TH(2), tNow, s))
-                              - sin(ST(TH(0), tNow, imz) + ST(TH(2), tNow, ipxmz) - ST(TH(0), tNow, s) - ST(TH(2), tNow, imz))) / (dz * dz);
-                double Fyx_x = (sin(ST(TH(1), tNow, s) + ST(TH(0), tNow, ipy) - ST(TH(1), tNow, ipx) - ST(TH(0), tNow, s))
-                              - sin(ST(TH(1), tNow, imx) + ST(TH(0), tNow, imxpy) - ST(TH(1), tNow, s) - ST(TH(0), tNow, imx))) / (dx * dx);
-                double Fyz_z = (sin(ST(TH(1), tNow, s) + ST(TH(2), tNow, ipy) - ST(TH(1), tNow, ipz) - ST(TH(2), tNow, s))
-                              - sin(ST(TH(1), tNow, imz) + ST(TH(2), tNow, ipymz) - ST(TH(1), tNow, s) - ST(TH(2), tNow, imz))) / (dz * dz);
-                double Fzx_x = (sin(ST(TH(2), tNow, s) + ST(TH(0), tNow, ipz) - ST(TH(2), tNow, ipx) - ST(TH(0), tNow, s))
-                              - sin(ST(TH(2), tNow, imx) + ST(TH(0), tNow, imxpz) - ST(TH(2), tNow, s) - ST(TH(0), tNow, imx))) / (dx * dx);
-                double Fzy_y = (sin(ST(TH(2), tNow, s) + ST(TH(1), tNow, ipz) - ST(TH(2), tNow, ipy) - ST(TH(1), tNow, s))
-                              - sin(ST(TH(2), tNow, imy) + ST(TH(1), tNow, imypz) - ST(TH(2), tNow, s) - ST(TH(1), tNow, imy))) / (dy * dy);
+                double Fxy_y = (psin(ST(TH(0), tNow, s) + ST(TH(1), tNow, ipx) - ST(TH(0), tNow, ipy) - ST(TH(1), tNow, s))
+                              - psin(ST(TH(0), tNow, imy) + ST(TH(1), tNow, ipxmy) - ST(TH(0), tNow, s) - ST(TH(1), tNow, imy))) / (dy * dy);
+                double Fxz_z = (psin(ST(TH(0), tNow, s) + ST(TH(2), tNow, ipx) - ST(TH(0), tNow, ipz) - ST(TH(2), tNow, s))
+                              - psin(ST(TH(0), tNow, imz) + ST(TH(2), tNow, ipxmz) - ST(TH(0), tNow, s) - ST(TH(2), tNow, imz))) / (dz * dz);
+                double Fyx_x = (psin(ST(TH(1), tNow, s) + ST(TH(0), tNow, ipy) - ST(TH(1), tNow, ipx) - ST(TH(0), tNow, s))
+                              - psin(ST(TH(1), tNow, imx) + ST(TH(0), tNow, imxpy) - ST(TH(1), tNow, s) - ST(TH(0), tNow, imx))) / (dx * dx);
+                double Fyz_z = (psin(ST(TH(1), tNow, s) + ST(TH(2), tNow, ipy) - ST(TH(1), tNow, ipz) - ST(TH(2), tNow, s))
+                              - psin(ST(TH(1), tNow, imz) + ST(TH(2), tNow, ipymz) - ST(TH(1), tNow, s) - ST(TH(2), tNow, imz))) / (dz * dz);
+                double Fzx_x = (psin(ST(TH(2), tNow, s) + ST(TH(0), tNow, ipz) - ST(TH(2), tNow, ipx) - ST(TH(0), tNow, s))
+                              - psin(ST(TH(2), tNow, imx) + ST(TH(0), tNow, imxpz) - ST(TH(2), tNow, s) - ST(TH(0), tNow, imx))) / (dx * dx);
+                double Fzy_y = (psin(ST(TH(2), tNow, s) + ST(TH(1), tNow, ipz) - ST(TH(2), tNow, ipy) - ST(TH(1), tNow, s))
+                              - psin(ST(TH(2), tNow, imy) + ST(TH(1), tNow, imypz) - ST(TH(2), tNow, s) - ST(TH(1), tNow, imy))) / (dy * dy);
 
                 double tt[3];
                 tt[0] = -2 * g * g * cur[0] - Fxy_y - Fxz_z;
@@ -757,8 +779,8 @@ static void moore_diag(const lat_params* p, const double* st, int64_t n, lat_dia
                         pt[f][comp] = (ST(PH(f, comp), tNow, s) - ST(PH(f, comp), tPast, s)) / dt;
                         for (int m = 0; m < 3; ++m) {
                             const int64_t mm = mmv[m];
-                            pd[f][m][comp] = (ST(PH(f, comp), tNow, s) - cos(qf * ST(TH(m), tNow, mm)) * ST(PH(f, comp), tNow, mm)
-                                              + cc * sin(qf * ST(TH(m), tNow, mm)) * ST(PH(f, oc), tNow, mm)) / dd[m];
+                            pd[f][m][comp] = (ST(PH(f, comp), tNow, s) - pcos(qf * ST(TH(m), tNow, mm)) * ST(PH(f, comp), tNow, mm)
+                                              + cc * psin(qf * ST(TH(m), tNow, mm)) * ST(PH(f, oc), tNow, mm)) / dd[m];
                         }
                     }
                 }
@@ -772,7 +794,7 @@ static void moore_diag(const lat_params* p, const double* st, int64_t n, lat_dia
                     double t2 = (ST(TH(2), tNow, s) - ST(TH(2), tPast, s)) / dt;
                     thetaDotCont = 0.5 * (t0 * t0 + t1 * t1 + t2 * t2);
                     double gxy = g * dx * dy, gxz = g * dx * dz, gyz = g * dy * dz;
-                    FCont = (1 - cos(Pxy)) / (gxy * gxy) + (1 - cos(Pxz)) / (gxz * gxz) + (1 - cos(Pyz)) / (gyz * gyz);
+                    FCont = (1 - pcos(Pxy)) / (gxy * gxy) + (1 - pcos(Pxz)) / (gxz * gxz) + (1 - pcos(Pyz)) / (gyz * gyz);
                 }
                 if (g != 0) {
                     double divNow = (ST(TH(0), tNow, s) - ST(TH(0), tNow, imx)) / (dx * dx) + (ST(TH(1), tNow, s) - ST(TH(1), tNow, imy)) / (dy * dy)
@@ -788,9 +810,9 @@ static void moore_diag(const lat_params* p, const double* st, int64_t n, lat_dia
                         double t2 = (ST(TH(2), tNow, s) - ST(TH(2), tPast, s)) / (g * dt * dz);
                         thetaDotCont = 0.5 * (t0 * t0 + t1 * t1 + t2 * t2);
                         double gxy = g * dx * dy, gxz = g * dx * dz, gyz = g * dy * dz;
-                        double Fxy = (1 - cos(Pxy)) / (gxy * gxy);
-                        double Fxz = (1 - cos(Pxz)) / (gxz * gxz);
-                        double Fyz = (1 - cos(Pyz)) / (gyz * gyz);
+                        double Fxy = (1 - pcos(Pxy)) / (gxy * gxy);
+                        double Fxz = (1 - pcos(Pxz)) / (gxz * gxz);
+                        double Fyz = (1 - pcos(Pyz)) / (gyz * gyz);
                         FCont = Fxy + Fxz + Fyz;
                     }
                 }
@@ -1526,5 +1548,178 @@ int64_t orc_loop_collision_ic(const lat_params* p, const lat_string_profile* pro
 #undef LST
 #undef IX
     free(buf);
+    return off;
+}
+
+/* ---------------------------------------------------------------------------
+ * Perturbed straight strings, initialConditions.cpp:113-668, restated with
+ * the reference's operation order (pow(x, 2) as the reference calls it).
+ * Both write one level of fields; here it goes into both slots.
+ * ------------------------------------------------------------------------- */
+
+#define NG_NELLIP 1001  /* N_ellipint, initialConditions.cpp:45 */
+#define NG_TOL 1e-6     /* tol, :44 */
+
+/* trapezoid rule for the string's z(sigma): E(Omega*sigma) with the phase
+ * shifted by -pi/2 (initialConditions.cpp:189-198) */
+static double ng_ellip(double eps, double Omega, double sigma)
+{
+    const double pi = 4 * atan(1.0);
+    double e = 0;
+    for (int j = 0; j < NG_NELLIP; j++) {
+        const double trap_fac = (j == 0 || j == NG_NELLIP - 1) ? 0.5 : 1;
+        const double theta = j * Omega * sigma / (NG_NELLIP - 1) - pi / 2;
+        e += trap_fac * sqrt(1 - pow(eps * sin(theta), 2)) * Omega * sigma / (NG_NELLIP - 1);
+    }
+    return e;
+}
+
+static double ng_dist2(double eps, double Omega, double sigma, double x, double z)
+{
+    const double pi = 4 * atan(1.0);
+    const double e = ng_ellip(eps, Omega, sigma);
+    return pow(x - eps * cos(Omega * sigma - pi / 2) / Omega, 2) + pow(z - e / Omega, 2);
+}
+
+/* Omega for a string periodic over the z extent dz*nz (initialConditions.cpp:143-160) */
+double orc_ng_omega(double eps, double dz, int64_t nz)
+{
+    const double pi = 4 * atan(1.0);
+    double e = 0;
+    for (int j = 0; j < NG_NELLIP; j++) {
+        const double trap_fac = (j == 0 || j == NG_NELLIP - 1) ? 0.5 : 1;
+        const double theta = j * 2 * pi / (NG_NELLIP - 1);
+        e += trap_fac * sqrt(1 - pow(eps * sin(theta), 2)) * 2 * pi / (NG_NELLIP - 1);
+    }
+    return e / (dz * (double)nz);
+}
+
+/* golden-section search for the string parameter closest to (x, z)
+ * (initialConditions.cpp:175-382) and the quantities the sites of column
+ * (x, z) use: out = xs, zs, xs_sigma, zs_sigma, paraVecMag, normal_dist */
+void orc_ng_column(double eps, double Omega, double x, double z, double* out)
+{
+    const double pi = 4 * atan(1.0);
+    const double gr = 0.5 * (1 + sqrt(5.0));
+    double a = -2 * pi / Omega, b = 2 * pi / Omega;
+    double sigma1 = b - (b - a) / gr, sigma2 = a + (b - a) / gr;
+    double d1 = ng_dist2(eps, Omega, sigma1, x, z), d2 = ng_dist2(eps, Omega, sigma2, x, z);
+    double tolTest = 1, sigma = 0;
+    while (tolTest > NG_TOL) {
+        if (d1 < d2) b = sigma2;
+        else a = sigma1;
+        sigma1 = b - (b - a) / gr;
+        sigma2 = a + (b - a) / gr;
+        d1 = ng_dist2(eps, Omega, sigma1, x, z);
+        d2 = ng_dist2(eps, Omega, sigma2, x, z);
+        tolTest = b - a;
+        if (tolTest <= NG_TOL) sigma = d1 > d2 ? sigma2 : sigma1;
+    }
+    const double xs = eps * cos(Omega * sigma - pi / 2) / Omega;
+    const double zs = ng_ellip(eps, Omega, sigma) / Omega;
+    const double xs_sigma = -eps * sin(Omega * sigma - pi / 2);
+    const double zs_sigma = sqrt(1 - pow(eps * sin(Omega * sigma - pi / 2), 2));
+    const double paraVecMag = sqrt(pow(xs_sigma, 2) + pow(zs_sigma, 2));
+    out[0] = xs;
+    out[1] = zs;
+    out[2] = xs_sigma;
+    out[3] = zs_sigma;
+    out[4] = paraVecMag;
+    out[5] = (zs_sigma * (x - xs) - xs_sigma * (z - zs)) / paraVecMag;
+}
+
+int64_t orc_ng_sine_ic(const lat_params* p, const lat_string_profile* prof, double eps, double* st)
+{
+    const int nx = p->nx, ny = p->ny, nz = p->nz;
+    if (nx < 2 || ny < 2 || nz < 2 || !prof || prof->m < 2 || !(prof->h > 0) || !(eps >= 0 && eps < 1)) return -1;
+    const int64_t N = (int64_t)nx * ny * nz;
+    const double dx = p->dx, dy = p->dy, dz = p->dz, g = p->g;
+    const double Omega = orc_ng_omega(eps, dz, nz);
+    const int x0 = (nx - 1) / 2, y0 = (ny - 1) / 2, z0 = (nz - 1) / 2;
+    double* F[5];
+    for (int c = 0; c < 5; ++c) F[c] = st + (size_t)c * 2 * N;   /* slot 0 first, copied to slot 1 below */
+    for (int c = 0; c < 5; ++c) memset(F[c], 0, sizeof(double) * (size_t)N);
+#define NIX(i, j, k) (((int64_t)(i) * ny + (j)) * nz + (k))
+    int64_t off = 0;
+    for (int k = z0; k < nz; k++) {
+        const double z = (k - z0) * dz;
+        for (int i = 0; i < nx; i++) {
+            const double x = (i - x0) * dx;
+            double col[6];
+            orc_ng_column(eps, Omega, x, z, col);
+            const double xs = col[0], zs = col[1], xs_sigma = col[2], zs_sigma = col[3], paraVecMag = col[4],
+                         normal_dist = col[5];
+            for (int j = 0; j < ny; j++) {
+                const double y = (j - y0) * dy;
+                const double distance = sqrt(pow(x - xs, 2) + pow(y, 2) + pow(z - zs, 2));
+                double phiMag, AMag, ph0, ph1, A0, A1, A2;
+                off += profile_at(prof, g, distance, &phiMag, &AMag);
+                if (normal_dist == 0) { ph0 = 0; A1 = 0; }
+                else { ph0 = phiMag * normal_dist / distance; A1 = AMag * normal_dist / pow(distance, 2); }
+                if (y == 0) { ph1 = 0; A0 = 0; A2 = 0; }
+                else {
+                    ph1 = phiMag * y / distance;
+                    A0 = -AMag * zs_sigma * y / (pow(distance, 2) * paraVecMag);
+                    A2 = AMag * xs_sigma * y / (pow(distance, 2) * paraVecMag);
+                }
+                const int64_t s = NIX(i, j, k), r = NIX(nx - 1 - i, j, nz - 1 - k);
+                F[0][s] = ph0;
+                F[1][s] = ph1;
+                F[2][s] = A0;
+                F[3][s] = A1;
+                F[4][s] = A2;
+                /* reflection across z = 0 (initialConditions.cpp:470-477) */
+                F[0][r] = -F[0][s];
+                F[1][r] = F[1][s];
+                F[2][r] = F[2][s];
+                F[3][r] = -F[3][s];
+                if (k != nz - 1) F[4][NIX(nx - 1 - i, j, nz - 2 - k)] = -F[4][s];
+            }
+        }
+    }
+#undef NIX
+    /* link columns d*g*A (initialConditions.cpp:482-486) */
+    for (int64_t s = 0; s < N; ++s) {
+        F[2][s] = dx * g * F[2][s];
+        F[3][s] = dy * g * F[3][s];
+        F[4][s] = dz * g * F[4][s];
+    }
+    for (int c = 0; c < 5; ++c) memcpy(F[c] + N, F[c], sizeof(double) * (size_t)N);
+    return off;
+}
+
+int64_t orc_simple_sine_ic(const lat_params* p, const lat_string_profile* prof, double eps, double* st)
+{
+    const int nx = p->nx, ny = p->ny, nz = p->nz;
+    if (nx < 2 || ny < 2 || nz < 2 || !prof || prof->m < 2 || !(prof->h > 0)) return -1;
+    const int64_t N = (int64_t)nx * ny * nz;
+    const double dx = p->dx, dy = p->dy, dz = p->dz, g = p->g;
+    const double pi = 4 * atan(1.0);
+    const double Omega = 2 * pi / (dz * (nz - 1));
+    const int x0 = (nx - 1) / 2, y0 = (ny - 1) / 2, z0 = (nz - 1) / 2;
+    int64_t off = 0;
+    for (int i = 0; i < nx; i++) {
+        const double x = (i - x0) * dx;
+        for (int j = 0; j < ny; j++) {
+            const double y = (j - y0) * dy;
+            for (int k = 0; k < nz; k++) {
+                const double z = (k - z0) * dz;
+                const double xdist = x - eps * sin(Omega * z) / Omega;
+                const double distance = sqrt(xdist * xdist + y * y);
+                double phiMag, AMag, ph0, ph1, A0, A1, A2;
+                off += profile_at(prof, g, distance, &phiMag, &AMag);
+                if (xdist == 0) { ph0 = 0; A1 = 0; }
+                else { ph0 = phiMag * xdist / distance; A1 = AMag * xdist / pow(distance, 2); }
+                if (y == 0) { ph1 = 0; A0 = 0; A2 = 0; }
+                else { ph1 = phiMag * y / distance; A0 = -AMag * y / pow(distance, 2); A2 = 0; }
+                const int64_t s = ((int64_t)i * ny + j) * nz + k;
+                const double v[5] = {ph0, ph1, dx * g * A0, dy * g * A1, dz * g * A2};
+                for (int c = 0; c < 5; ++c) {
+                    st[((size_t)c * 2) * N + s] = v[c];
+                    st[((size_t)c * 2 + 1) * N + s] = v[c];
+                }
+            }
+        }
+    }
     return off;
 }

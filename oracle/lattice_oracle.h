@@ -77,6 +77,25 @@ int64_t orc_boost_ic(const lat_params* p, const lat_string_profile* prof, const 
 int64_t orc_loop_collision_ic(const lat_params* p, const lat_string_profile* prof, const lat_loop_collision_ic* c,
                               double* st);
 
+/* Perturbed straight strings of initialConditions.cpp into both slots of a
+ * full AH state: "NG sine" (:113-486, a Nambu-Goto sine wave: per (x, z)
+ * column a golden-section search for the closest string point, fields
+ * reflected across z = 0) and "simple sine" (:488-668, the straight string
+ * offset along x by eps*sin(Omega z)/Omega).  eps is the amplitude the
+ * reference reads from standard input.  Return the number of evaluations
+ * beyond the profile table, or -1 for bad arguments. */
+int64_t orc_ng_sine_ic(const lat_params* p, const lat_string_profile* prof, double eps, double* st);
+int64_t orc_simple_sine_ic(const lat_params* p, const lat_string_profile* prof, double eps, double* st);
+/* the NG-sine pieces: Omega of the lattice, and one column's string point
+ * (xs, zs, xs_sigma, zs_sigma, paraVecMag, normal_dist) */
+double orc_ng_omega(double eps, double dz, int64_t nz);
+void orc_ng_column(double eps, double Omega, double x, double z, double* out);
+
+/* Test only: move the step's sin/cos results by one ulp for a fraction frac of
+ * the arguments (0 = the reference's values), to measure how far one-ulp
+ * differences carry through the dynamics. */
+void orc_set_trig_perturbation(double frac);
+
 /* total string length by greedy chaining of crossings, ic_w_evolution.cpp:961-1087 */
 int orc_string_length(const lat_params* p, const double* xyz, int64_t M, int split, double* L0, double* L1);
 

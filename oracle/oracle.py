@@ -60,6 +60,13 @@ def lib():
         L.orc_loop_collision_ic.argtypes = [P(LatParams), ctypes.c_void_p, ctypes.c_void_p, dp]
         L.orc_loop_collision_ic.restype = ctypes.c_int64
         L.orc_string_length.argtypes = [P(LatParams), dp, ctypes.c_int64, ctypes.c_int, dp, dp]
+        for name in ("orc_ng_sine_ic", "orc_simple_sine_ic"):
+            getattr(L, name).argtypes = [P(LatParams), ctypes.c_void_p, ctypes.c_double, dp]
+            getattr(L, name).restype = ctypes.c_int64
+        L.orc_ng_omega.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int64]
+        L.orc_ng_omega.restype = ctypes.c_double
+        L.orc_set_trig_perturbation.argtypes = [ctypes.c_double]
+        L.orc_ng_column.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp]
         _lib = L
     return _lib
 
@@ -189,6 +196,37 @@ def loop_collision_ic(p: LatParams, phi: np.ndarray, A: np.ndarray, h: float, ge
     if off < 0:
         raise RuntimeError("orc_loop_collision_ic: bad arguments")
     return st, int(off)
+
+
+def set_trig_perturbation(frac: float) -> None:
+    """Test only: one-ulp moves of a fraction `frac` of the step's sin/cos
+    results (0 restores the reference's values)."""
+    lib().orc_set_trig_perturbation(float(frac))
+
+
+def sine_string_ic(p: LatParams, phi: np.ndarray, A: np.ndarray, h: float, eps: float, kind: str,
+                   winding: float = 1.0):
+    """Perturbed straight string of initialConditions.cpp: kind "NG sine"
+    (:113-486) or "simple sine" (:488-668), amplitude eps (the value the
+    reference reads from standard input), one level in both slots.  Returns
+    (state, number of evaluations off the table)."""
+    from axions_gb300.params import string_profile
+    fn = {"NG sine": "orc_ng_sine_ic", "simple sine": "orc_simple_sine_ic"}[kind]
+    prof, keep = string_profile(phi, A, h, winding)
+    st = empty_state(p)
+    off = getattr(lib(), fn)(ctypes.byref(p), ctypes.byref(prof), float(eps), _dp(st))
+    del keep
+    if off < 0:
+        raise RuntimeError(f"{fn}: bad arguments")
+    return st, int(off)
+
+
+def ng_column(eps: float, Omega: float, x: float, z: float) -> np.ndarray:
+    """(xs, zs, xs_sigma, zs_sigma, paraVecMag, normal_dist) of the NG-sine
+    string point closest to (x, z)."""
+    out = np.zeros(6)
+    lib().orc_ng_column(float(eps), float(Omega), float(x), float(z), _dp(out))
+    return out
 
 
 def string_length(p: LatParams, xyz: np.ndarray, split: bool = True):

@@ -28,8 +28,16 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 ORACLE = HERE.parent
 REF_OUT = ORACLE / "_ref"
-REFERENCE = Path(os.environ.get("AXIONS_REFERENCE", "/root/reference"))
+# The reference checkout: given by the caller (set_reference) or the
+# AXIONS_REFERENCE environment variable; there is no default location.
+REFERENCE: Path | None = Path(os.environ["AXIONS_REFERENCE"]) if os.environ.get("AXIONS_REFERENCE") else None
 SCRATCH = Path(os.environ.get("AXIONS_REF_SCRATCH", "/tmp/axions_ref"))
+
+
+def set_reference(path) -> None:
+    """Use the reference checkout at `path` for the builds below."""
+    global REFERENCE
+    REFERENCE = Path(path)
 
 # program -> (extra sources that lie in the reference dir, MPI field list)
 PROGRAMS = {
@@ -45,7 +53,14 @@ PROGRAMS = {
 
 
 def reference_available() -> bool:
-    return (REFERENCE / "mpi_evolution.cpp").is_file()
+    return REFERENCE is not None and (REFERENCE / "mpi_evolution.cpp").is_file()
+
+
+def _require_reference() -> Path:
+    if not reference_available():
+        raise RuntimeError("reference sources not found: pass the reference directory (set_reference, "
+                           "--reference) or set AXIONS_REFERENCE")
+    return REFERENCE
 
 
 def _fmt(v) -> str:
@@ -80,6 +95,7 @@ def build(program: str, tag: str, consts: dict, extra_consts: dict | None = None
     if program not in PROGRAMS:
         raise ValueError(program)
     extra, fields = PROGRAMS[program]
+    _require_reference()
     work = SCRATCH / tag
     if work.exists():
         shutil.rmtree(work)

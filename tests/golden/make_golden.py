@@ -300,10 +300,34 @@ def gen_loop_collision_ic(name, nx, ny, nz, g, dt, profile, sor_h, dz=0.5, geome
     print(name, ic.shape)
 
 
+def gen_sine_ic(name, kind, nx, ny, nz, g, eps, profile, sor_h, dz=0.5):
+    """initialConditions.cpp, ic_type "NG sine" or "simple sine" (a straight
+    string perturbed by a sine wave of amplitude eps, which the program reads
+    from standard input): Data/ic.txt, one level (17 digits), from the
+    profile table at dir_path/Data/SOR_Fields.txt."""
+    m = profile.shape[1]
+    consts = {"nx": nx, "ny": ny, "nz": nz, "ic_type": kind, "g": float(g), "SORnx": m, "SORa": float(sor_h),
+              "dz": float(dz)}
+    build_ref.build("initialConditions", name, consts)
+    work = build_ref.SCRATCH / name
+    lines = [f"{float(profile[0, r])!r} {float(profile[1, r])!r}" for r in range(m)]
+    (work / "Data" / "SOR_Fields.txt").write_text("\n".join(lines) + "\n")
+    work = build_ref.run(name, stdin=f"{eps!r}\n")
+    ic = build_ref.read_columns(work / "Data" / "ic.txt").reshape(nx * ny * nz, 5).T.copy()
+    np.savez_compressed(OUT / f"{name}.npz", program="initialConditions", ic_type=kind, nx=nx, ny=ny, nz=nz,
+                        dx=0.5, dy=0.5, dz=dz, g=g, eps=eps, sor_h=sor_h, profile=profile, ic=ic)
+    print(name, ic.shape)
+
+
 def main():
+    args = sys.argv[1:]
+    if args[:1] == ["--reference"] and len(args) >= 2:
+        build_ref.set_reference(args[1])
+        args = args[2:]
     if not build_ref.reference_available():
-        raise SystemExit("reference sources not found; fixtures can only be made where they are")
-    only = sys.argv[1:]
+        raise SystemExit("usage: make_golden.py --reference <reference checkout> [gen_...(...) ...] "
+                         "(or set AXIONS_REFERENCE); fixtures can only be made where the reference is")
+    only = args
     if only:
         for call in only:
             eval(call)

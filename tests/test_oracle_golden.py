@@ -214,3 +214,39 @@ def test_loop_collision_default_geometry_is_the_references(oracle_mod):
     geo = default_loop_collision(int(z["nx"]), int(z["ny"]), int(z["nz"]), 0.5, 0.5, float(z["dz"]))
     for k in LOOP_COLLISION_KEYS:
         assert np.array_equal(np.array(geo[k], dtype=np.float64), z[k]), k
+
+
+SINE_CASES = ["ref_ng_sine_ic", "ref_ng_sine_ic_b", "ref_simple_sine_ic"]
+
+
+def sine_params(z):
+    from axions_gb300.params import make_params
+    return make_params(0, nx=int(z["nx"]), ny=int(z["ny"]), nz=int(z["nz"]), dx=float(z["dx"]), dy=float(z["dy"]),
+                       dz=float(z["dz"]), g=float(z["g"]))
+
+
+@pytest.mark.parametrize("name", SINE_CASES)
+def test_sine_string_ic_bit_exact(oracle_mod, name):
+    """initialConditions.cpp "NG sine" (golden-section search for the closest
+    point of a Nambu-Goto sine wave, fields reflected across z = 0) and
+    "simple sine" (the string offset by eps*sin(Omega z)/Omega), with eps read
+    from standard input: the one level of Data/ic.txt, in both slots."""
+    z = load_golden(name)
+    st, off = oracle_mod.sine_string_ic(sine_params(z), z["profile"][0], z["profile"][1], float(z["sor_h"]),
+                                        float(z["eps"]), str(z["ic_type"]))
+    assert off == 0
+    v = st.reshape(5, 2, -1)
+    assert np.array_equal(v[:, 0], z["ic"]) and np.array_equal(v[:, 1], z["ic"])
+
+
+def test_ng_sine_column_is_the_closest_string_point(oracle_mod):
+    """The golden-section result is a local minimum of the distance to the
+    curve (xs(sigma), zs(sigma)), and normal_dist is the signed distance along
+    the unit normal: |normal_dist| = |(x, z) - (xs, zs)|."""
+    z = load_golden("ref_ng_sine_ic")
+    eps, dz, nz = float(z["eps"]), float(z["dz"]), int(z["nz"])
+    Om = oracle_mod.lib().orc_ng_omega(eps, dz, nz)
+    for x, zz in ((0.7, 0.3), (-2.0, 1.5), (3.1, 4.0), (0.0, 0.0)):
+        xs, zs, xsg, zsg, pm, nd = oracle_mod.ng_column(eps, Om, x, zz)
+        assert abs(pm - 1.0) < 1e-12
+        assert abs(abs(nd) - np.hypot(x - xs, zz - zs)) < 1e-6

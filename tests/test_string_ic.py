@@ -271,3 +271,89 @@ def test_icw_program_boost_and_data_modes(tmp_path, oracle_mod):
     for c in range(5):
         ref = np.max(np.abs(fb[c]))
         assert np.max(np.abs(fa[c] - fb[c])) <= TOL * max(ref, 1e-300)
+
+
+SINE_CASES = ["ref_ng_sine_ic", "ref_ng_sine_ic_b", "ref_simple_sine_ic"]
+
+
+def _sine_params(z, precision=0):
+    from axions_gb300.params import make_params
+    return make_params(0, nx=int(z["nx"]), ny=int(z["ny"]), nz=int(z["nz"]), dx=float(z["dx"]), dy=float(z["dy"]),
+                       dz=float(z["dz"]), g=float(z["g"]), precision=precision)
+
+
+@pytest.mark.parametrize("name", SINE_CASES)
+def test_sine_string_ic_against_reference(lattice_mod, oracle_mod, name):
+    """initialConditions.cpp "NG sine" and "simple sine" built on the GPU:
+    both slots hold the reference's one level, each field within 1e-12 of
+    its largest value.  (The golden-section search compares two distances
+    per pass; CUDA's sin and cos can round them differently from glibc's,
+    which can move the end of the search by up to its 1e-6 tolerance in the
+    string parameter.  The site values depend on that parameter only to
+    second order at the minimum, except the links' tangent factors; the
+    cases here meet the bar.)"""
+    z = load_golden(name)
+    kind = str(z["ic_type"])
+    with lattice_mod.Lattice(_sine_params(z)) as lat:
+        off = lat.sine_string_ic_device(z["profile"][0], z["profile"][1], float(z["sor_h"]), float(z["eps"]), kind)
+        assert off == 0 and lat.time_step == 0
+        got = _levels(lat)
+    want = np.stack([z["ic"], z["ic"]], axis=1)
+    _close(got, want, TOL)
+    # FP32 handle: the same values rounded to float
+    with lattice_mod.Lattice(_sine_params(z, precision=1)) as lat:
+        lat.sine_string_ic_device(z["profile"][0], z["profile"][1], float(z["sor_h"]), float(z["eps"]), kind)
+        g32 = _levels(lat)
+    assert np.allclose(g32, want.astype(np.float32).astype(np.float64), rtol=0, atol=1e-6)
+
+
+def test_sine_string_ic_at_size_against_oracle(lattice_mod, oracle_mod):
+    """NG sine on a 64 x 40 x 81 lattice (2,624 searched columns) and simple
+    sine on 48^3, against the oracle's restatement (pinned bit-exact on the
+    fixtures above): within 1e-12 of each field's largest value."""
+    z = load_golden("ref_ng_sine_ic")
+    prof, h = z["profile"], float(z["sor_h"])
+    from axions_gb300.params import make_params
+    for kind, (nx, ny, nz), eps in (("NG sine", (64, 40, 81), 0.45), ("simple sine", (48, 48, 48), 0.7)):
+        p = make_params(0, nx=nx, ny=ny, nz=nz, d=0.5, g=1.0)
+        want, off_ref = oracle_mod.sine_string_ic(p, prof[0], prof[1], h, eps, kind)
+        with lattice_mod.Lattice(p) as lat:
+            off = lat.sine_string_ic_device(prof[0], prof[1], h, eps, kind)
+            got = lat.get_slots()
+        assert off == off_ref
+        _close(got, want, TOL)
+
+
+def test_sine_string_ic_rejects_bad_arguments(lattice_mod):
+    z = load_golden("ref_simple_sine_ic")
+    prof = z["profile"]
+    from axions_gb300.params import MODEL_MOORE, make_params
+    with lattice_mod.Lattice(_sine_params(z)) as lat:
+        for eps in (-0.1, 1.0, float("nan")):
+            with pytest.raises(lattice_mod.LatticeError):
+                lat.sine_string_ic_device(prof[0], prof[1], 0.01, eps, "NG sine")
+    with lattice_mod.Lattice(make_params(MODEL_MOORE, n=8)) as lat:
+        with pytest.raises(lattice_mod.LatticeError):
+            lat.sine_string_ic_device(prof[0], prof[1], 0.01, 0.3, "simple sine")
+
+
+@pytest.mark.parametrize("name", ["ref_ng_sine_ic", "ref_simple_sine_ic"])
+def test_initial_conditions_program_sine(tmp_path, name):
+    """bin/initialConditions ic_type="NG sine" / "simple sine" with eps=
+    (the reference reads it from standard input) writes the reference's
+    one-level Data/ic.txt from Data/SOR_Fields.txt."""
+    z = load_golden(name)
+    prof = z["profile"]
+    (tmp_path / "Data").mkdir()
+    (tmp_path / "Data" / "SOR_Fields.txt").write_text(
+        "".join(f"{float(a)!r} {float(b)!r}\n" for a, b in zip(prof[0], prof[1])))
+    args = {"ic_type": str(z["ic_type"]), "nx": int(z["nx"]), "ny": int(z["ny"]), "nz": int(z["nz"]), "dx": 0.5,
+            "dy": 0.5, "dz": float(z["dz"]), "g": float(z["g"]), "SORnx": prof.shape[1], "SORa": float(z["sor_h"]),
+            "eps": repr(float(z["eps"])), "digits": 17}
+    cmd = [str(ROOT / "axions_gb300" / "bin" / "initialConditions"), f"out_dir={tmp_path}"]
+    r = subprocess.run(cmd + [f"{k}={x}" for k, x in args.items()], capture_output=True, timeout=300)
+    assert r.returncode == 0, r.stderr.decode()
+    got = np.array([float(t) for t in (tmp_path / "Data" / "ic.txt").read_text().split()]).reshape(-1, 5).T
+    _close(got[:, None, :], z["ic"][:, None, :], TOL)
+    r = subprocess.run(cmd + [f"{k}={x}" for k, x in args.items() if k != "eps"], capture_output=True, timeout=300)
+    assert r.returncode == 2 and b"eps" in r.stderr
