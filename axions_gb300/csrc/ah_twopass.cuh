@@ -185,24 +185,62 @@ __global__ void __launch_bounds__(BLOCK, 2) ah_update_kernel(const Geom g, const
         const double phiMagSqr = p0 * p0 + p1 * p1;
         const double pot = c.halfLambda * (phiMagSqr - c.etaSq);
 
-        // covariant Laplacian (mpi_evolution.cpp:418-428), c = +1 then c = -1
-        double lap0 = sdiv<RECIP>(cx * p0xp + sx * p1xp - twop0 + cxm * p0xm - sxm_ * p1xm, c.dx2, c.inv_dx2)
-                    + sdiv<RECIP>(cy * p0yp + sy * p1yp - twop0 + cym * p0ym - sym * p1ym, c.dy2, c.inv_dy2)
-                    + sdiv<RECIP>(cz * p0zp + sz * p1zp - twop0 + czm * p0zm - szm_ * p1zm, c.dz2, c.inv_dz2);
-        double lap1 = sdiv<RECIP>(cx * p1xp - sx * p0xp - twop1 + cxm * p1xm + sxm_ * p0xm, c.dx2, c.inv_dx2)
-                    + sdiv<RECIP>(cy * p1yp - sy * p0yp - twop1 + cym * p1ym + sym * p0ym, c.dy2, c.inv_dy2)
-                    + sdiv<RECIP>(cz * p1zp - sz * p0zp - twop1 + czm * p1zm + szm_ * p0zm, c.dz2, c.inv_dz2);
-        double tt0 = lap0 - pot * p0;
-        double tt1 = lap1 - pot * p1;
-        if (c.fric != 0) {
-            tt0 = tt0 - c.fric * tdiv<STRICT>(p0 - q0, c.dt, c.inv_dt);
-            tt1 = tt1 - c.fric * tdiv<STRICT>(p1 - q1, c.dt, c.inv_dt);
+        double tt0, tt1, curx, cury, curz;
+        if constexpr (STRICT) {
+            // covariant Laplacian (mpi_evolution.cpp:418-428), c = +1 then c = -1
+            const double lap0 = sdiv<RECIP>(cx * p0xp + sx * p1xp - twop0 + cxm * p0xm - sxm_ * p1xm, c.dx2, c.inv_dx2)
+                              + sdiv<RECIP>(cy * p0yp + sy * p1yp - twop0 + cym * p0ym - sym * p1ym, c.dy2, c.inv_dy2)
+                              + sdiv<RECIP>(cz * p0zp + sz * p1zp - twop0 + czm * p0zm - szm_ * p1zm, c.dz2, c.inv_dz2);
+            const double lap1 = sdiv<RECIP>(cx * p1xp - sx * p0xp - twop1 + cxm * p1xm + sxm_ * p0xm, c.dx2, c.inv_dx2)
+                              + sdiv<RECIP>(cy * p1yp - sy * p0yp - twop1 + cym * p1ym + sym * p0ym, c.dy2, c.inv_dy2)
+                              + sdiv<RECIP>(cz * p1zp - sz * p0zp - twop1 + czm * p1zm + szm_ * p0zm, c.dz2, c.inv_dz2);
+            tt0 = lap0 - pot * p0;
+            tt1 = lap1 - pot * p1;
+            if (c.fric != 0) {
+                tt0 = tt0 - c.fric * tdiv<STRICT>(p0 - q0, c.dt, c.inv_dt);
+                tt1 = tt1 - c.fric * tdiv<STRICT>(p1 - q1, c.dt, c.inv_dt);
+            }
+            // gauge current (mpi_evolution.cpp:459-466)
+            curx = cx * (p1 * p0xp - p0 * p1xp) + sx * (p0 * p0xp + p1 * p1xp);
+            cury = cy * (p1 * p0yp - p0 * p1yp) + sy * (p0 * p0yp + p1 * p1yp);
+            curz = cz * (p1 * p0zp - p0 * p1zp) + sz * (p0 * p0zp + p1 * p1zp);
+        } else {
+            // The same quantities with fewer FP64 instructions.  The forward
+            // link-transported neighbour U_mu phi(x+mu), A = c phi0' + s phi1',
+            // B = c phi1' - s phi0', enters both the Laplacian and the current:
+            // j_mu = c (phi1 phi0' - phi0 phi1') + s (phi0 phi0' + phi1 phi1')
+            //      = phi1 A - phi0 B.
+            // With equal spacings the three directions are summed before one
+            // scaling; friction uses fric/dt from the host.
+            const double Ax = fma(sx, p1xp, cx * p0xp), Bx = fma(-sx, p0xp, cx * p1xp);
+            const double Ay = fma(sy, p1yp, cy * p0yp), By = fma(-sy, p0yp, cy * p1yp);
+            const double Az = fma(sz, p1zp, cz * p0zp), Bz = fma(-sz, p0zp, cz * p1zp);
+            double lap0, lap1;
+            if (c.iso != 0) {
+                const double s0 = fma(-sxm_, p1xm, fma(cxm, p0xm, Ax)) + fma(-sym, p1ym, fma(cym, p0ym, Ay))
+                                + fma(-szm_, p1zm, fma(czm, p0zm, Az));
+                const double s1 = fma(sxm_, p0xm, fma(cxm, p1xm, Bx)) + fma(sym, p0ym, fma(cym, p1ym, By))
+                                + fma(szm_, p0zm, fma(czm, p1zm, Bz));
+                lap0 = sdiv<RECIP>(fma(-6.0, p0, s0), c.dx2, c.inv_dx2);
+                lap1 = sdiv<RECIP>(fma(-6.0, p1, s1), c.dx2, c.inv_dx2);
+            } else {
+                lap0 = sdiv<RECIP>(fma(-sxm_, p1xm, fma(cxm, p0xm, Ax)) - twop0, c.dx2, c.inv_dx2)
+                     + sdiv<RECIP>(fma(-sym, p1ym, fma(cym, p0ym, Ay)) - twop0, c.dy2, c.inv_dy2)
+                     + sdiv<RECIP>(fma(-szm_, p1zm, fma(czm, p0zm, Az)) - twop0, c.dz2, c.inv_dz2);
+                lap1 = sdiv<RECIP>(fma(sxm_, p0xm, fma(cxm, p1xm, Bx)) - twop1, c.dx2, c.inv_dx2)
+                     + sdiv<RECIP>(fma(sym, p0ym, fma(cym, p1ym, By)) - twop1, c.dy2, c.inv_dy2)
+                     + sdiv<RECIP>(fma(szm_, p0zm, fma(czm, p1zm, Bz)) - twop1, c.dz2, c.inv_dz2);
+            }
+            tt0 = fma(-pot, p0, lap0);
+            tt1 = fma(-pot, p1, lap1);
+            if (c.fric != 0) {
+                tt0 = fma(-c.fric_dt, p0 - q0, tt0);
+                tt1 = fma(-c.fric_dt, p1 - q1, tt1);
+            }
+            curx = fma(p1, Ax, -p0 * Bx);
+            cury = fma(p1, Ay, -p0 * By);
+            curz = fma(p1, Az, -p0 * Bz);
         }
-
-        // gauge current (mpi_evolution.cpp:459-466)
-        const double curx = cx * (p1 * p0xp - p0 * p1xp) + sx * (p0 * p0xp + p1 * p1xp);
-        const double cury = cy * (p1 * p0yp - p0 * p1yp) + sy * (p0 * p0yp + p1 * p1yp);
-        const double curz = cz * (p1 * p0zp - p0 * p1zp) + sz * (p0 * p0zp + p1 * p1zp);
 
         // lattice curl (mpi_evolution.cpp:471-487)
         const double Fxy_y = sdiv<RECIP>(sPxy - sPxy_m, c.dy2, c.inv_dy2);

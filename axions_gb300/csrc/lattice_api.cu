@@ -96,6 +96,8 @@ StepCoef make_coef(const lat_params& p, int64_t n)
     c.inv_gxy2 = c.gxy2 != 0 ? 1.0 / c.gxy2 : 0.0;
     c.inv_gxz2 = c.gxz2 != 0 ? 1.0 / c.gxz2 : 0.0;
     c.inv_gyz2 = c.gyz2 != 0 ? 1.0 / c.gyz2 : 0.0;
+    c.iso = (p.dx == p.dy && p.dx == p.dz) ? 1.0 : 0.0;
+    c.fric_dt = c.fric / p.dt;
     return c;
 }
 
@@ -200,8 +202,9 @@ int lat::validate_params(const lat_params* p)
     LAT_REQUIRE(p->model == LAT_MODEL_AH || p->model == LAT_MODEL_MOORE, "unknown model");
     LAT_REQUIRE(p->precision == LAT_F64 || p->precision == LAT_F32 || p->precision == LAT_F64_FAST,
                 "unknown precision");
-    LAT_REQUIRE(p->kernel_variant == 0 || p->kernel_variant == 1 || (p->kernel_variant == 2 && p->precision == LAT_F32),
-                "unknown kernel_variant (2 is for FP32 only)");
+    LAT_REQUIRE(p->kernel_variant == 0 || p->kernel_variant == 1 ||
+                    ((p->kernel_variant == 2 || p->kernel_variant == 3) && p->precision == LAT_F32),
+                "unknown kernel_variant (2 and 3 are for FP32 only)");
     LAT_REQUIRE(p->bc >= LAT_BC_PERIODIC && p->bc <= LAT_BC_ABSORBING, "unknown boundary condition");
     LAT_REQUIRE(p->bc_z >= LAT_BCZ_AS_XY && p->bc_z <= LAT_BCZ_NEUMANN, "unknown bc_z");
     const int kz = bc_z_kind(*p);
@@ -539,6 +542,7 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
         return LAT_OK;
     };
     if (!split && (rc = divergence())) return rc;
+    int tiled_used = 0;  // CTAs of the x-marching FP32 step, if it ran
     if (p.model == LAT_MODEL_AH) {
         if (h->elem == 8) {
             Fields<double, 5> f;
@@ -571,7 +575,7 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
                 f.past[c] = (float*)h->slot(c, tPast);
             }
             if (p.kernel_variant != 1)
-                LAT_CKL(launch_ah_tiled_f32(h->geom, f, cf, d, diag, h->chunk, h->stream, p.kernel_variant == 0));
+                LAT_CKL(launch_ah_tiled_f32(h->geom, f, cf, d, diag, h->chunk, h->stream, p.kernel_variant, &tiled_used));
             else LAT_CKL(launch_ah_step_f32(h->geom, f, cf, d, diag, h->stream));
         }
     } else {
@@ -589,15 +593,14 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
                 f.past[c] = (float*)h->slot(c, tPast);
             }
             if (p.kernel_variant != 1)
-                LAT_CKL(launch_moore_tiled_f32(h->geom, f, cf, d, diag, h->chunk, h->stream, p.kernel_variant == 0));
+                LAT_CKL(launch_moore_tiled_f32(h->geom, f, cf, d, diag, h->chunk, h->stream, p.kernel_variant, &tiled_used));
             else LAT_CKL(launch_moore_step_f32(h->geom, f, cf, d, diag, h->stream));
         }
     }
     if (absorb) LAT_CKL(launch_absorb_update(h->geom, (int)h->elem, nowv, pastv, h->btt, p.dt * p.dt, h->stream));
     if (diag) {
         // partials written by the step: one per CTA of the kernel that ran
-        const bool tiled = h->elem == 4 && p.kernel_variant != 1;
-        const int used = tiled ? tiled_blocks(h->geom, h->chunk) : h->nblocks;
+        const int used = tiled_used > 0 ? tiled_used : h->nblocks;
         LAT_CKL(launch_finalize(h->partials, used, diag_dst, h->stream));
     }
     if (write) {

@@ -55,7 +55,9 @@ inline dim3 site_grid(const Geom& g)
     X(quarterLambda) X(quarterLambda2) X(halfLambda12e)                       \
     X(twog)                              /* 2*g                            */ \
     X(inv_dx2) X(inv_dy2) X(inv_dz2) X(inv_dt) X(inv_dx) X(inv_dy) X(inv_dz) X(inv_g) \
-    X(inv_gdtdx) X(inv_gdtdy) X(inv_gdtdz) X(inv_gxy2) X(inv_gxz2) X(inv_gyz2)
+    X(inv_gdtdx) X(inv_gdtdy) X(inv_gdtdz) X(inv_gxy2) X(inv_gxz2) X(inv_gyz2) \
+    X(iso)                               /* 1 when dx == dy == dz, else 0 */      \
+    X(fric_dt)                           /* fric / dt (fused FP64 step)    */
 
 template <class R>
 struct StepCoefT {
@@ -122,12 +124,15 @@ int default_chunk(const lat_params& p);
 int batch_chunk(const Geom& g);
 // number of CTAs (and diagnostic partials) of the tiled FP32 step
 int tiled_blocks(const Geom&, int chunk);
-// tiled, x-marching FP32 Abelian-Higgs step; `chunk` x-planes per CTA.
-// allow_vec = false keeps the one-element staging copies (kernel_variant 2)
+// x-marching FP32 steps, `chunk` x-planes per CTA.  variant 0: the pair step
+// (two z-sites per thread, pair_step.cuh) where the layout allows it, else the
+// tiled step (tiled_step.cuh); 2: the tiled step with one-element staging
+// copies; 3: the tiled step with 16-byte staging where allowed.  *blocks
+// receives the CTAs (diagnostic partials) of the kernel launched.
 cudaError_t launch_ah_tiled_f32(const Geom&, const Fields<float, 5>&, const StepCoef&, const DiagOut&, bool diag,
-                                int chunk, cudaStream_t, bool allow_vec = true);
+                                int chunk, cudaStream_t, int variant, int* blocks);
 cudaError_t launch_moore_tiled_f32(const Geom&, const Fields<float, 7>&, const StepCoef&, const DiagOut&, bool diag,
-                                   int chunk, cudaStream_t, bool allow_vec = true);
+                                   int chunk, cudaStream_t, int variant, int* blocks);
 // divergence of theta on one level into divbuf (used when no previous step stored it)
 cudaError_t launch_divergence_f64(const Geom&, const double* thx, const double* thy, const double* thz,
                                   const StepCoef&, double* out, cudaStream_t);

@@ -1,0 +1,622 @@
+// FP32 lattice step for NS complex scalars on one compact U(1) gauge field,
+// two z-sites per thread in packed float2 arithmetic.
+//   NS = 1: Abelian-Higgs (mpi_evolution.cpp:381-501, charge 1);
+//   NS = 2: Moore model, charges q1, q2 (moore_mpi_evolution.cpp:405-550,
+//           mooreEvol.cpp:191-337).
+//
+// The FP32 step moves 60 B (Abelian-Higgs) or 84 B (Moore) per site, so at
+// HBM speed an SM has under 3 cycles per site: the step is issue-bound unless
+// its instruction count per site is small.  This kernel halves it against a
+// one-site-per-thread tile (tiled_step.cuh) by giving each thread the z-pair
+// (k, k+1) of one (x, y) column and computing both sites in the two lanes of
+// GB300's paired FP32 instructions (FFMA2/FADD2/FMUL2, __ffma2_rn and
+// friends): one instruction updates two sites.  A pair is also one 8-byte
+// shared-memory or global access, and its inner z-neighbours are in
+// registers.  The structure is otherwise the tiled step's:
+//   * a CTA owns a 64 (z) x 8 (y) tile and marches `chunk` x-planes;
+//   * each plane's now level, tile plus one-site halo, is staged in shared
+//     memory by 16-byte cp.async chunks, two planes ahead, in a 3-stage ring;
+//   * every site's link data (e^{i q theta} per direction and scalar, sines of
+//     the plaquettes P_xy, P_xz, P_yz) is evaluated once per step: own sites by
+//     their thread, the low y and z halo by warps 0 and 1;
+//   * x-backward data, and the next plane's own values (read as x-forward
+//     neighbours), are carried in registers.
+// Used where the layout allows 16-byte chunks and aligned pairs: periodic z,
+// nz a multiple of 4, 16-byte aligned fields (every benchmark and serving
+// shape); x and y may be periodic or fixed.  Elsewhere the tiled step runs.
+// HBM traffic is the algorithmic 3 accesses per value.  Energy and Gauss sums
+// are accumulated in FP64.
+#pragma once
+
+#include <cuda_pipeline.h>
+
+#include "site_common.cuh"
+#include "tiled_step.cuh"
+
+namespace lat {
+
+constexpr int PT_TZ = 32;              // threads along z (each two sites)
+constexpr int PT_Z = 2 * PT_TZ;        // tile width along z
+constexpr int PT_Y = 8;                // tile height along y (warps per CTA)
+constexpr int PT_THREADS = PT_TZ * PT_Y;
+constexpr int PT_HY = PT_Y + 2;        // staged rows j0-1 .. j0+8
+constexpr int PT_PZ = 72;              // staged row pitch (floats): column c holds z = k0 - 4 + c
+constexpr int PT_C0 = 4;               // column of z = k0 (16-byte aligned; own pairs 8-byte aligned)
+constexpr int PT_NQ = PT_PZ / 4;       // 16-byte chunks per staged row
+constexpr int PT_LY = PT_Y + 1;        // link rows j0-1 .. j0+7 (row ly holds j0 - 1 + ly)
+constexpr int PT_LP = 68;              // link row pitch (floats): column PT_LC0 + m holds z = k0 + m
+constexpr int PT_LC0 = 2;
+constexpr int PT_STAGES = 3;
+
+template <int NS>
+struct PairSmem {
+    float st[PT_STAGES][2 * NS + 3][PT_HY][PT_PZ];  // components in field order: scalars, then theta_x,y,z
+    float L[4 * NS + 3][PT_LY][PT_LP];              // link data (LinkIdx<NS> order)
+    double red[2][PT_Y];
+};
+
+// ---- paired FP32 arithmetic (two sites per instruction) --------------------
+__device__ __forceinline__ float2 p2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 neg2(float2 a) { return __fmul2_rn(a, make_float2(-1.f, -1.f)); }
+
+__device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ void sts2(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+
+// sin and cos of both lanes: Cody-Waite reduction to [-pi, pi] in paired
+// arithmetic (6.28125 has 8 significant bits, so k*6.28125 is exact for
+// |k| < 2^16), then the hardware approximations (Trig<float> of site_common.cuh
+// does the same per element).
+__device__ __forceinline__ float2 reduce2(float2 x)
+{
+    const float2 t = mul2(x, p2(0.159154943091895336f));
+    const float2 k = make_float2(rintf(t.x), rintf(t.y));
+    const float2 r = fma2(neg2(k), p2(6.28125f), x);
+    return fma2(neg2(k), p2(1.93530717958647692e-3f), r);
+}
+__device__ __forceinline__ void sincos2(float2 x, float2& s, float2& c)
+{
+    const float2 r = reduce2(x);
+    __sincosf(r.x, &s.x, &c.x);
+    __sincosf(r.y, &s.y, &c.y);
+}
+__device__ __forceinline__ float2 sin2(float2 x)
+{
+    const float2 r = reduce2(x);
+    return make_float2(__sinf(r.x), __sinf(r.y));
+}
+
+// e^{i q theta} of both lanes from e^{i theta} = (c, s)
+__device__ __forceinline__ void charged2(float2 theta, float2 c1, float2 s1, const Charges<float>& ch, int f, float2& cq,
+                                         float2& sq)
+{
+    const int q = ch.qpow[f];
+    if (q == 1) {
+        cq = c1;
+        sq = s1;
+    } else if (q != 0) {
+        float2 rc = c1, rs = s1;
+        const int n = q < 0 ? -q : q;
+        for (int m = 1; m < n; ++m) {
+            const float2 t = fma2(rc, c1, neg2(mul2(rs, s1)));
+            rs = fma2(rc, s1, mul2(rs, c1));
+            rc = t;
+        }
+        cq = rc;
+        sq = q < 0 ? neg2(rs) : rs;
+    } else {
+        sincos2(mul2(p2(ch.q[f]), theta), sq, cq);
+    }
+}
+
+// Whether the pair step can run: 16-byte staging and 8-byte aligned pairs.
+template <int NC>
+inline bool pair_ok(const Geom& g, const Fields<float, NC>& f)
+{
+    return tiled_vec_ok<float, NC>(g, f);
+}
+
+inline dim3 pair_grid(const Geom& g, int chunk)
+{
+    return dim3((unsigned)((g.nz + PT_Z - 1) / PT_Z), (unsigned)((g.hiy - g.loy + PT_Y - 1) / PT_Y),
+                (unsigned)((g.hix - g.lox + chunk - 1) / chunk));
+}
+
+// The step coefficients the kernel uses, in float, with the products that
+// occur once per term taken on the host.
+struct PairCoef {
+    float inv_dx2, inv_dy2, inv_dz2, dt2, halfLambda, etaSq, halfLambda2, eta2Sq, halfLambda12;
+    float m2gg, fric_dt, damp_dt, inv_dt, inv_dx, inv_dy, inv_dz, inv_g, twog;
+    float inv_gdtdx, inv_gdtdy, inv_gdtdz, inv_gxy2, inv_gxz2, inv_gyz2, quarterLambda, quarterLambda2, halfLambda12e;
+    float dV, dxdydz, g;
+    int fric, damp;
+};
+
+inline PairCoef pair_coef(const StepCoef& c)
+{
+    PairCoef o;
+    o.inv_dx2 = (float)c.inv_dx2;
+    o.inv_dy2 = (float)c.inv_dy2;
+    o.inv_dz2 = (float)c.inv_dz2;
+    o.dt2 = (float)c.dt2;
+    o.halfLambda = (float)c.halfLambda;
+    o.etaSq = (float)c.etaSq;
+    o.halfLambda2 = (float)c.halfLambda2;
+    o.eta2Sq = (float)c.eta2Sq;
+    o.halfLambda12 = (float)c.halfLambda12;
+    o.m2gg = (float)c.m2gg;
+    o.fric_dt = (float)(c.fric * c.inv_dt);
+    o.damp_dt = (float)(c.damp * c.inv_dt);
+    o.inv_dt = (float)c.inv_dt;
+    o.inv_dx = (float)c.inv_dx;
+    o.inv_dy = (float)c.inv_dy;
+    o.inv_dz = (float)c.inv_dz;
+    o.inv_g = (float)c.inv_g;
+    o.twog = (float)c.twog;
+    o.inv_gdtdx = (float)c.inv_gdtdx;
+    o.inv_gdtdy = (float)c.inv_gdtdy;
+    o.inv_gdtdz = (float)c.inv_gdtdz;
+    o.inv_gxy2 = (float)c.inv_gxy2;
+    o.inv_gxz2 = (float)c.inv_gxz2;
+    o.inv_gyz2 = (float)c.inv_gyz2;
+    o.quarterLambda = (float)c.quarterLambda;
+    o.quarterLambda2 = (float)c.quarterLambda2;
+    o.halfLambda12e = (float)c.halfLambda12e;
+    o.dV = (float)c.dV;
+    o.dxdydz = (float)(c.dx * c.dy * c.dz);
+    o.g = (float)c.g;
+    o.fric = c.fric != 0;
+    o.damp = c.damp != 0;
+    return o;
+}
+
+// Issue the 16-byte copies of plane `pi` into stage b: thread p < PT_HY*PT_NQ
+// copies (row p / PT_NQ, chunk p % PT_NQ) of every component.  Chunk q of row
+// hy holds z = k0-4+4q .. k0-1+4q of row j0-1+hy; only the rows and chunks the
+// tile's in-range sites use are copied (rows hy <= wy+1, chunks q <= 1+wz/4),
+// whose indices wrap at most once.
+template <int NS>
+__device__ __forceinline__ void pair_stage(PairSmem<NS>& sm, int b, const Fields<float, 2 * NS + 3>& f, const Geom& g,
+                                           int pi, int off, int dst)
+{
+    if (dst >= 0) {
+        const long long s = (long long)pi * g.syz + off;
+#pragma unroll
+        for (int c = 0; c < 2 * NS + 3; ++c)
+            __pipeline_memcpy_async(&sm.st[b][c][0][0] + dst, f.now[c] + s, 16);
+    }
+    __pipeline_commit();
+}
+
+// One tile: z-pairs (bx*64.., by*8..) of the evolved region, x-planes
+// [bz*chunk, bz*chunk + chunk).  Called by every thread of the CTA.  With DIAG
+// the CTA's energy and |G| sums are written to part[0], part[1].
+template <int NS, bool DIAG>
+__device__ __forceinline__ void pair_tile(PairSmem<NS>& sm, const Geom& g, const Fields<float, 2 * NS + 3>& f,
+                                          const PairCoef& c, const Charges<float>& ch, const DiagOut& d, int bx,
+                                          int by, int bz, int chunk, double* part)
+{
+    using LI = LinkIdx<NS>;
+    constexpr int TH = 2 * NS;  // first theta component
+
+    const int tz = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * PT_TZ + tz;
+    const int k0 = bx * PT_Z;
+    const int j0 = g.loy + by * PT_Y;
+    const int ib = g.lox + bz * chunk;
+    const int ie = min(ib + chunk, g.hix);
+    const int wy = min(PT_Y, g.hiy - j0), wz = min(PT_Z, g.nz - k0);
+    const int k = k0 + 2 * tz, j = j0 + ty;
+    const bool active = (2 * tz < wz) && (ty < wy);
+    const int kk = active ? k : k0, jj = active ? j : j0;    // in-range copy for the prologue loads
+    const int hy = ty + 1;                                    // own staged row
+    const int col = PT_C0 + 2 * tz;                           // own staged column (z = k)
+    const int ly = ty + 1, lcol = PT_LC0 + 2 * tz;            // own link position
+
+    // staging plan: (row, chunk) of this thread, or none
+    int soff = 0, sdst = -1;
+    {
+        const int hq = tid / PT_NQ, q = tid - hq * PT_NQ;
+        if (tid < PT_HY * PT_NQ && hq <= wy + 1 && q <= 1 + (wz >> 2)) {
+            soff = wrap_idx(j0 - 1 + hq, g.ny) * g.nz + wrap_idx(k0 - 4 + 4 * q, g.nz);
+            sdst = hq * PT_PZ + 4 * q;
+        }
+    }
+    // halo tasks: warp 0 the low row (ly = 0) as pairs, warp 1's first 8 lanes the low column (z = k0-1)
+    const bool halo_row = ty == 0;
+    const bool halo_col = ty == 1 && tz < PT_Y;
+
+    const float2 inv_dx2 = p2(c.inv_dx2), inv_dy2 = p2(c.inv_dy2), inv_dz2 = p2(c.inv_dz2);
+
+    // ---- prologue: link data and fields of plane ib-1 for the own pair
+    const int im = wrap_idx(ib - 1, g.nx), ib0 = wrap_idx(ib, g.nx);
+    float2 cxm[NS], sxm[NS], vm[2 * NS], sPxy_xm, sPxz_xm, txm;
+    {
+        const long long s = ((long long)im * g.ny + jj) * g.nz + kk;
+        const long long sxp = ((long long)ib0 * g.ny + jj) * g.nz + kk;
+        const long long syp = ((long long)im * g.ny + wrap_idx(jj + 1, g.ny)) * g.nz + kk;
+        const long long szp = ((long long)im * g.ny + jj) * g.nz + wrap_idx(kk + 2, g.nz);
+        const float2 tx = *reinterpret_cast<const float2*>(f.now[TH] + s);
+        const float2 tyv = *reinterpret_cast<const float2*>(f.now[TH + 1] + s);
+        const float2 tzv = *reinterpret_cast<const float2*>(f.now[TH + 2] + s);
+        const float2 tyxp = *reinterpret_cast<const float2*>(f.now[TH + 1] + sxp);
+        const float2 tzxp = *reinterpret_cast<const float2*>(f.now[TH + 2] + sxp);
+        const float2 txyp = *reinterpret_cast<const float2*>(f.now[TH] + syp);
+        const float2 txzp = make_float2(tx.y, f.now[TH][szp]);
+        float2 c1, s1;
+        sincos2(tx, s1, c1);
+#pragma unroll
+        for (int q = 0; q < NS; ++q) charged2(tx, c1, s1, ch, q, cxm[q], sxm[q]);
+        sPxy_xm = sin2(sub2(sub2(add2(tx, tyxp), txyp), tyv));
+        sPxz_xm = sin2(sub2(sub2(add2(tx, tzxp), txzp), tzv));
+        txm = tx;
+#pragma unroll
+        for (int cc = 0; cc < 2 * NS; ++cc) vm[cc] = *reinterpret_cast<const float2*>(f.now[cc] + s);
+    }
+    int cur = 0;
+    pair_stage<NS>(sm, 0, f, g, ib0, soff, sdst);
+    pair_stage<NS>(sm, 1, f, g, wrap_idx(ib + 1, g.nx), soff, sdst);
+
+    double e_acc = 0.0, g_acc = 0.0;
+    // own values of the current plane carried from the previous plane's x-forward reads
+    float2 v[2 * NS], tyo, tzo;
+    bool carried = false;
+
+    // Two barriers per plane (as tiled_step.cuh): the first makes planes i and
+    // i+1 visible and ends every read of plane i-1's stage and link data; the
+    // second publishes the link data of plane i.
+    for (int i = ib; i < ie; ++i) {
+        const int nxt = cur == 2 ? 0 : cur + 1;
+        const int nn = nxt == 2 ? 0 : nxt + 1;
+        __pipeline_wait_prior(0);
+        __syncthreads();
+        if (i + 1 < ie) pair_stage<NS>(sm, nn, f, g, wrap_idx(i + 2, g.nx), soff, sdst);
+        const float* S = &sm.st[cur][0][0][0];
+        const float* X = &sm.st[nxt][0][0][0];
+        constexpr int CS = PT_HY * PT_PZ;   // floats per staged component
+        auto at = [&](const float* base, int comp, int row, int column) { return base + comp * CS + row * PT_PZ + column; };
+
+        // the own pair's level n-1, loaded now so that the link phase covers the latency
+        const long long s = ((long long)i * g.ny + jj) * g.nz + kk;
+        float2 qv[2 * NS + 3];
+        if (active) {
+#pragma unroll
+            for (int cc = 0; cc < 2 * NS + 3; ++cc) qv[cc] = *reinterpret_cast<const float2*>(f.past[cc] + s);
+        } else {
+#pragma unroll
+            for (int cc = 0; cc < 2 * NS + 3; ++cc) qv[cc] = p2(0.f);
+        }
+
+        // ---- link data of the own pair
+        const float2 tx = lds2(at(S, TH, hy, col));
+        if (!carried) {
+            tyo = lds2(at(S, TH + 1, hy, col));
+            tzo = lds2(at(S, TH + 2, hy, col));
+        }
+        const float2 tyv = tyo, tzv = tzo;
+        const float2 tyxp = lds2(at(X, TH + 1, hy, col)), tzxp = lds2(at(X, TH + 2, hy, col));
+        const float2 txyp = lds2(at(S, TH, hy + 1, col)), tzyp = lds2(at(S, TH + 2, hy + 1, col));
+        const float2 txzp = make_float2(tx.y, *at(S, TH, hy, col + 2));
+        const float2 tyzp = make_float2(tyv.y, *at(S, TH + 1, hy, col + 2));
+        float2 cx[NS], sx[NS], cy[NS], sy[NS], cz[NS], sz[NS], sPxy, sPxz, sPyz, cP[3];
+        {
+            float2 c1, s1;
+            sincos2(tx, s1, c1);
+#pragma unroll
+            for (int q = 0; q < NS; ++q) charged2(tx, c1, s1, ch, q, cx[q], sx[q]);
+            sincos2(tyv, s1, c1);
+#pragma unroll
+            for (int q = 0; q < NS; ++q) charged2(tyv, c1, s1, ch, q, cy[q], sy[q]);
+            sincos2(tzv, s1, c1);
+#pragma unroll
+            for (int q = 0; q < NS; ++q) charged2(tzv, c1, s1, ch, q, cz[q], sz[q]);
+            const float2 Pxy = sub2(sub2(add2(tx, tyxp), txyp), tyv);
+            const float2 Pxz = sub2(sub2(add2(tx, tzxp), txzp), tzv);
+            const float2 Pyz = sub2(sub2(add2(tyv, tzyp), tyzp), tzv);
+            if constexpr (DIAG) {
+                sincos2(Pxy, sPxy, cP[0]);
+                sincos2(Pxz, sPxz, cP[1]);
+                sincos2(Pyz, sPyz, cP[2]);
+            } else {
+                sPxy = sin2(Pxy);
+                sPxz = sin2(Pxz);
+                sPyz = sin2(Pyz);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            sts2(&sm.L[LI::cy(q)][ly][lcol], cy[q]);
+            sts2(&sm.L[LI::sy(q)][ly][lcol], sy[q]);
+            sts2(&sm.L[LI::cz(q)][ly][lcol], cz[q]);
+            sts2(&sm.L[LI::sz(q)][ly][lcol], sz[q]);
+        }
+        sts2(&sm.L[LI::pxy][ly][lcol], sPxy);
+        sts2(&sm.L[LI::pxz][ly][lcol], sPxz);
+        sts2(&sm.L[LI::pyz][ly][lcol], sPyz);
+        if (halo_row) {
+            // row j0-1 (staged row 0), the pair at z = k: what row j0 reads as its y-backward data
+            const float2 hty = lds2(at(S, TH + 1, 0, col)), htx = lds2(at(S, TH, 0, col));
+            const float2 htz = lds2(at(S, TH + 2, 0, col));
+            const float2 htyxp = lds2(at(X, TH + 1, 0, col)), htxyp = lds2(at(S, TH, 1, col));
+            const float2 htzyp = lds2(at(S, TH + 2, 1, col));
+            const float2 htyzp = make_float2(hty.y, *at(S, TH + 1, 0, col + 2));
+            float2 c1, s1, hc, hs;
+            sincos2(hty, s1, c1);
+#pragma unroll
+            for (int q = 0; q < NS; ++q) {
+                charged2(hty, c1, s1, ch, q, hc, hs);
+                sts2(&sm.L[LI::cy(q)][0][lcol], hc);
+                sts2(&sm.L[LI::sy(q)][0][lcol], hs);
+            }
+            sts2(&sm.L[LI::pxy][0][lcol], sin2(sub2(sub2(add2(htx, htyxp), htxyp), hty)));
+            sts2(&sm.L[LI::pyz][0][lcol], sin2(sub2(sub2(add2(hty, htzyp), htyzp), htz)));
+        }
+        if (halo_col) {
+            // z = k0-1 of row j0+tz (staged column PT_C0-1): what z = k0 reads as its z-backward data
+            const int r = tz + 1;
+            const float htx = *at(S, TH, r, PT_C0 - 1), hty = *at(S, TH + 1, r, PT_C0 - 1);
+            const float htz = *at(S, TH + 2, r, PT_C0 - 1);
+            const float htzxp = *at(X, TH + 2, r, PT_C0 - 1), htxzp = *at(S, TH, r, PT_C0);
+            const float htzyp = *at(S, TH + 2, r + 1, PT_C0 - 1), htyzp = *at(S, TH + 1, r, PT_C0);
+            float s1, c1;
+            Trig<float>::sincos(htz, &s1, &c1);
+#pragma unroll
+            for (int q = 0; q < NS; ++q) {
+                float hc, hs;
+                charged<float>(htz, c1, s1, ch, q, hc, hs);
+                sm.L[LI::cz(q)][r][PT_LC0 - 1] = hc;
+                sm.L[LI::sz(q)][r][PT_LC0 - 1] = hs;
+            }
+            sm.L[LI::pxz][r][PT_LC0 - 1] = Trig<float>::sin(htx + htzxp - htxzp - htz);
+            sm.L[LI::pyz][r][PT_LC0 - 1] = Trig<float>::sin(hty + htzyp - htyzp - htz);
+        }
+        __syncthreads();
+
+        if (!carried) {
+#pragma unroll
+            for (int cc = 0; cc < 2 * NS; ++cc) v[cc] = lds2(at(S, cc, hy, col));
+        }
+        // x-forward neighbours: the next plane's own values
+        float2 vxp[2 * NS];
+#pragma unroll
+        for (int cc = 0; cc < 2 * NS; ++cc) vxp[cc] = lds2(at(X, cc, hy, col));
+        if (active) {
+            const float2 sPxy_ym = lds2(&sm.L[LI::pxy][ly - 1][lcol]), sPyz_ym = lds2(&sm.L[LI::pyz][ly - 1][lcol]);
+            const float2 sPxz_zm = make_float2(sm.L[LI::pxz][ly][lcol - 1], sPxz.x);
+            const float2 sPyz_zm = make_float2(sm.L[LI::pyz][ly][lcol - 1], sPyz.x);
+
+            float2 mag[NS], npot[NS];
+#pragma unroll
+            for (int q = 0; q < NS; ++q) mag[q] = fma2(v[2 * q], v[2 * q], mul2(v[2 * q + 1], v[2 * q + 1]));
+            if constexpr (NS == 1) {
+                npot[0] = mul2(p2(-c.halfLambda), sub2(mag[0], p2(c.etaSq)));
+            } else {
+                const float2 m1 = sub2(mag[0], p2(c.etaSq)), m2 = sub2(mag[1], p2(c.eta2Sq));
+                npot[0] = neg2(fma2(p2(c.halfLambda), m1, mul2(p2(c.halfLambda12), m2)));
+                npot[1] = neg2(fma2(p2(c.halfLambda2), m2, mul2(p2(c.halfLambda12), m1)));
+            }
+            float2 acc[2 * NS];
+            float2 curx = p2(0.f), cury = p2(0.f), curz = p2(0.f), gsum = p2(0.f);
+            float2 pt[2 * NS], pd[NS][3][2];
+#pragma unroll
+            for (int q = 0; q < NS; ++q) {
+                const float2 re = v[2 * q], imv = v[2 * q + 1];
+                const float2 rexp = vxp[2 * q], imxp = vxp[2 * q + 1];
+                const float2 reyp = lds2(at(S, 2 * q, hy + 1, col)), imyp = lds2(at(S, 2 * q + 1, hy + 1, col));
+                const float2 reym = lds2(at(S, 2 * q, hy - 1, col)), imym = lds2(at(S, 2 * q + 1, hy - 1, col));
+                const float2 rezp = make_float2(re.y, *at(S, 2 * q, hy, col + 2));
+                const float2 imzp = make_float2(imv.y, *at(S, 2 * q + 1, hy, col + 2));
+                const float2 rezm = make_float2(*at(S, 2 * q, hy, col - 1), re.x);
+                const float2 imzm = make_float2(*at(S, 2 * q + 1, hy, col - 1), imv.x);
+                const float2 rexm = vm[2 * q], imxm = vm[2 * q + 1];
+                const float2 cym = lds2(&sm.L[LI::cy(q)][ly - 1][lcol]), sym = lds2(&sm.L[LI::sy(q)][ly - 1][lcol]);
+                const float2 czm = make_float2(sm.L[LI::cz(q)][ly][lcol - 1], cz[q].x);
+                const float2 szm = make_float2(sm.L[LI::sz(q)][ly][lcol - 1], sz[q].x);
+                const float2 m2re = mul2(p2(-2.f), re), m2im = mul2(p2(-2.f), imv);
+                // covariant Laplacian: c = +1 for the real part, -1 for the imaginary part
+                float2 lx = fma2(cx[q], rexp, fma2(sx[q], imxp, fma2(cxm[q], rexm, fma2(neg2(sxm[q]), imxm, m2re))));
+                float2 lyv = fma2(cy[q], reyp, fma2(sy[q], imyp, fma2(cym, reym, fma2(neg2(sym), imym, m2re))));
+                float2 lz = fma2(cz[q], rezp, fma2(sz[q], imzp, fma2(czm, rezm, fma2(neg2(szm), imzm, m2re))));
+                float2 a_re = fma2(lz, inv_dz2, fma2(lyv, inv_dy2, fma2(lx, inv_dx2, mul2(npot[q], re))));
+                lx = fma2(cx[q], imxp, fma2(neg2(sx[q]), rexp, fma2(cxm[q], imxm, fma2(sxm[q], rexm, m2im))));
+                lyv = fma2(cy[q], imyp, fma2(neg2(sy[q]), reyp, fma2(cym, imym, fma2(sym, reym, m2im))));
+                lz = fma2(cz[q], imzp, fma2(neg2(sz[q]), rezp, fma2(czm, imzm, fma2(szm, rezm, m2im))));
+                float2 a_im = fma2(lz, inv_dz2, fma2(lyv, inv_dy2, fma2(lx, inv_dx2, mul2(npot[q], imv))));
+                if (c.fric) {
+                    a_re = fma2(p2(-c.fric_dt), sub2(re, qv[2 * q]), a_re);
+                    a_im = fma2(p2(-c.fric_dt), sub2(imv, qv[2 * q + 1]), a_im);
+                }
+                acc[2 * q] = a_re;
+                acc[2 * q + 1] = a_im;
+                // gauge current of this scalar
+                const float2 nre = neg2(re);
+                float2 jx = fma2(cx[q], fma2(imv, rexp, mul2(nre, imxp)), mul2(sx[q], fma2(re, rexp, mul2(imv, imxp))));
+                float2 jy = fma2(cy[q], fma2(imv, reyp, mul2(nre, imyp)), mul2(sy[q], fma2(re, reyp, mul2(imv, imyp))));
+                float2 jz = fma2(cz[q], fma2(imv, rezp, mul2(nre, imzp)), mul2(sz[q], fma2(re, rezp, mul2(imv, imzp))));
+                if (ch.charge_current) {
+                    jx = mul2(jx, p2(ch.q[q]));
+                    jy = mul2(jy, p2(ch.q[q]));
+                    jz = mul2(jz, p2(ch.q[q]));
+                }
+                curx = add2(curx, jx);
+                cury = add2(cury, jy);
+                curz = add2(curz, jz);
+                if constexpr (DIAG) {
+                    pt[2 * q] = mul2(sub2(re, qv[2 * q]), p2(c.inv_dt));
+                    pt[2 * q + 1] = mul2(sub2(imv, qv[2 * q + 1]), p2(c.inv_dt));
+                    pd[q][0][0] = mul2(fma2(sxm[q], imxm, fma2(neg2(cxm[q]), rexm, re)), p2(c.inv_dx));
+                    pd[q][0][1] = mul2(fma2(neg2(sxm[q]), rexm, fma2(neg2(cxm[q]), imxm, imv)), p2(c.inv_dx));
+                    pd[q][1][0] = mul2(fma2(sym, imym, fma2(neg2(cym), reym, re)), p2(c.inv_dy));
+                    pd[q][1][1] = mul2(fma2(neg2(sym), reym, fma2(neg2(cym), imym, imv)), p2(c.inv_dy));
+                    pd[q][2][0] = mul2(fma2(szm, imzm, fma2(neg2(czm), rezm, re)), p2(c.inv_dz));
+                    pd[q][2][1] = mul2(fma2(neg2(szm), rezm, fma2(neg2(czm), imzm, imv)), p2(c.inv_dz));
+                    const float qq = NS == 1 ? 1.f : ch.q[q];
+                    gsum = fma2(p2(qq), fma2(imv, pt[2 * q], mul2(nre, pt[2 * q + 1])), gsum);
+                }
+            }
+            // lattice curl with sin(P_yx) = -sin(P_xy), sin(P_zx) = -sin(P_xz), sin(P_zy) = -sin(P_yz)
+            const float2 Fxy_y = mul2(sub2(sPxy, sPxy_ym), inv_dy2);
+            const float2 Fxz_z = mul2(sub2(sPxz, sPxz_zm), inv_dz2);
+            const float2 Fyx_x = mul2(sub2(sPxy_xm, sPxy), inv_dx2);
+            const float2 Fyz_z = mul2(sub2(sPyz, sPyz_zm), inv_dz2);
+            const float2 Fzx_x = mul2(sub2(sPxz_xm, sPxz), inv_dx2);
+            const float2 Fzy_y = mul2(sub2(sPyz_ym, sPyz), inv_dy2);
+            float2 ttx = fma2(p2(c.m2gg), curx, neg2(add2(Fxy_y, Fxz_z)));
+            float2 tty = fma2(p2(c.m2gg), cury, neg2(add2(Fyx_x, Fyz_z)));
+            float2 ttz = fma2(p2(c.m2gg), curz, neg2(add2(Fzx_x, Fzy_y)));
+            if (c.damp) {
+                ttx = fma2(p2(-c.damp_dt), sub2(tx, qv[TH]), ttx);
+                tty = fma2(p2(-c.damp_dt), sub2(tyv, qv[TH + 1]), tty);
+                ttz = fma2(p2(-c.damp_dt), sub2(tzv, qv[TH + 2]), ttz);
+            }
+            float2 divNow = p2(0.f);
+            if (DIAG || d.store_div) {
+                const float2 tym = lds2(at(S, TH + 1, hy - 1, col));
+                const float2 tzm = make_float2(*at(S, TH + 2, hy, col - 1), tzv.x);
+                divNow = fma2(sub2(tzv, tzm), inv_dz2, fma2(sub2(tyv, tym), inv_dy2, mul2(sub2(tx, txm), inv_dx2)));
+            }
+            if constexpr (DIAG) {
+                float2 tdc = p2(0.f), fc = p2(0.f), gauss = p2(0.f);
+                const float2 onem0 = sub2(p2(1.f), cP[0]), onem1 = sub2(p2(1.f), cP[1]), onem2 = sub2(p2(1.f), cP[2]);
+                if (d.energy_form == LAT_ENERGY_MPI) {
+                    const float2 a0 = mul2(sub2(tx, qv[TH]), p2(c.inv_dt)), a1 = mul2(sub2(tyv, qv[TH + 1]), p2(c.inv_dt));
+                    const float2 a2 = mul2(sub2(tzv, qv[TH + 2]), p2(c.inv_dt));
+                    tdc = mul2(p2(0.5f), fma2(a2, a2, fma2(a1, a1, mul2(a0, a0))));
+                    fc = fma2(onem2, p2(c.inv_gyz2), fma2(onem1, p2(c.inv_gxz2), mul2(onem0, p2(c.inv_gxy2))));
+                }
+                if (c.g != 0) {
+                    const float2 divPast = *reinterpret_cast<const float2*>(reinterpret_cast<const float*>(d.divbuf) + s);
+                    gauss = fma2(p2(-c.twog), gsum, mul2(mul2(sub2(divNow, divPast), p2(c.inv_dt)), p2(c.inv_g)));
+                    if (d.energy_form != LAT_ENERGY_MPI) {
+                        const float2 a0 = mul2(sub2(tx, qv[TH]), p2(c.inv_gdtdx));
+                        const float2 a1 = mul2(sub2(tyv, qv[TH + 1]), p2(c.inv_gdtdy));
+                        const float2 a2 = mul2(sub2(tzv, qv[TH + 2]), p2(c.inv_gdtdz));
+                        tdc = mul2(p2(0.5f), fma2(a2, a2, fma2(a1, a1, mul2(a0, a0))));
+                        fc = fma2(onem2, p2(c.inv_gyz2), fma2(onem1, p2(c.inv_gxz2), mul2(onem0, p2(c.inv_gxy2))));
+                    }
+                }
+                float2 ed = p2(0.f);
+#pragma unroll
+                for (int q = 0; q < NS; ++q) {
+                    ed = fma2(pt[2 * q], pt[2 * q], ed);
+                    ed = fma2(pt[2 * q + 1], pt[2 * q + 1], ed);
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        ed = fma2(pd[q][a][0], pd[q][a][0], ed);
+                        ed = fma2(pd[q][a][1], pd[q][a][1], ed);
+                    }
+                }
+                const float2 m1 = sub2(mag[0], p2(c.etaSq));
+                ed = add2(add2(ed, add2(tdc, fc)), mul2(p2(c.quarterLambda), mul2(m1, m1)));
+                if constexpr (NS == 2) {
+                    const float2 m2 = sub2(mag[1], p2(c.eta2Sq));
+                    ed = fma2(p2(c.quarterLambda2), mul2(m2, m2), ed);
+                    ed = fma2(mul2(p2(c.halfLambda12e), m1), m2, ed);
+                }
+                const float scale = d.energy_form == LAT_ENERGY_MPI ? c.dxdydz : c.dV;
+                e_acc += (double)(ed.x * scale) + (double)(ed.y * scale);
+                g_acc += (double)fabsf(gauss.x) + (double)fabsf(gauss.y);
+            }
+            if (d.store_div) *reinterpret_cast<float2*>(reinterpret_cast<float*>(d.divbuf) + s) = divNow;
+            if (d.write) {
+                const float2 dt2 = p2(c.dt2);
+#pragma unroll
+                for (int cc = 0; cc < 2 * NS; ++cc)
+                    *reinterpret_cast<float2*>(f.past[cc] + s) = fma2(dt2, acc[cc], add2(v[cc], sub2(v[cc], qv[cc])));
+                *reinterpret_cast<float2*>(f.past[TH] + s) = fma2(dt2, ttx, add2(tx, sub2(tx, qv[TH])));
+                *reinterpret_cast<float2*>(f.past[TH + 1] + s) = fma2(dt2, tty, add2(tyv, sub2(tyv, qv[TH + 1])));
+                *reinterpret_cast<float2*>(f.past[TH + 2] + s) = fma2(dt2, ttz, add2(tzv, sub2(tzv, qv[TH + 2])));
+            }
+        }
+        // carry: x-backward data of the next plane, and its own values read here as x-forward neighbours
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+            cxm[q] = cx[q];
+            sxm[q] = sx[q];
+        }
+        sPxy_xm = sPxy;
+        sPxz_xm = sPxz;
+        txm = tx;
+#pragma unroll
+        for (int cc = 0; cc < 2 * NS; ++cc) {
+            vm[cc] = v[cc];
+            v[cc] = vxp[cc];
+        }
+        tyo = tyxp;
+        tzo = tzxp;
+        carried = true;
+        cur = nxt;
+    }
+    __pipeline_wait_prior(0);  // nothing is in flight here; kept for an empty x-range
+
+    if constexpr (DIAG) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            e_acc += __shfl_down_sync(0xffffffffu, e_acc, o);
+            g_acc += __shfl_down_sync(0xffffffffu, g_acc, o);
+        }
+        if (tz == 0) {
+            sm.red[0][ty] = e_acc;
+            sm.red[1][ty] = g_acc;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double a = 0, b = 0;
+            for (int w = 0; w < PT_Y; ++w) {
+                a += sm.red[0][w];
+                b += sm.red[1][w];
+            }
+            part[0] = a;
+            part[1] = b;
+        }
+        __syncthreads();  // sm.red is reused by the CTA's next tile
+    }
+}
+
+template <int NS, bool DIAG>
+__global__ void __launch_bounds__(PT_THREADS, 2)
+pair_step_kernel(const Geom g, const Fields<float, 2 * NS + 3> f, const PairCoef c, const Charges<float> ch,
+                 const DiagOut d, const int chunk)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PairSmem<NS>& sm = *reinterpret_cast<PairSmem<NS>*>(smem_raw);
+    const int blk = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    pair_tile<NS, DIAG>(sm, g, f, c, ch, d, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, chunk,
+                        DIAG ? d.partials + 2 * blk : nullptr);
+}
+
+// Launch the pair step if the layout allows it; returns cudaErrorNotSupported
+// (nothing launched) otherwise.
+template <int NS>
+cudaError_t launch_pair_t(const Geom& g, const Fields<float, 2 * NS + 3>& f, const StepCoef& c64, const DiagOut& d,
+                          bool diag, int chunk, cudaStream_t st)
+{
+    if (!pair_ok(g, f)) return cudaErrorNotSupported;
+    Charges<float> ch;
+    if (NS == 1) {
+        ch.q[0] = 1;
+        ch.q[1] = 0;
+        ch.qpow[0] = 1;
+        ch.qpow[1] = 0;
+    } else {
+        ch.q[0] = (float)c64.q1;
+        ch.q[1] = (float)c64.q2;
+        ch.qpow[0] = small_int_power(c64.q1);
+        ch.qpow[1] = small_int_power(c64.q2);
+    }
+    ch.charge_current = d.charge_current;
+    const PairCoef c = pair_coef(c64);
+    const size_t smem = sizeof(PairSmem<NS>);
+    cudaFuncSetAttribute(pair_step_kernel<NS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(pair_step_kernel<NS, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const dim3 grid = pair_grid(g, chunk);
+    const dim3 block(PT_TZ, PT_Y);
+    if (diag) pair_step_kernel<NS, true><<<grid, block, smem, st>>>(g, f, c, ch, d, chunk);
+    else pair_step_kernel<NS, false><<<grid, block, smem, st>>>(g, f, c, ch, d, chunk);
+    return cudaGetLastError();
+}
+
+}  // namespace lat

@@ -447,12 +447,15 @@ def test_twopass_strict_bitwise_equals_onepass_above_int32_link_offsets(lattice_
     assert np.array_equal(a_now, b_now) and np.array_equal(a_past, b_past)
 
 
-@pytest.mark.parametrize("d", [0.5, 0.35])
+@pytest.mark.parametrize("d", [0.5, 0.35, (0.5, 0.4, 0.35), (0.5, 0.25, 0.5)])
 def test_fp64_fast_meets_parity_bar(lattice_mod, oracle_mod, d):
-    """LAT_F64_FAST (fused multiply-adds) against the oracle: 48^3, 300 steps,
-    config-1 physics; also a spacing that is not a power of two."""
+    """LAT_F64_FAST (fused multiply-adds; directions summed before one
+    scaling when the spacings are equal) against the oracle: 48^3, 300 steps,
+    config-1 physics with PRS friction; power-of-two and other spacings,
+    equal and unequal."""
     from axions_gb300.params import ENERGY_EVOLUTION, F64_FAST, make_params
-    p = make_params(0, n=48, d=d, dt=0.1, lam=2.0, eta=1.0, g=1.0, damped_nt=0, alpha=0.0,
+    dx, dy, dz = d if isinstance(d, tuple) else (d, d, d)
+    p = make_params(0, n=48, dx=dx, dy=dy, dz=dz, dt=0.1, lam=2.0, eta=1.0, g=1.0, damped_nt=0, alpha=3.0,
                     energy_form=ENERGY_EVOLUTION)
     st = oracle_mod.random_phase_ic(p, 4)
     ref = oracle_mod.evolve(p, st, 0, 300, diag_every=50)
@@ -547,8 +550,8 @@ def test_fp32_tiled_moore(lattice_mod, bc, charges, current):
 @pytest.mark.parametrize("sides", [(70, 29, 44), (33, 17, 32), (40, 12, 100), (24, 20, 36), (10, 3, 4), (9, 5, 8)])
 def test_fp32_tiled_vector_staging_is_bitwise_the_element_staging(lattice_mod, model, sides):
     """With periodic z and nz a multiple of 4 the tiled FP32 step stages its
-    planes in 16-byte row chunks; kernel_variant 2 stages one element per
-    copy.  Both fill the same shared-memory positions and the arithmetic is
+    planes in 16-byte row chunks (kernel_variant 3); kernel_variant 2 stages
+    one element per copy.  Both fill the same shared-memory positions and the arithmetic is
     the same, so fields and diagnostics are bitwise equal.  The sides cover a
     partial last z tile, one tile wrapping at both ends, four tiles, a right
     edge cut to the lattice, and lattices narrower than the tile (nz = 4,
@@ -564,7 +567,7 @@ def test_fp32_tiled_vector_staging_is_bitwise_the_element_staging(lattice_mod, m
                         energy_form=ENERGY_EVOLUTION, precision=F32)
     ic = lattice_mod.random_phase_ic(p, 31, independent=model == 1)
     out = []
-    for variant in (0, 2):
+    for variant in (3, 2):
         q = p.copy()
         q.kernel_variant = variant
         with lattice_mod.Lattice(q) as lat:
@@ -573,3 +576,45 @@ def test_fp32_tiled_vector_staging_is_bitwise_the_element_staging(lattice_mod, m
             out.append((lat.get_slots(), d))
     assert np.array_equal(out[0][0], out[1][0])
     assert out[0][1] == out[1][1]
+
+
+@pytest.mark.parametrize("model", [0, 1])
+@pytest.mark.parametrize("sides,bc", [((40, 36, 64), 0), ((33, 17, 96), 0), ((24, 20, 4), 0), ((21, 19, 44), 1),
+                                      ((9, 11, 132), 1), ((70, 29, 8), 0)])
+def test_fp32_pair_step_tracks_tiled_and_fp64(lattice_mod, model, sides, bc):
+    """The pair step (two z-sites per thread in paired FP32 arithmetic; the
+    default where z is periodic and nz a multiple of 4) against the tiled
+    step (kernel_variant 3) and the FP64 path: 12 steps with energy/Gauss
+    every 4, periodic and fixed x/y walls, z extents that fill 64-wide tiles,
+    end in a partial tile, or are narrower than a tile.  The two FP32 steps
+    round differently (other contractions), so they agree to FP32 accuracy,
+    not bitwise: fields L2 within 2e-6, max within 2e-5 of the FP64 path's,
+    energies 1e-5 and Gauss sums 1e-4 relative."""
+    from axions_gb300.params import ENERGY_EVOLUTION, F32, MODEL_MOORE, make_params
+    nx, ny, nz = sides
+    if model == 0:
+        p = make_params(0, nx=nx, ny=ny, nz=nz, d=0.5, dt=0.1, lam=2.0, g=1.0, damped_nt=3, dampFac=0.5, alpha=3.0,
+                        energy_form=ENERGY_EVOLUTION, bc=bc, bc_z=1)
+    else:
+        p = make_params(MODEL_MOORE, nx=nx, ny=ny, nz=nz, d=0.5, dt=0.1, lam=2.0, lambda2=2.0, lambda12=0.3,
+                        eta=1.0, eta2=1.0, q1=1.0, q2=2.0, g=0.8, damped_nt=3, dampFac=0.5, alpha=3.0, bc=bc, bc_z=1,
+                        energy_form=ENERGY_EVOLUTION, moore_current=1)
+    ic = lattice_mod.random_phase_ic(p, 41, independent=model == 1)
+    res = {}
+    for name, prec, var in (("f64", 0, 0), ("pair", F32, 0), ("tiled", F32, 3)):
+        q = p.copy()
+        q.precision = prec
+        q.kernel_variant = var
+        with lattice_mod.Lattice(q) as lat:
+            lat.set_state(ic, ic, 0)
+            d = lat.advance(12, diag_every=4)
+            res[name] = (lat.get_slots(), d)
+    s64 = res["f64"][0]
+    for name in ("pair", "tiled"):
+        st, d = res[name]
+        mx, l2 = normwise(st, s64)
+        assert l2 < 2e-6 and mx < 2e-5, (name, mx, l2)
+        np.testing.assert_allclose([x[1] for x in d], [x[1] for x in res["f64"][1]], rtol=1e-5)
+        np.testing.assert_allclose([x[2] for x in d], [x[2] for x in res["f64"][1]], rtol=1e-4)
+    mx, l2 = normwise(res["pair"][0], res["tiled"][0])
+    assert l2 < 2e-6, l2

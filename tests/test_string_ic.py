@@ -310,7 +310,13 @@ def test_sine_string_ic_against_reference(lattice_mod, oracle_mod, name):
 def test_sine_string_ic_at_size_against_oracle(lattice_mod, oracle_mod):
     """NG sine on a 64 x 40 x 81 lattice (2,624 searched columns) and simple
     sine on 48^3, against the oracle's restatement (pinned bit-exact on the
-    fixtures above): within 1e-12 of each field's largest value."""
+    fixtures above), relative to each field's largest value: phi within
+    1e-12; the links of NG sine within 1e-6.  (Where CUDA's and glibc's sine
+    round one golden-section comparison differently, the search ends up to
+    its 1e-6 tolerance away in the string parameter sigma; phi depends on it
+    only at second order, the links' tangent factors xs_sigma, zs_sigma at
+    first order, by at most eps*Omega*1e-6: 1.7e-8 seen here.)  Simple sine:
+    every field within 1e-12."""
     z = load_golden("ref_ng_sine_ic")
     prof, h = z["profile"], float(z["sor_h"])
     from axions_gb300.params import make_params
@@ -321,7 +327,8 @@ def test_sine_string_ic_at_size_against_oracle(lattice_mod, oracle_mod):
             off = lat.sine_string_ic_device(prof[0], prof[1], h, eps, kind)
             got = lat.get_slots()
         assert off == off_ref
-        _close(got, want, TOL)
+        _close(got[:2], want[:2], TOL)
+        _close(got[2:], want[2:], TOL if kind == "simple sine" else 1e-6)
 
 
 def test_sine_string_ic_rejects_bad_arguments(lattice_mod):
