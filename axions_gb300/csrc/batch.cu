@@ -4,8 +4,9 @@
 // lattices (different seeds, couplings and sizes) is a loop of separate runs.
 // Here every lattice of a batch advances in the same kernel launch: a
 // persistent grid (one or two CTAs per SM) walks a table of work items, one
-// item per (lattice, y/z tile, x-chunk) of the tiled FP32 step
-// (tiled_step.cuh).  A call advancing K steps is one CUDA graph: a copy of the
+// item per (lattice, y/z tile, x-chunk) of the FP32 step: the pair tile
+// (pair_step.cuh, two z-sites per thread) where the lattice's layout allows
+// it, else the tiled step's tile (tiled_step.cuh).  A call advancing K steps is one CUDA graph: a copy of the
 // K per-step job tables from pinned host memory, then for each step the step
 // kernel and a per-lattice diagnostic reduction.  The graph is reused as long
 // as K is; lattices join and leave between calls by rewriting the tables.
@@ -21,6 +22,7 @@
 #include <vector>
 
 #include "lattice_handle.hpp"
+#include "pair_step.cuh"
 #include "tiled_step.cuh"
 
 namespace lat {
@@ -30,13 +32,17 @@ constexpr int kBatchMaxJobs = 256;
 struct BatchJob {
     Geom g;
     Fields<float, 7> f;     // AH uses the first 5 components
-    StepCoefT<float> c;
+    union {
+        StepCoefT<float> c;  // tiled tile
+        PairCoef pc;         // pair tile
+    };
     Charges<float> ch;
     DiagOut d;
     int ns;                 // scalars: 1 (AH) or 2 (Moore)
     int diag;               // record diagnostics at this step
     int chunk;
     int vec;                // 16-byte staging (tiled_vec_ok)
+    int pair;               // the pair tile (pair_ok); else the tiled tile
     int tiles_z, tiles_y;
     int items;              // tiles_z * tiles_y * x-chunks
     int item_begin;         // first work item of this job in the step
@@ -62,10 +68,16 @@ int batch_chunk(const Geom& g)
 
 namespace {
 
-template <int NS, bool DIAG>
+template <int NS, bool PAIR, bool DIAG>
 __device__ __forceinline__ void run_item(unsigned char* smem_raw, const BatchJob& J, const Fields<float, 5>& f5,
                                          int bx, int by, int bz, double* part)
 {
+    if constexpr (PAIR) {
+        PairSmem<NS>& ps = *reinterpret_cast<PairSmem<NS>*>(smem_raw);
+        if constexpr (NS == 1) pair_tile<1, DIAG>(ps, J.g, f5, J.pc, J.ch, J.d, bx, by, bz, J.chunk, part);
+        else pair_tile<2, DIAG>(ps, J.g, J.f, J.pc, J.ch, J.d, bx, by, bz, J.chunk, part);
+        return;
+    }
     TiledSmem<float, NS>& sm = *reinterpret_cast<TiledSmem<float, NS>*>(smem_raw);
     if constexpr (NS == 1) {
         tiled_tile<float, 1, DIAG>(sm, J.g, f5, J.c, J.ch, J.d, bx, by, bz, J.chunk, part, J.vec != 0);
@@ -74,11 +86,14 @@ __device__ __forceinline__ void run_item(unsigned char* smem_raw, const BatchJob
     }
 }
 
-// Persistent step kernel for the lattices with NS scalars: CTAs stride over
-// the work items of all of them.  One kernel per model keeps each kernel's
-// register use to that model's tile.
-template <int NS>
-__global__ void __launch_bounds__(TT_THREADS, NS == 1 ? 4 : 3) batch_step_kernel(const BatchStep* __restrict__ tab)
+// Persistent step kernel for the lattices with NS scalars that use the pair
+// tile (PAIR) or the tiled tile: CTAs stride over the work items of all of
+// them.  One kernel per model and tile keeps each kernel's register use to
+// that tile's: two CTAs per SM for the pair tile, as the pair step, four
+// (Abelian-Higgs) or three (Moore) for the tiled tile.
+template <int NS, bool PAIR>
+__global__ void __launch_bounds__(TT_THREADS, PAIR ? 2 : (NS == 1 ? 4 : 3))
+batch_step_kernel(const BatchStep* __restrict__ tab)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ BatchJob sj;
@@ -119,8 +134,8 @@ __global__ void __launch_bounds__(TT_THREADS, NS == 1 ? 4 : 3) batch_step_kernel
         const int by = r % sj.tiles_y;
         const int bz = r / sj.tiles_y;
         double* part = sj.diag ? sj.d.partials + 2 * local : nullptr;
-        if (sj.diag) run_item<NS, true>(smem_raw, sj, sf5, bx, by, bz, part);
-        else run_item<NS, false>(smem_raw, sj, sf5, bx, by, bz, part);
+        if (sj.diag) run_item<NS, PAIR, true>(smem_raw, sj, sf5, bx, by, bz, part);
+        else run_item<NS, PAIR, false>(smem_raw, sj, sf5, bx, by, bz, part);
         __syncthreads();  // sj and the tile's shared memory are reused by the next item
     }
 }
@@ -160,11 +175,14 @@ __global__ void __launch_bounds__(1024) batch_finalize_kernel(const BatchStep* _
     }
 }
 
-template <int NS>
+template <int NS, bool PAIR>
 size_t batch_smem_ns()
 {
-    return sizeof(TiledSmem<float, NS>);
+    return PAIR ? sizeof(PairSmem<NS>) : sizeof(TiledSmem<float, NS>);
 }
+
+// job tables per step: [tiled AH, tiled Moore, pair AH, pair Moore]
+constexpr int kTables = 4;
 
 }  // namespace
 
@@ -183,11 +201,11 @@ struct lat_batch {
     int device = 0;
     int max_jobs = 0;
     cudaStream_t stream = nullptr;
-    int grid[2] = {0, 0};            // persistent CTAs of the AH / Moore step kernels
+    int grid[kTables] = {};          // persistent CTAs of each step kernel (table order)
     int K = 0;                       // steps in the captured graph
     int chunk = 0;                   // x-planes per work item; 0: the per-shape rule
-    BatchStep* tab_host = nullptr;   // pinned [K][2]: per step, AH jobs then Moore jobs
-    BatchStep* tab_dev = nullptr;    // [K][2]
+    BatchStep* tab_host = nullptr;   // pinned [K][kTables]: per step, the jobs of each kernel
+    BatchStep* tab_dev = nullptr;    // [K][kTables]
     double* diag_dev = nullptr;      // [K][max_jobs][2]
     double* diag_host = nullptr;     // pinned copy
     cudaGraph_t graph = nullptr;
@@ -226,17 +244,20 @@ static int ensure_graph(lat_batch* b, int K)
 {
     if (b->K == K && b->exec) return LAT_OK;
     release_graph(b);
-    BATCH_CK(cudaMallocHost((void**)&b->tab_host, sizeof(BatchStep) * 2 * (size_t)K));
-    BATCH_CK(cudaMalloc((void**)&b->tab_dev, sizeof(BatchStep) * 2 * (size_t)K));
+    BATCH_CK(cudaMallocHost((void**)&b->tab_host, sizeof(BatchStep) * kTables * (size_t)K));
+    BATCH_CK(cudaMalloc((void**)&b->tab_dev, sizeof(BatchStep) * kTables * (size_t)K));
     BATCH_CK(cudaMalloc((void**)&b->diag_dev, sizeof(double) * 2 * (size_t)K * b->max_jobs));
     BATCH_CK(cudaMallocHost((void**)&b->diag_host, sizeof(double) * 2 * (size_t)K * b->max_jobs));
     BATCH_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    cudaMemcpyAsync(b->tab_dev, b->tab_host, sizeof(BatchStep) * 2 * (size_t)K, cudaMemcpyHostToDevice, b->stream);
+    cudaMemcpyAsync(b->tab_dev, b->tab_host, sizeof(BatchStep) * kTables * (size_t)K, cudaMemcpyHostToDevice,
+                    b->stream);
     for (int s = 0; s < K; ++s) {
-        batch_step_kernel<1><<<b->grid[0], dim3(TT_Z, TT_Y), batch_smem_ns<1>(), b->stream>>>(b->tab_dev + 2 * s);
-        batch_step_kernel<2><<<b->grid[1], dim3(TT_Z, TT_Y), batch_smem_ns<2>(), b->stream>>>(b->tab_dev + 2 * s + 1);
-        batch_finalize_kernel<<<b->max_jobs, 1024, 0, b->stream>>>(b->tab_dev + 2 * s);
-        batch_finalize_kernel<<<b->max_jobs, 1024, 0, b->stream>>>(b->tab_dev + 2 * s + 1);
+        BatchStep* t = b->tab_dev + kTables * s;
+        batch_step_kernel<1, false><<<b->grid[0], dim3(TT_Z, TT_Y), batch_smem_ns<1, false>(), b->stream>>>(t);
+        batch_step_kernel<2, false><<<b->grid[1], dim3(TT_Z, TT_Y), batch_smem_ns<2, false>(), b->stream>>>(t + 1);
+        batch_step_kernel<1, true><<<b->grid[2], dim3(PT_TZ, PT_Y), batch_smem_ns<1, true>(), b->stream>>>(t + 2);
+        batch_step_kernel<2, true><<<b->grid[3], dim3(PT_TZ, PT_Y), batch_smem_ns<2, true>(), b->stream>>>(t + 3);
+        for (int q = 0; q < kTables; ++q) batch_finalize_kernel<<<b->max_jobs, 1024, 0, b->stream>>>(t + q);
     }
     cudaMemcpyAsync(b->diag_host, b->diag_dev, sizeof(double) * 2 * (size_t)K * b->max_jobs, cudaMemcpyDeviceToHost,
                     b->stream);
@@ -263,13 +284,18 @@ int lat_batch_create(int32_t max_jobs, lat_batch** out)
         set_error("lat_batch_create: no CUDA device or stream");
         return LAT_ERR_NODEVICE;
     }
-    int sms = 0, per_sm = 0;
+    int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_step_kernel<1>, TT_THREADS, batch_smem_ns<1>());
-    b->grid[0] = std::max(1, sms * std::max(1, per_sm));
-    per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_step_kernel<2>, TT_THREADS, batch_smem_ns<2>());
-    b->grid[1] = std::max(1, sms * std::max(1, per_sm));
+    auto grid_of = [&](auto kernel, size_t smem) {
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TT_THREADS, smem);
+        return std::max(1, sms * std::max(1, per_sm));
+    };
+    b->grid[0] = grid_of(batch_step_kernel<1, false>, batch_smem_ns<1, false>());
+    b->grid[1] = grid_of(batch_step_kernel<2, false>, batch_smem_ns<2, false>());
+    b->grid[2] = grid_of(batch_step_kernel<1, true>, batch_smem_ns<1, true>());
+    b->grid[3] = grid_of(batch_step_kernel<2, true>, batch_smem_ns<2, true>());
     *out = b;
     return LAT_OK;
 }
@@ -382,24 +408,36 @@ int lat_batch_advance(lat_batch* b, int32_t nsteps)
     }
     std::vector<std::vector<int>> diag_slots(b->jobs.size());
     for (int s = 0; s < K; ++s) {
-        b->tab_host[2 * s].njobs = b->tab_host[2 * s + 1].njobs = 0;
-        b->tab_host[2 * s].total_items = b->tab_host[2 * s + 1].total_items = 0;
+        for (int q = 0; q < kTables; ++q) {
+            b->tab_host[kTables * s + q].njobs = 0;
+            b->tab_host[kTables * s + q].total_items = 0;
+        }
         for (size_t q = 0; q < b->jobs.size(); ++q) {
             if (s >= plan[q].steps) continue;
             auto& j = b->jobs[q];
             lat_handle* h = j.h;
-            BatchStep& T = b->tab_host[2 * s + (h->p.model == LAT_MODEL_MOORE ? 1 : 0)];
             const int64_t n = plan[q].n0 + s;
             const int tNow = (int)((n + 1) % 2), tPast = (int)(n % 2);
+            Fields<float, 7> fj{};
+            for (int c = 0; c < h->ncomp; ++c) {
+                fj.now[c] = (const float*)h->slot(c, tNow);
+                fj.past[c] = (float*)h->slot(c, tPast);
+            }
+            Fields<float, 5> f5;
+            for (int c = 0; c < 5; ++c) {
+                f5.now[c] = fj.now[c];
+                f5.past[c] = fj.past[c];
+            }
+            // the pair tile where the lattice's own layout allows it: the choice
+            // depends on the lattice alone, never on its company
+            const bool moore = h->p.model == LAT_MODEL_MOORE;
+            const bool pair = moore ? pair_ok(h->geom, fj) : pair_ok(h->geom, f5);
+            BatchStep& T = b->tab_host[kTables * s + (pair ? 2 : 0) + (moore ? 1 : 0)];
             BatchJob& J = T.jobs[T.njobs];
             std::memset(&J, 0, sizeof(J));
             J.g = h->geom;
-            for (int c = 0; c < h->ncomp; ++c) {
-                J.f.now[c] = (const float*)h->slot(c, tNow);
-                J.f.past[c] = (float*)h->slot(c, tPast);
-            }
+            J.f = fj;
             const StepCoef c64 = make_coef(h->p, n);
-            J.c = coef_as<float>(c64);
             J.ns = h->p.model == LAT_MODEL_MOORE ? 2 : 1;
             if (J.ns == 1) {
                 J.ch.q[0] = 1;
@@ -427,7 +465,10 @@ int lat_batch_advance(lat_batch* b, int32_t nsteps)
             // results do not depend on the mix.
             J.chunk = b->chunk > 0 ? std::min(h->geom.hix - h->geom.lox, b->chunk) : batch_chunk(h->geom);
             J.vec = h->p.kernel_variant != 2 && tiled_vec_ok(h->geom, J.f) ? 1 : 0;
-            const dim3 tg = tiled_grid(h->geom, J.chunk);
+            J.pair = pair ? 1 : 0;
+            if (pair) J.pc = pair_coef(c64);
+            else J.c = coef_as<float>(c64);
+            const dim3 tg = pair ? pair_grid(h->geom, J.chunk) : tiled_grid(h->geom, J.chunk);
             J.tiles_z = (int)tg.x;
             J.tiles_y = (int)tg.y;
             J.items = (int)(tg.x * tg.y * tg.z);
@@ -441,7 +482,7 @@ int lat_batch_advance(lat_batch* b, int32_t nsteps)
     }
     BATCH_CK(cudaGraphLaunch(b->exec, b->stream));
     BATCH_CK(cudaStreamSynchronize(b->stream));
-    b->launches += 2 * (int64_t)K;
+    b->launches += kTables * (int64_t)K;
     int active = 0;
     for (size_t q = 0; q < b->jobs.size(); ++q) {
         auto& j = b->jobs[q];

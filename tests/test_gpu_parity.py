@@ -579,14 +579,15 @@ def test_fp32_tiled_vector_staging_is_bitwise_the_element_staging(lattice_mod, m
 
 
 @pytest.mark.parametrize("model", [0, 1])
-@pytest.mark.parametrize("sides,bc", [((40, 36, 64), 0), ((33, 17, 96), 0), ((24, 20, 4), 0), ((21, 19, 44), 1),
-                                      ((9, 11, 132), 1), ((70, 29, 8), 0)])
+@pytest.mark.parametrize("sides,bc", [((40, 36, 64), 0), ((33, 17, 128), 0), ((8, 7, 64), 1), ((21, 19, 580), 0),
+                                      ((9, 11, 600), 1), ((30, 29, 192), 0)])
 def test_fp32_pair_step_tracks_tiled_and_fp64(lattice_mod, model, sides, bc):
     """The pair step (two z-sites per thread in paired FP32 arithmetic; the
-    default where z is periodic and nz a multiple of 4) against the tiled
-    step (kernel_variant 3) and the FP64 path: 12 steps with energy/Gauss
-    every 4, periodic and fixed x/y walls, z extents that fill 64-wide tiles,
-    end in a partial tile, or are narrower than a tile.  The two FP32 steps
+    default where z is periodic, nz a multiple of 4 and its 64-wide z-tiles at
+    least 90 % full) against the tiled step (kernel_variant 3) and the FP64
+    path: 12 steps with energy/Gauss every 4, periodic and fixed x/y walls, z
+    extents that fill the tiles and that end in a partial tile (580: 4 sites,
+    600: 24), y extents narrower than a tile.  The two FP32 steps
     round differently (other contractions), so they agree to FP32 accuracy,
     not bitwise: fields L2 within 2e-6, max within 2e-5 of the FP64 path's,
     energies 1e-5 and Gauss sums 1e-4 relative."""
