@@ -89,10 +89,10 @@ __device__ __forceinline__ void run_item(unsigned char* smem_raw, const BatchJob
 // Persistent step kernel for the lattices with NS scalars that use the pair
 // tile (PAIR) or the tiled tile: CTAs stride over the work items of all of
 // them.  One kernel per model and tile keeps each kernel's register use to
-// that tile's: two CTAs per SM for the pair tile, as the pair step, four
-// (Abelian-Higgs) or three (Moore) for the tiled tile.
+// that tile's: four 4-warp CTAs per SM for the pair tile, as the pair step,
+// four (Abelian-Higgs) or three (Moore) 8-warp CTAs for the tiled tile.
 template <int NS, bool PAIR>
-__global__ void __launch_bounds__(TT_THREADS, PAIR ? 2 : (NS == 1 ? 4 : 3))
+__global__ void __launch_bounds__(PAIR ? PT_THREADS : TT_THREADS, PAIR ? 4 : (NS == 1 ? 4 : 3))
 batch_step_kernel(const BatchStep* __restrict__ tab)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -121,7 +121,8 @@ batch_step_kernel(const BatchStep* __restrict__ tab)
         {
             const int* src = reinterpret_cast<const int*>(&tab->jobs[s_job]);
             int* dst = reinterpret_cast<int*>(&sj);
-            for (int q = tid; q < (int)(sizeof(BatchJob) / sizeof(int)); q += TT_THREADS) dst[q] = src[q];
+            const int nthreads = (int)(blockDim.x * blockDim.y);
+            for (int q = tid; q < (int)(sizeof(BatchJob) / sizeof(int)); q += nthreads) dst[q] = src[q];
             if (tid < 5) {
                 sf5.now[tid] = tab->jobs[s_job].f.now[tid];
                 sf5.past[tid] = tab->jobs[s_job].f.past[tid];
@@ -286,16 +287,16 @@ int lat_batch_create(int32_t max_jobs, lat_batch** out)
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-    auto grid_of = [&](auto kernel, size_t smem) {
+    auto grid_of = [&](auto kernel, int threads, size_t smem) {
         if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TT_THREADS, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
         return std::max(1, sms * std::max(1, per_sm));
     };
-    b->grid[0] = grid_of(batch_step_kernel<1, false>, batch_smem_ns<1, false>());
-    b->grid[1] = grid_of(batch_step_kernel<2, false>, batch_smem_ns<2, false>());
-    b->grid[2] = grid_of(batch_step_kernel<1, true>, batch_smem_ns<1, true>());
-    b->grid[3] = grid_of(batch_step_kernel<2, true>, batch_smem_ns<2, true>());
+    b->grid[0] = grid_of(batch_step_kernel<1, false>, TT_THREADS, batch_smem_ns<1, false>());
+    b->grid[1] = grid_of(batch_step_kernel<2, false>, TT_THREADS, batch_smem_ns<2, false>());
+    b->grid[2] = grid_of(batch_step_kernel<1, true>, PT_THREADS, batch_smem_ns<1, true>());
+    b->grid[3] = grid_of(batch_step_kernel<2, true>, PT_THREADS, batch_smem_ns<2, true>());
     *out = b;
     return LAT_OK;
 }

@@ -13,14 +13,16 @@
 // friends): one instruction updates two sites.  A pair is also one 8-byte
 // shared-memory or global access, and its inner z-neighbours are in
 // registers.  The structure is otherwise the tiled step's:
-//   * a CTA owns a 64 (z) x 8 (y) tile and marches `chunk` x-planes;
+//   * a CTA (4 warps) owns a 64 (z) x 4 (y) tile and marches `chunk`
+//     x-planes; four CTAs share an SM, so while one waits at a barrier the
+//     others issue (8-row tiles of 8 warps, two per SM, ran 6 % slower);
 //   * each plane's now level, tile plus one-site halo, is staged in shared
 //     memory by 16-byte cp.async chunks, two planes ahead, in a 3-stage ring;
 //   * every site's link data (e^{i q theta} per direction and scalar, sines of
 //     the plaquettes P_xy, P_xz, P_yz) is evaluated once per step: own sites by
-//     their thread, the low y and z halo by warps 7 and 6 (warps 0-5 issue
-//     the staging copies; this balance measured 1-4 % faster than the halo
-//     on warps 0 and 1);
+//     their thread, the low y and z halo by the last two warps (with 8-row
+//     tiles, putting it on the warps that issue no staging copies measured
+//     1-4 % faster than on warps 0 and 1);
 //   * x-backward data, and the next plane's own values (read as x-forward
 //     neighbours), are carried in registers.
 // Used where the layout allows 16-byte chunks and aligned pairs: periodic z,
@@ -39,7 +41,7 @@ namespace lat {
 
 constexpr int PT_TZ = 32;              // threads along z (each two sites)
 constexpr int PT_Z = 2 * PT_TZ;        // tile width along z
-constexpr int PT_Y = 8;                // tile height along y (warps per CTA)
+constexpr int PT_Y = 4;                // tile height along y (warps per CTA)
 constexpr int PT_THREADS = PT_TZ * PT_Y;
 constexpr int PT_HY = PT_Y + 2;        // staged rows j0-1 .. j0+8
 constexpr int PT_PZ = 72;              // staged row pitch (floats): column c holds z = k0 - 4 + c
@@ -232,8 +234,8 @@ __device__ __forceinline__ void pair_tile(PairSmem<NS>& sm, const Geom& g, const
             sdst = hq * PT_PZ + 4 * q;
         }
     }
-    // halo tasks: warp 7 the low row (ly = 0) as pairs, warp 6's first 8 lanes the low column
-    // (z = k0-1); threads 0..179 (warps 0-5) issue the staging copies
+    // halo tasks: the last warp the low row (ly = 0) as pairs, the first PT_Y lanes of the
+    // warp before it the low column (z = k0-1); threads 0 .. PT_HY*PT_NQ-1 issue the staging copies
     const bool halo_row = ty == PT_Y - 1;
     const bool halo_col = ty == PT_Y - 2 && tz < PT_Y;
 
@@ -585,7 +587,7 @@ __device__ __forceinline__ void pair_tile(PairSmem<NS>& sm, const Geom& g, const
 }
 
 template <int NS, bool DIAG>
-__global__ void __launch_bounds__(PT_THREADS, 2)
+__global__ void __launch_bounds__(PT_THREADS, 4)
 pair_step_kernel(const Geom g, const Fields<float, 2 * NS + 3> f, const PairCoef c, const Charges<float> ch,
                  const DiagOut d, const int chunk)
 {
