@@ -333,8 +333,9 @@ struct LcArgs {
     int nx, ny, nz, x0, y0, z0;
     double dx, dy, dz, dt, g;
     LcBoost B[4];        // 1s, 1a, 2s, 2a
-    double sf[4][2];     // rest-frame positions
+    double sf[4][2];     // rest-frame positions (lab-frame ones in ic_func's form)
     Profile pr;
+    int older;           // ic_func.cpp's form: boosted one-forms keep only the boost term
 };
 
 // (a + i b)/d as std::complex builds it from `a + ci*b` and `/ d`
@@ -346,7 +347,8 @@ __device__ __forceinline__ void lc_unit(double a, double b, double d, double& re
 
 __device__ __forceinline__ double lc_sq(double x) { return x * x; }
 
-// initialConditions.cpp:1061-1330 (t = 0) and 1430-1690 (t = dt) for one site
+// initialConditions.cpp:1061-1330 (t = 0) and 1430-1690 (t = dt) for one site;
+// with q.older, ic_func.cpp:1006-1250 and 1365-1621
 __device__ int lc_site(const LcArgs& q, int t, int i, int j, int k, long long s, double* At, long long N,
                        double P0[4], double th[3])
 {
@@ -429,7 +431,11 @@ __device__ int lc_site(const LcArgs& q, int t, int i, int j, int k, long long s,
         const LcBoost& b = q.B[w];
         const double dotA = w < 2 ? b.v[1] * A[w][1] + b.v[2] * A[w][2] : b.v[0] * A[w][0] + b.v[1] * A[w][1];
 #pragma unroll
-        for (int cc = 0; cc < 3; ++cc) Ap[w][cc] = b.vsq == 0 ? A[w][cc] : A[w][cc] + (b.gamma - 1) * dotA * b.v[cc] / b.vsq;
+        for (int cc = 0; cc < 3; ++cc) {
+            const double boost = (b.gamma - 1) * dotA * b.v[cc] / b.vsq;
+            // ic_func.cpp:1195-1196, 1229-1230: the boost term alone (|v| > 0 there)
+            Ap[w][cc] = q.older ? boost : (b.vsq == 0 ? A[w][cc] : A[w][cc] + boost);
+        }
         if (!t) At[w * N + s] = -b.gamma * dotA;
     }
     if (t) {
@@ -572,27 +578,33 @@ void lc_boost_init(LcBoost& b, const double v[3])
 
 }  // namespace lat
 
-extern "C" int lat_loop_collision_ic_device(lat_handle* h, const lat_string_profile* prof,
-                                            const lat_loop_collision_ic* c, int64_t* off_table)
+namespace lat {
+namespace {
+
+// Both loop-collision forms; `older` selects ic_func.cpp's.
+int loop_collision_device(const char* who, lat_handle* h, const lat_string_profile* prof,
+                          const lat_loop_collision_ic* c, int64_t* off_table, bool older)
 {
+    const std::string name(who);
     if (!h || !prof || !c || !prof->phi || !prof->A) {
-        set_error("lat_loop_collision_ic_device: null argument");
+        set_error(name + ": null argument");
         return LAT_ERR_INVALID;
     }
     const lat_params& p = h->p;
     if (p.model != LAT_MODEL_AH) {
-        set_error("lat_loop_collision_ic_device: Abelian-Higgs handles only");
+        set_error(name + ": Abelian-Higgs handles only");
         return LAT_ERR_INVALID;
     }
     if (p.nx < 3 || p.ny < 3 || p.nz < 3) {
-        set_error("lat_loop_collision_ic_device: every side must be at least 3");
+        set_error(name + ": every side must be at least 3");
         return LAT_ERR_INVALID;
     }
     if (prof->m < 2 || !(prof->h > 0)) {
-        set_error("lat_loop_collision_ic_device: the profile needs m >= 2 points and h > 0");
+        set_error(name + ": the profile needs m >= 2 points and h > 0");
         return LAT_ERR_INVALID;
     }
     LcArgs q;
+    q.older = older ? 1 : 0;
     q.nx = (int)p.nx;
     q.ny = (int)p.ny;
     q.nz = (int)p.nz;
@@ -609,13 +621,19 @@ extern "C" int lat_loop_collision_ic_device(lat_handle* h, const lat_string_prof
     for (int w = 0; w < 4; ++w) {
         lc_boost_init(q.B[w], vel[w]);
         if (!(q.B[w].vsq < 1)) {
-            set_error("lat_loop_collision_ic_device: every |v| must be below 1");
+            set_error(name + ": every |v| must be below 1");
+            return LAT_ERR_INVALID;
+        }
+        if (older && !(q.B[w].vsq > 0)) {
+            // ic_func.cpp divides by |v|^2 with no branch for a string at rest
+            set_error(name + ": every string must move (0 < |v| < 1)");
             return LAT_ERR_INVALID;
         }
         // rest-frame positions (initialConditions.cpp:1030-1046), on the host with
-        // the reference's operations
+        // the reference's operations; ic_func's form measures from the given
+        // lab-frame positions (ic_func.cpp:1034-1037)
         const LcBoost& b = q.B[w];
-        if (b.vsq == 0) {
+        if (b.vsq == 0 || older) {
             q.sf[w][0] = pos[w][0];
             q.sf[w][1] = pos[w][1];
         } else {
@@ -636,7 +654,7 @@ extern "C" int lat_loop_collision_ic_device(lat_handle* h, const lat_string_prof
     char* scratch = nullptr;
     if (e == cudaSuccess) e = cudaMallocAsync((void**)&scratch, need, h->stream);
     if (e != cudaSuccess) {
-        set_error(std::string("lat_loop_collision_ic_device: ") + cudaGetErrorString(e));
+        set_error(name + ": " + cudaGetErrorString(e));
         return e == cudaErrorMemoryAllocation ? LAT_ERR_NOMEM : LAT_ERR_CUDA;
     }
     double* S0 = (double*)scratch;
@@ -657,7 +675,7 @@ extern "C" int lat_loop_collision_ic_device(lat_handle* h, const lat_string_prof
     if (e == cudaSuccess) e = ef;
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) {
-        set_error(std::string("lat_loop_collision_ic_device: ") + cudaGetErrorString(e));
+        set_error(name + ": " + cudaGetErrorString(e));
         return LAT_ERR_CUDA;
     }
     h->n = 0;
@@ -666,6 +684,21 @@ extern "C" int lat_loop_collision_ic_device(lat_handle* h, const lat_string_prof
     h->launches += 6;
     if (off_table) *off_table = (int64_t)off_host;
     return LAT_OK;
+}
+
+}  // namespace
+}  // namespace lat
+
+extern "C" int lat_loop_collision_ic_device(lat_handle* h, const lat_string_profile* prof,
+                                            const lat_loop_collision_ic* c, int64_t* off_table)
+{
+    return lat::loop_collision_device("lat_loop_collision_ic_device", h, prof, c, off_table, false);
+}
+
+extern "C" int lat_icfunc_loop_collision_ic_device(lat_handle* h, const lat_string_profile* prof,
+                                                   const lat_loop_collision_ic* c, int64_t* off_table)
+{
+    return lat::loop_collision_device("lat_icfunc_loop_collision_ic_device", h, prof, c, off_table, true);
 }
 
 // ---------------------------------------------------------------------------

@@ -176,12 +176,14 @@ Params::Params(Program prog)
         v["stringPos"] = "false";
         v["stringDetect"] = "true";
         v["splitLength"] = "true";
-        // ic_func.cpp: "random" and "boost" are built in-process here; its
-        // default, "loop collision", is an older variant of
-        // initialConditions.cpp's, whose Data/ic.txt "data" reads
-        v["ic_type"] = "random";
+        // ic_func.cpp:25 ships with "loop collision" (its older form,
+        // :966-1720); "random" and "boost" are its other in-process types,
+        // and "data" reads two levels of Data/<ic_file>
+        v["ic_type"] = "loop collision";
         v["seed"] = "1";
-        v["sor_file"] = "SOR_Fields.txt";   // ic_func.cpp:38-39,692 (next to the program)
+        // the profile table: Data/SOR_Fields.txt for "loop collision"
+        // (ic_func.cpp:978), SOR_Fields.txt next to the program for "boost" (:692)
+        v["sor_file"] = "";
         v["SORnx"] = "30001";
         v["SORa"] = "0.01";
         v["n"] = "1";
@@ -726,7 +728,7 @@ void icfunc_random(const Run& r, double seed, std::vector<double>& now)
     }
 }
 
-enum class StringIc { Boost, LoopCollision };
+enum class StringIc { Boost, LoopCollision, IcfuncLoopCollision };
 void string_ic_table(Params& q, const std::string& dir, StringIc kind, int form, std::vector<double>& tab);
 
 int run_icw(Run& r)
@@ -754,10 +756,19 @@ int run_icw(Run& r)
             std::copy(tab.begin() + (size_t)c * 2 * r.N, tab.begin() + (size_t)c * 2 * r.N + r.N, past.begin() + (size_t)c * r.N);
             std::copy(tab.begin() + (size_t)c * 2 * r.N + r.N, tab.begin() + (size_t)(c + 1) * 2 * r.N, now.begin() + (size_t)c * r.N);
         }
+    } else if (ic_type == "loop collision") {
+        std::vector<double> tab;
+        string_ic_table(q, q.str("out_dir"), StringIc::IcfuncLoopCollision, LAT_IC_FORM_INPROCESS, tab);
+        past.assign((size_t)5 * r.N, 0.0);
+        now.assign((size_t)5 * r.N, 0.0);
+        for (int c = 0; c < 5; ++c) {
+            std::copy(tab.begin() + (size_t)c * 2 * r.N, tab.begin() + (size_t)c * 2 * r.N + r.N, past.begin() + (size_t)c * r.N);
+            std::copy(tab.begin() + (size_t)c * 2 * r.N + r.N, tab.begin() + (size_t)(c + 1) * 2 * r.N, now.begin() + (size_t)c * r.N);
+        }
     } else if (ic_type == "data") {
         r.read_ic(r.data(q.str("ic_file")), 5, 2, past, now);
     } else {
-        fail("ic_type: this program provides ic_func.cpp's \"random\" and \"boost\", and \"data\"");
+        fail("ic_type: this program provides ic_func.cpp's \"loop collision\", \"random\" and \"boost\", and \"data\"");
     }
     check(lat_create(&r.p, &r.h), "lat_create");
     check(lat_set_state(r.h, now.data(), past.data(), 0), "lat_set_state");
@@ -856,12 +867,18 @@ void string_ic_table(Params& q, const std::string& dir, StringIc kind, int form,
         b.reserved = 0;
         rc = lat_boost_ic_device(h, &sp, &b, &off);
     } else {
-        // initialConditions.cpp:72-84
         const double Ly = (double)(p.ny - 1), Lz = (double)(p.nz - 1), Lx = (double)(p.nx - 1);
-        const std::vector<std::pair<const char*, std::vector<double>>> def = {
-            {"pos1s", {0.15 * Ly * p.dy, -0.25 * Lz * p.dz}}, {"pos1a", {-0.15 * Ly * p.dy, 0.25 * Lz * p.dz}},
-            {"pos2s", {0.25 * Lx * p.dx, 0}},                {"pos2a", {-0.25 * Lx * p.dx, 0}},
-            {"v1s", {0, -0.75, 0}}, {"v1a", {0, 0.75, 0}}, {"v2s", {0, 0, 0}}, {"v2a", {0, 0, 0}}};
+        const double a = 0.6 * 0.4, b = 0.6 * std::sqrt(1 - std::pow(0.4, 2));
+        const std::vector<std::pair<const char*, std::vector<double>>> def =
+            kind == StringIc::LoopCollision
+                ? std::vector<std::pair<const char*, std::vector<double>>>{   // initialConditions.cpp:72-84
+                      {"pos1s", {0.15 * Ly * p.dy, -0.25 * Lz * p.dz}}, {"pos1a", {-0.15 * Ly * p.dy, 0.25 * Lz * p.dz}},
+                      {"pos2s", {0.25 * Lx * p.dx, 0}},                {"pos2a", {-0.25 * Lx * p.dx, 0}},
+                      {"v1s", {0, -0.75, 0}}, {"v1a", {0, 0.75, 0}}, {"v2s", {0, 0, 0}}, {"v2a", {0, 0, 0}}}
+                : std::vector<std::pair<const char*, std::vector<double>>>{   // ic_func.cpp:61-72
+                      {"pos1s", {2, -0.25 * Lz * p.dz}}, {"pos1a", {-2, 0.25 * Lz * p.dz}},
+                      {"pos2s", {0.25 * Lx * p.dx, -1}}, {"pos2a", {-0.25 * Lx * p.dx, 1}},
+                      {"v1s", {0, -b, -a}}, {"v1a", {0, b, a}}, {"v2s", {a, b, 0}}, {"v2a", {-a, -b, 0}}};
         lat_loop_collision_ic c;
         double* dst[8] = {c.pos1s, c.pos1a, c.pos2s, c.pos2a, c.v1s, c.v1a, c.v2s, c.v2a};
         for (int w = 0; w < 8; ++w) {
@@ -869,11 +886,14 @@ void string_ic_table(Params& q, const std::string& dir, StringIc kind, int form,
             const std::vector<double> v = txt.empty() ? def[w].second : numbers(def[w].first, txt, def[w].second.size());
             for (size_t e = 0; e < v.size(); ++e) dst[w][e] = v[e];
         }
-        rc = lat_loop_collision_ic_device(h, &sp, &c, &off);
+        rc = kind == StringIc::LoopCollision ? lat_loop_collision_ic_device(h, &sp, &c, &off)
+                                             : lat_icfunc_loop_collision_ic_device(h, &sp, &c, &off);
     }
     if (rc != LAT_OK) {
         lat_destroy(h);
-        check(rc, kind == StringIc::Boost ? "lat_boost_ic_device" : "lat_loop_collision_ic_device");
+        check(rc, kind == StringIc::Boost           ? "lat_boost_ic_device"
+                  : kind == StringIc::LoopCollision ? "lat_loop_collision_ic_device"
+                                                    : "lat_icfunc_loop_collision_ic_device");
     }
     const int64_t N = p.nx * p.ny * p.nz;
     std::vector<double> now((size_t)5 * N), past((size_t)5 * N);

@@ -33,6 +33,7 @@ EXPORTS = [
     "lat_batch_create", "lat_batch_destroy", "lat_batch_add", "lat_batch_remove", "lat_batch_size",
     "lat_batch_kernel_launches", "lat_batch_set_chunk", "lat_batch_advance", "lat_batch_take_diags",
     "lat_random_phase_ic_device", "lat_boost_ic_device", "lat_loop_collision_ic_device",
+    "lat_icfunc_loop_collision_ic_device",
     "lat_ng_sine_ic_device", "lat_simple_sine_ic_device", "lat_philox4x32_10", "lat_dtrig_eval", "lat_autotune", "lat_get_tuning", "lat_set_tuning",
     "lat_tune_cache_save", "lat_tune_cache_load", "lat_footprint_bytes",
     "lat_server_create", "lat_server_submit", "lat_server_poll", "lat_server_wait", "lat_server_diags",
@@ -121,6 +122,7 @@ def load_library(path: Path | None = None):
     L.lat_random_phase_ic_device.argtypes = [vp, ctypes.c_uint64, ctypes.c_int32]
     L.lat_boost_ic_device.argtypes = [vp, vp, vp, P(ctypes.c_int64)]
     L.lat_loop_collision_ic_device.argtypes = [vp, vp, vp, P(ctypes.c_int64)]
+    L.lat_icfunc_loop_collision_ic_device.argtypes = [vp, vp, vp, P(ctypes.c_int64)]
     L.lat_ng_sine_ic_device.argtypes = [vp, vp, ctypes.c_double, P(ctypes.c_int64)]
     L.lat_simple_sine_ic_device.argtypes = [vp, vp, ctypes.c_double, P(ctypes.c_int64)]
     L.lat_philox4x32_10.argtypes = [u32p, u32p, u32p]
@@ -260,21 +262,27 @@ class Lattice:
         del keep
         return int(off.value)
 
-    def loop_collision_ic_device(self, phi, A, h: float, geometry: dict | None = None, winding: float = 1.0) -> int:
-        """Loop-collision IC (initialConditions.cpp:994-1716) from the profile
-        table (phi, A) with spacing h, built on the GPU; state at TimeStep 0.
-        `geometry` (pos1s, pos1a, pos2s, pos2a, v1s, v1a, v2s, v2a) defaults to
-        the reference's placement for this lattice.  Returns the number of
-        site evaluations beyond the table."""
-        from .params import default_loop_collision, loop_collision_ic, string_profile
+    def loop_collision_ic_device(self, phi, A, h: float, geometry: dict | None = None, winding: float = 1.0,
+                                 form: str = "initialConditions") -> int:
+        """Loop-collision IC from the profile table (phi, A) with spacing h,
+        built on the GPU; state at TimeStep 0.  form "initialConditions":
+        initialConditions.cpp:994-1716, `geometry` (pos1s, pos1a, pos2s, pos2a,
+        v1s, v1a, v2s, v2a) defaulting to its placement for this lattice; form
+        "ic_func": the older ic_func.cpp:966-1720 that ic_w_evolution builds,
+        defaulting to ic_func.cpp:61-72.  Returns the number of site
+        evaluations beyond the table."""
+        from .params import default_loop_collision, icfunc_loop_collision, loop_collision_ic, string_profile
+        if form not in ("initialConditions", "ic_func"):
+            raise ValueError("form must be initialConditions or ic_func")
         p = self.params
-        geo = default_loop_collision(p.nx, p.ny, p.nz, p.dx, p.dy, p.dz)
+        geo = (default_loop_collision if form == "initialConditions" else icfunc_loop_collision)(
+            p.nx, p.ny, p.nz, p.dx, p.dy, p.dz)
         geo.update(geometry or {})
         prof, keep = string_profile(phi, A, h, winding)
         c = loop_collision_ic(**geo)
         off = ctypes.c_int64(0)
-        _check("lat_loop_collision_ic_device",
-               self.L.lat_loop_collision_ic_device(self.h, ctypes.byref(prof), ctypes.byref(c), ctypes.byref(off)))
+        name = "lat_loop_collision_ic_device" if form == "initialConditions" else "lat_icfunc_loop_collision_ic_device"
+        _check(name, getattr(self.L, name)(self.h, ctypes.byref(prof), ctypes.byref(c), ctypes.byref(off)))
         del keep
         return int(off.value)
 

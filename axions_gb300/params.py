@@ -213,6 +213,16 @@ def loop_collision_ic(**geo) -> LatLoopCollisionIC:
     return c
 
 
+def icfunc_loop_collision(nx: int, ny: int, nz: int, dx: float, dy: float, dz: float) -> dict:
+    """ic_func.cpp:61-72: pair 1 (x-directed) at y = +-2, z = -+0.25 L_z and pair
+    2 (z-directed) at x = +-0.25 L_x, y = -+1, every string moving at 0.6 with
+    the directions of the reference's constants."""
+    a, b = 0.6 * 0.4, 0.6 * math.sqrt(1 - 0.4 ** 2)
+    return dict(pos1s=[2.0, -0.25 * (nz - 1) * dz], pos1a=[-2.0, 0.25 * (nz - 1) * dz],
+                pos2s=[0.25 * (nx - 1) * dx, -1.0], pos2a=[-0.25 * (nx - 1) * dx, 1.0],
+                v1s=[0.0, -b, -a], v1a=[0.0, b, a], v2s=[a, b, 0.0], v2a=[-a, -b, 0.0])
+
+
 def default_loop_collision(nx: int, ny: int, nz: int, dx: float, dy: float, dz: float) -> dict:
     """initialConditions.cpp:72-84: pair 1 at y = +-0.15 L_y, z = -+0.25 L_z moving
     along y at -+0.75; pair 2 at x = +-0.25 L_x at rest."""

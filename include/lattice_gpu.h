@@ -387,6 +387,21 @@ typedef struct lat_loop_collision_ic {
 
 int lat_loop_collision_ic_device(lat_handle* h, const lat_string_profile* prof, const lat_loop_collision_ic* c,
                                  int64_t* off_table);
+/* The older loop collision of ic_func.cpp:966-1720, which ic_w_evolution
+ * builds in process (ic_func.cpp:25 ships with ic_type "loop collision";
+ * positions and velocities of ic_func.cpp:61-72).  The same steps and outputs
+ * as lat_loop_collision_ic_device, except that:
+ *   - each string's distance is measured from the given position as it stands
+ *     (initialConditions.cpp first maps it to the string's rest frame);
+ *   - each string's boosted one-form keeps only the boost term
+ *     (gamma-1)(v.A)v/|v|^2 (ic_func.cpp:1195-1196, 1229-1230, 1539-1542);
+ *   - every string must move: 0 < |v| < 1 (the form divides by |v|^2).
+ * ic_func.cpp declares A1s with two elements and stores its z component in
+ * A1s[2] (:973, :1100); here that component is a third element, which is what
+ * the reference's own build computes (its ic_w_evolution output after three
+ * steps matches bit for bit).  Abelian-Higgs handles only; sides >= 3. */
+int lat_icfunc_loop_collision_ic_device(lat_handle* h, const lat_string_profile* prof,
+                                        const lat_loop_collision_ic* c, int64_t* off_table);
 /* Straight strings perturbed by a sine wave of amplitude eps in [0, 1) (the
  * value the reference reads from standard input), built on the device from
  * the profile table into both slots of an Abelian-Higgs handle (one level, as

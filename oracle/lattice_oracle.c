@@ -1317,10 +1317,12 @@ static void lc_unit(double a, double b, double d, double* re, double* im)
 }
 
 /* the per-site work of one level (initialConditions.cpp:1061-1330 at t = 0,
- * 1430-1690 at t = dt); At is written at t = 0 and read at t = dt */
+ * 1430-1690 at t = dt); At is written at t = 0 and read at t = dt.  older:
+ * ic_func.cpp's form (:1006-1250 at t = 0, :1365-1621 at t = dt), whose boosted
+ * one-forms keep only the boost term (:1195-1196, :1229-1230, :1539-1542) */
 static int lc_site(const lat_params* p, const lat_string_profile* prof, const lat_loop_collision_ic* c,
                    const lc_boost B[4], const double sf[4][2], int t, int i, int j, int k, double* At[4],
-                   double P0[4], double th[3])
+                   double P0[4], double th[3], int older)
 {
     const int nx = p->nx, ny = p->ny, nz = p->nz;
     const int x0 = (nx - 1) / 2, y0 = (ny - 1) / 2, z0 = (nz - 1) / 2;
@@ -1407,7 +1409,13 @@ static int lc_site(const lat_params* p, const lat_string_profile* prof, const la
     /* Lorentz transformation of the one-forms (pair 1 dots v with A's y, z;
      * pair 2 with A's x, y) */
     double Ap[4][3];
-    for (int cc = 0; cc < 3; ++cc) {
+    for (int cc = 0; cc < 3 && older; ++cc) {
+        Ap[0][cc] = (b1s->gamma - 1) * (b1s->v[1] * A[0][1] + b1s->v[2] * A[0][2]) * b1s->v[cc] / b1s->vsq;
+        Ap[1][cc] = (b1a->gamma - 1) * (b1a->v[1] * A[1][1] + b1a->v[2] * A[1][2]) * b1a->v[cc] / b1a->vsq;
+        Ap[2][cc] = (b2s->gamma - 1) * (b2s->v[0] * A[2][0] + b2s->v[1] * A[2][1]) * b2s->v[cc] / b2s->vsq;
+        Ap[3][cc] = (b2a->gamma - 1) * (b2a->v[0] * A[3][0] + b2a->v[1] * A[3][1]) * b2a->v[cc] / b2a->vsq;
+    }
+    for (int cc = 0; cc < 3 && !older; ++cc) {
         Ap[0][cc] = b1s->vsq == 0 ? A[0][cc]
                                   : A[0][cc] + (b1s->gamma - 1) * (b1s->v[1] * A[0][1] + b1s->v[2] * A[0][2]) * b1s->v[cc] / b1s->vsq;
         Ap[1][cc] = b1a->vsq == 0 ? A[1][cc]
@@ -1467,8 +1475,8 @@ static double lc_mag(const double* re, const double* im, int64_t s)
     return sqrt(pow(re[s], 2) + pow(im[s], 2));
 }
 
-int64_t orc_loop_collision_ic(const lat_params* p, const lat_string_profile* prof, const lat_loop_collision_ic* c,
-                              double* st)
+static int64_t lc_build(const lat_params* p, const lat_string_profile* prof, const lat_loop_collision_ic* c,
+                        double* st, int older)
 {
     const int nx = p->nx, ny = p->ny, nz = p->nz;
     if (nx < 3 || ny < 3 || nz < 3 || !prof || prof->m < 2 || !(prof->h > 0) || !c) return -1;
@@ -1478,13 +1486,14 @@ int64_t orc_loop_collision_ic(const lat_params* p, const lat_string_profile* pro
     lc_boost_init(&B[2], c->v2s);
     lc_boost_init(&B[3], c->v2a);
     for (int q = 0; q < 4; ++q)
-        if (!(B[q].vsq < 1)) return -1;
-    /* positions in each string's rest frame (:1030-1046) */
+        if (!(B[q].vsq < 1) || (older && !(B[q].vsq > 0))) return -1;
+    /* positions in each string's rest frame (:1030-1046); ic_func's form
+     * measures from the lab-frame positions (ic_func.cpp:1034-1037) */
     double sf[4][2];
     const double* pos[4] = {c->pos1s, c->pos1a, c->pos2s, c->pos2a};
     for (int q = 0; q < 4; ++q) {
         const lc_boost* b = &B[q];
-        if (b->vsq == 0) { sf[q][0] = pos[q][0]; sf[q][1] = pos[q][1]; continue; }
+        if (b->vsq == 0 || older) { sf[q][0] = pos[q][0]; sf[q][1] = pos[q][1]; continue; }
         const int i0 = q < 2 ? 1 : 0;   /* pair 1: (y, z) use v[1], v[2]; pair 2: (x, y) use v[0], v[1] */
         const double dot = b->v[i0] * pos[q][0] + b->v[i0 + 1] * pos[q][1];
         sf[q][0] = pos[q][0] + (b->gamma - 1) * dot * b->v[i0] / b->vsq;
@@ -1506,7 +1515,7 @@ int64_t orc_loop_collision_ic(const lat_params* p, const lat_string_profile* pro
             for (int j = 0; j < ny; ++j)
                 for (int k = 0; k < nz; ++k) {
                     double v4[4], th[3];
-                    off += lc_site(p, prof, c, B, sf, t, i, j, k, At, v4, th);
+                    off += lc_site(p, prof, c, B, sf, t, i, j, k, At, v4, th, older);
                     const int64_t s = IX(i, j, k);
                     for (int q = 0; q < 4; ++q) P0[q][s] = v4[q];
                     LST(2, t)[s] = th[0];
@@ -1549,6 +1558,23 @@ int64_t orc_loop_collision_ic(const lat_params* p, const lat_string_profile* pro
 #undef IX
     free(buf);
     return off;
+}
+
+int64_t orc_loop_collision_ic(const lat_params* p, const lat_string_profile* prof, const lat_loop_collision_ic* c,
+                              double* st)
+{
+    return lc_build(p, prof, c, st, 0);
+}
+
+/* ic_func.cpp:966-1720, the "loop collision" that ic_w_evolution builds in
+ * process (ic_func.cpp:25): the same steps as initialConditions.cpp's except
+ * that the strings sit at the given lab-frame positions, the boosted one-forms
+ * keep only the boost term, and every velocity must be non-zero (the form
+ * divides by |v|^2 with no v = 0 branch) */
+int64_t orc_icfunc_loop_collision_ic(const lat_params* p, const lat_string_profile* prof,
+                                     const lat_loop_collision_ic* c, double* st)
+{
+    return lc_build(p, prof, c, st, 1);
 }
 
 /* ---------------------------------------------------------------------------

@@ -76,6 +76,8 @@ int64_t orc_boost_ic(const lat_params* p, const lat_string_profile* prof, const 
  * profile table, or -1 for bad arguments. */
 int64_t orc_loop_collision_ic(const lat_params* p, const lat_string_profile* prof, const lat_loop_collision_ic* c,
                               double* st);
+int64_t orc_icfunc_loop_collision_ic(const lat_params* p, const lat_string_profile* prof,
+                                     const lat_loop_collision_ic* c, double* st);
 
 /* Perturbed straight strings of initialConditions.cpp into both slots of a
  * full AH state: "NG sine" (:113-486, a Nambu-Goto sine wave: per (x, z)

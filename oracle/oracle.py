@@ -57,8 +57,9 @@ def lib():
         L.orc_icfunc_random_ic.argtypes = [P(LatParams), ctypes.c_uint32, dp]
         L.orc_boost_ic.argtypes = [P(LatParams), ctypes.c_void_p, ctypes.c_void_p, dp]
         L.orc_boost_ic.restype = ctypes.c_int64
-        L.orc_loop_collision_ic.argtypes = [P(LatParams), ctypes.c_void_p, ctypes.c_void_p, dp]
-        L.orc_loop_collision_ic.restype = ctypes.c_int64
+        for name in ("orc_loop_collision_ic", "orc_icfunc_loop_collision_ic"):
+            getattr(L, name).argtypes = [P(LatParams), ctypes.c_void_p, ctypes.c_void_p, dp]
+            getattr(L, name).restype = ctypes.c_int64
         L.orc_string_length.argtypes = [P(LatParams), dp, ctypes.c_int64, ctypes.c_int, dp, dp]
         for name in ("orc_ng_sine_ic", "orc_simple_sine_ic"):
             getattr(L, name).argtypes = [P(LatParams), ctypes.c_void_p, ctypes.c_double, dp]
@@ -183,18 +184,23 @@ def boost_ic(p: LatParams, phi: np.ndarray, A: np.ndarray, h: float, v, form: in
     return st, int(off)
 
 
-def loop_collision_ic(p: LatParams, phi: np.ndarray, A: np.ndarray, h: float, geometry: dict, winding: float = 1.0):
-    """Loop-collision IC (initialConditions.cpp:994-1716).  `geometry` holds
-    pos1s, pos1a, pos2s, pos2a, v1s, v1a, v2s, v2a.  Returns (state, number of
-    evaluations off the table)."""
+def loop_collision_ic(p: LatParams, phi: np.ndarray, A: np.ndarray, h: float, geometry: dict, winding: float = 1.0,
+                      form: str = "initialConditions"):
+    """Loop-collision IC: initialConditions.cpp:994-1716, or with form="ic_func"
+    ic_func.cpp:966-1720 (the form ic_w_evolution builds in process).
+    `geometry` holds pos1s, pos1a, pos2s, pos2a, v1s, v1a, v2s, v2a.  Returns
+    (state, number of evaluations off the table)."""
     from axions_gb300.params import loop_collision_ic as _c, string_profile
+    if form not in ("initialConditions", "ic_func"):
+        raise ValueError("form must be initialConditions or ic_func")
     prof, keep = string_profile(phi, A, h, winding)
     c = _c(**geometry)
     st = empty_state(p)
-    off = lib().orc_loop_collision_ic(ctypes.byref(p), ctypes.byref(prof), ctypes.byref(c), _dp(st))
+    fn = lib().orc_loop_collision_ic if form == "initialConditions" else lib().orc_icfunc_loop_collision_ic
+    off = fn(ctypes.byref(p), ctypes.byref(prof), ctypes.byref(c), _dp(st))
     del keep
     if off < 0:
-        raise RuntimeError("orc_loop_collision_ic: bad arguments")
+        raise RuntimeError("loop collision IC: bad arguments")
     return st, int(off)
 
 

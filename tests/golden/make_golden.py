@@ -300,6 +300,35 @@ def gen_loop_collision_ic(name, nx, ny, nz, g, dt, profile, sor_h, dz=0.5, geome
     print(name, ic.shape)
 
 
+def gen_icfunc_loop_collision(name, nx, ny, nz, nt, g, d=0.35, dt=0.05, sor_h=0.01, profile=None):
+    """ic_w_evolution with ic_func's shipped ic_type, "loop collision"
+    (ic_func.cpp:25, 966-1720), built in process from the profile table at
+    dir_path/Data/SOR_Fields.txt (ic_func's own dir_path), then nt steps of
+    periodic evolution.  ic_w_evolution writes no IC, so the fixture holds what
+    it does write: valsPerLoop (energy, Gauss deviation, L0, L1 per step) and
+    finalField (both fields of the newest level after nt steps)."""
+    if profile is None:
+        profile = np.load(OUT / "ref_sor_gauge.npz")["profile"]
+    m = profile.shape[1]
+    consts = {"nx": nx, "ny": ny, "nz": nz, "nt": nt, "dx": d, "dy": d, "dz": d, "dt": float(dt), "g": float(g),
+              "makeGif": False}
+    build_ref.build("ic_w_evolution", name, consts,
+                    {"ic_func.cpp": {"ic_type": "loop collision", "SORnx": m, "SORa": float(sor_h)}})
+    work = build_ref.SCRATCH / name
+    lines = [f"{float(profile[0, r])!r} {float(profile[1, r])!r}" for r in range(m)]
+    (work / "Data" / "SOR_Fields.txt").write_text("\n".join(lines) + "\n")
+    work = build_ref.run(name)
+    vals = build_ref.read_columns(work / "Data" / "valsPerLoop_test.txt").reshape(nt, 4)
+    N = nx * ny * nz
+    final = build_ref.read_columns(work / "Data" / "finalField.txt").reshape(N, 5).T.copy()
+    p = make_params(MODEL_AH, nx=nx, ny=ny, nz=nz, d=d, dt=dt, lam=1.0, eta=1.0, g=g, damped_nt=0,
+                    dampFac=0.0, alpha=0.0, scaling=1.0, tau0=1.0, bc=BC_PERIODIC)
+    np.savez_compressed(OUT / f"{name}.npz", program="ic_w_evolution", ic_type="loop collision",
+                        params=_params_json(p), nt=nt, sor_h=sor_h, profile=profile, energy=vals[:, 0],
+                        deviation=vals[:, 1], L0=vals[:, 2], L1=vals[:, 3], final=final)
+    print(name, "vals", vals.shape)
+
+
 def gen_sine_ic(name, kind, nx, ny, nz, g, eps, profile, sor_h, dz=0.5):
     """initialConditions.cpp, ic_type "NG sine" or "simple sine" (a straight
     string perturbed by a sine wave of amplitude eps, which the program reads
@@ -377,6 +406,8 @@ def main():
                           geometry=dict(pos1s=[1.1, -0.9], pos1a=[-0.8, 1.3], pos2s=[1.4, 0.2], pos2a=[-1.2, -0.3],
                                         v1s=[0.1, -0.5, 0.3], v1a=[0.0, 0.6, -0.2], v2s=[0.3, 0.2, 0.0],
                                         v2a=[-0.25, -0.3, 0.1]))
+    # ic_w_evolution's own IC, ic_func's older loop collision (no rest-frame positions, boost-only one-forms)
+    gen_icfunc_loop_collision("ref_icfunc_loop_collision", 21, 19, 23, 3, g=0.8, profile=prof)
 
 
 if __name__ == "__main__":

@@ -129,7 +129,7 @@ def test_icw_program_reproduces_reference_output(tmp_path, name):
     bc = "periodic" if p.bc == 0 else "fixed"
     args = {"nx": p.nx, "ny": p.ny, "nz": p.nz, "nt": nt, "dx": p.dx, "dy": p.dy, "dz": p.dz, "dt": p.dt,
             "xyBC": bc, "zBC": bc, "seed": int(z["seed"]), "splitLength": "true" if split else "false",
-            "makeGif": "false"}
+            "makeGif": "false", "ic_type": "random"}
     r = _run("ic_w_evolution", tmp_path, args)
     assert r.returncode == 0, r.stderr.decode()
     vals = _cols(tmp_path / "Data" / "valsPerLoop_test.txt").reshape(nt, 4 if split else 3)
@@ -141,6 +141,35 @@ def test_icw_program_reproduces_reference_output(tmp_path, name):
     assert np.array_equal(final[:2], z["final_phi"])
 
 
+@pytest.mark.gpu
+def test_icw_program_loop_collision_reproduces_reference_output(tmp_path):
+    """bin/ic_w_evolution with no ic_type builds what the reference's does,
+    ic_func.cpp's "loop collision" (:25, :966-1720, read from
+    Data/SOR_Fields.txt), then evolves: against the reference's run, energy per
+    step to 1e-12, L0 and L1 per step to 1e-9, and the last level's fields to
+    1e-12 of each component's largest value (g != 0: the step's sines are this
+    library's, not libm's)."""
+    z = load_golden("ref_icfunc_loop_collision")
+    p = params_from_json(z["params"])
+    nt = int(z["nt"])
+    prof = z["profile"]
+    (tmp_path / "Data").mkdir()
+    (tmp_path / "Data" / "SOR_Fields.txt").write_text(
+        "".join(f"{float(a)!r} {float(b)!r}\n" for a, b in zip(prof[0], prof[1])))
+    args = {"nx": p.nx, "ny": p.ny, "nz": p.nz, "nt": nt, "dx": p.dx, "dy": p.dy, "dz": p.dz, "dt": p.dt, "g": p.g,
+            "makeGif": "false", "SORnx": prof.shape[1], "SORa": float(z["sor_h"])}
+    r = _run("ic_w_evolution", tmp_path, args)
+    assert r.returncode == 0, r.stderr.decode()
+    vals = _cols(tmp_path / "Data" / "valsPerLoop_test.txt").reshape(nt, 4)
+    assert np.max(np.abs(vals[:, 0] - z["energy"]) / np.abs(z["energy"])) <= 1e-12
+    for c, key in ((2, "L0"), (3, "L1")):
+        assert np.max(np.abs(vals[:, c] - z[key])) <= 1e-9 * np.max(np.abs(z[key])), key
+    final = _cols(tmp_path / "Data" / "finalField.txt").reshape(-1, 5).T
+    for c in range(5):
+        ref = np.max(np.abs(z["final"][c]))
+        assert np.max(np.abs(final[c] - z["final"][c])) <= 1e-12 * ref, c
+
+
 def test_icw_program_rejects_unprovided_ic(tmp_path):
-    r = _run("ic_w_evolution", tmp_path, {"nx": 4, "ny": 4, "nz": 4, "nt": 1, "ic_type": "loop collision"})
+    r = _run("ic_w_evolution", tmp_path, {"nx": 4, "ny": 4, "nz": 4, "nt": 1, "ic_type": "NG sine"})
     assert r.returncode == 2 and b"ic_type" in r.stderr

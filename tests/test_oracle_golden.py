@@ -216,6 +216,52 @@ def test_loop_collision_default_geometry_is_the_references(oracle_mod):
         assert np.array_equal(np.array(geo[k], dtype=np.float64), z[k]), k
 
 
+def test_icfunc_loop_collision_bit_exact(oracle_mod):
+    """ic_w_evolution's own IC, ic_func.cpp's "loop collision" (:966-1720, the
+    ic_type it ships with, :25), then three periodic steps: ic_w_evolution
+    writes no IC, so the pin is what it writes -- the newest level after the
+    steps and the L0/L1 string lengths of every step, bit for bit -- and its
+    energies to 1e-12 (the reference sums them in its own OpenMP order)."""
+    from axions_gb300.params import ENERGY_EVOLUTION, icfunc_loop_collision
+    O = oracle_mod
+    z = load_golden("ref_icfunc_loop_collision")
+    p = params_from_json(z["params"])
+    geo = icfunc_loop_collision(p.nx, p.ny, p.nz, p.dx, p.dy, p.dz)
+    st, off = O.loop_collision_ic(p, z["profile"][0], z["profile"][1], float(z["sor_h"]), geo, form="ic_func")
+    assert off == 0
+    q = p.copy()
+    q.energy_form = ENERGY_EVOLUTION
+    diags = O.evolve(q, st.copy(), 0, int(z["nt"]), diag_every=1)
+    L0s, L1s = [], []
+    for n in range(int(z["nt"])):
+        L0, L1 = O.string_length(p, O.detect(p, st, n, 0), True)
+        L0s.append(L0)
+        L1s.append(L1)
+        O.step(p, st, n)
+    assert np.array_equal(np.array(L0s), z["L0"])
+    assert np.array_equal(np.array(L1s), z["L1"])
+    last = (int(z["nt"]) - 1) % 2
+    assert np.array_equal(st.reshape(5, 2, -1)[:, last], z["final"])
+    assert np.allclose([d[1] for d in diags], z["energy"], rtol=1e-12, atol=0)
+
+
+def test_icfunc_loop_collision_differs_from_initialconditions_form(oracle_mod):
+    """The two loop-collision forms are different ICs on the same geometry (the
+    ic_func form measures from lab-frame positions and keeps only the boost
+    term of the one-forms), and the ic_func form rejects a string at rest."""
+    from axions_gb300.params import icfunc_loop_collision
+    z = load_golden("ref_icfunc_loop_collision")
+    p = params_from_json(z["params"])
+    geo = icfunc_loop_collision(p.nx, p.ny, p.nz, p.dx, p.dy, p.dz)
+    a, _ = oracle_mod.loop_collision_ic(p, z["profile"][0], z["profile"][1], float(z["sor_h"]), geo, form="ic_func")
+    b, _ = oracle_mod.loop_collision_ic(p, z["profile"][0], z["profile"][1], float(z["sor_h"]), geo)
+    assert not np.array_equal(a, b)
+    rest = dict(geo, v2s=[0.0, 0.0, 0.0])
+    with pytest.raises(RuntimeError):
+        oracle_mod.loop_collision_ic(p, z["profile"][0], z["profile"][1], float(z["sor_h"]), rest, form="ic_func")
+    oracle_mod.loop_collision_ic(p, z["profile"][0], z["profile"][1], float(z["sor_h"]), rest)
+
+
 SINE_CASES = ["ref_ng_sine_ic", "ref_ng_sine_ic_b", "ref_simple_sine_ic"]
 
 

@@ -13,7 +13,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import ROOT, load_golden
+from conftest import ROOT, load_golden, params_from_json
 
 pytestmark = pytest.mark.gpu
 
@@ -196,6 +196,25 @@ def test_loop_collision_default_geometry_and_evolution(lattice_mod, oracle_mod):
     for c in range(5):
         ref = np.linalg.norm(want[c])
         assert np.linalg.norm(now[c] - want[c]) <= TOL * ref
+
+
+def test_icfunc_loop_collision_ic_against_oracle(lattice_mod, oracle_mod):
+    """ic_func.cpp's older "loop collision" (:966-1720) on the GPU against the
+    oracle's, which matches the reference's ic_w_evolution bit for bit: both
+    levels within 1e-12, with ic_func.cpp:61-72's strings as the default."""
+    from axions_gb300.params import icfunc_loop_collision
+    z = load_golden("ref_icfunc_loop_collision")
+    p = params_from_json(z["params"])
+    prof = z["profile"]
+    st, _ = oracle_mod.loop_collision_ic(p, prof[0], prof[1], float(z["sor_h"]),
+                                         icfunc_loop_collision(p.nx, p.ny, p.nz, p.dx, p.dy, p.dz), form="ic_func")
+    with lattice_mod.Lattice(p) as lat:
+        off = lat.loop_collision_ic_device(prof[0], prof[1], float(z["sor_h"]), form="ic_func")
+        assert off == 0 and lat.time_step == 0
+        _close(_levels(lat), st.reshape(5, 2, -1), TOL)
+        with pytest.raises(Exception):
+            lat.loop_collision_ic_device(prof[0], prof[1], float(z["sor_h"]), {"v2a": [0.0, 0.0, 0.0]},
+                                         form="ic_func")
 
 
 def test_loop_collision_rejects_bad_arguments(lattice_mod):
