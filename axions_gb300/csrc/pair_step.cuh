@@ -24,7 +24,13 @@
 //     tiles, putting it on the warps that issue no staging copies measured
 //     1-4 % faster than on warps 0 and 1);
 //   * x-backward data, and the next plane's own values (read as x-forward
-//     neighbours), are carried in registers.
+//     neighbours), are carried in registers;
+//   * Abelian-Higgs loads each pair's level n-1 one plane ahead and unrolls
+//     its x-march by two (0.756 -> 0.797 of measured HBM at 512^3); Moore,
+//     at the register limit, re-reads its own link data from shared memory
+//     after the barrier (0.703 -> 0.709 at 768^3);
+//   * per-plane global offsets are 32-bit (nx*ny*nz < 2^31), one multiply-add
+//     per address (Moore 0.675 -> 0.703).
 // Used where the layout allows 16-byte chunks and aligned pairs: periodic z,
 // nz a multiple of 4, 16-byte aligned fields (every benchmark and serving
 // shape); x and y may be periodic or fixed.  Elsewhere the tiled step runs.
@@ -192,7 +198,7 @@ __device__ __forceinline__ void pair_stage(PairSmem<NS>& sm, int b, const Fields
                                            int pi, int off, int dst)
 {
     if (dst >= 0) {
-        const long long s = (long long)pi * g.syz + off;
+        const int s = pi * (int)g.syz + off;   // below nx*ny*nz < 2^31
 #pragma unroll
         for (int c = 0; c < 2 * NS + 3; ++c)
             __pipeline_memcpy_async(&sm.st[b][c][0][0] + dst, f.now[c] + s, 16);
@@ -200,10 +206,15 @@ __device__ __forceinline__ void pair_stage(PairSmem<NS>& sm, int b, const Fields
     __pipeline_commit();
 }
 
-// One tile: z-pairs (bx*64.., by*8..) of the evolved region, x-planes
+// One tile: z-pairs (bx*64.., by*4..) of the evolved region, x-planes
 // [bz*chunk, bz*chunk + chunk).  Called by every thread of the CTA.  With DIAG
-// the CTA's energy and |G| sums are written to part[0], part[1].
-template <int NS, bool DIAG>
+// the CTA's energy and |G| sums are written to part[0], part[1].  PIPE: the
+// level n-1 of the own pair is loaded one plane ahead, and the plain step's
+// x-march is unrolled by two (the carried values then change registers
+// without copies); Abelian-Higgs in its own kernel.  The Moore tile, at the
+// register limit of four CTAs per SM, and the batch kernel, which holds both
+// DIAG forms, keep the plain march.
+template <int NS, bool DIAG, bool PIPE = false>
 __device__ __forceinline__ void pair_tile(PairSmem<NS>& sm, const Geom& g, const Fields<float, 2 * NS + 3>& f,
                                           const PairCoef& c, const Charges<float>& ch, const DiagOut& d, int bx,
                                           int by, int bz, int chunk, double* part)
@@ -271,6 +282,14 @@ __device__ __forceinline__ void pair_tile(PairSmem<NS>& sm, const Geom& g, const
     pair_stage<NS>(sm, 1, f, g, wrap_idx(ib + 1, g.nx), soff, sdst);
 
     double e_acc = 0.0, g_acc = 0.0;
+    // level n-1 of the own pair for the next plane (PIPE)
+    float2 qn[2 * NS + 3];
+    if constexpr (PIPE) {
+        const int s0 = (ib * g.ny + jj) * g.nz + kk;
+#pragma unroll
+        for (int cc = 0; cc < 2 * NS + 3; ++cc)
+            qn[cc] = (active && ib < ie) ? *reinterpret_cast<const float2*>(f.past[cc] + s0) : p2(0.f);
+    }
     // own values of the current plane carried from the previous plane's x-forward reads
     float2 v[2 * NS], tyo, tzo;
     bool carried = false;
@@ -278,6 +297,7 @@ __device__ __forceinline__ void pair_tile(PairSmem<NS>& sm, const Geom& g, const
     // Two barriers per plane (as tiled_step.cuh): the first makes planes i and
     // i+1 visible and ends every read of plane i-1's stage and link data; the
     // second publishes the link data of plane i.
+#pragma unroll((PIPE && !DIAG) ? 2 : 1)
     for (int i = ib; i < ie; ++i) {
         const int nxt = cur == 2 ? 0 : cur + 1;
         const int nn = nxt == 2 ? 0 : nxt + 1;
@@ -289,10 +309,19 @@ __device__ __forceinline__ void pair_tile(PairSmem<NS>& sm, const Geom& g, const
         constexpr int CS = PT_HY * PT_PZ;   // floats per staged component
         auto at = [&](const float* base, int comp, int row, int column) { return base + comp * CS + row * PT_PZ + column; };
 
-        // the own pair's level n-1, loaded now so that the link phase covers the latency
-        const long long s = ((long long)i * g.ny + jj) * g.nz + kk;
+        // the own pair's level n-1: loaded now so that the link phase covers the
+        // latency, or (PIPE) taken from the previous plane's load
+        const int s = (i * g.ny + jj) * g.nz + kk;   // below nx*ny*nz < 2^31
         float2 qv[2 * NS + 3];
-        if (active) {
+        if constexpr (PIPE) {
+#pragma unroll
+            for (int cc = 0; cc < 2 * NS + 3; ++cc) qv[cc] = qn[cc];
+            if (active && i + 1 < ie) {
+#pragma unroll
+                for (int cc = 0; cc < 2 * NS + 3; ++cc)
+                    qn[cc] = *reinterpret_cast<const float2*>(f.past[cc] + (s + (int)g.syz));
+            }
+        } else if (active) {
 #pragma unroll
             for (int cc = 0; cc < 2 * NS + 3; ++cc) qv[cc] = *reinterpret_cast<const float2*>(f.past[cc] + s);
         } else {
@@ -423,17 +452,27 @@ __device__ __forceinline__ void pair_tile(PairSmem<NS>& sm, const Geom& g, const
                 const float2 imzm = make_float2(*at(S, 2 * q + 1, hy, col - 1), imv.x);
                 const float2 rexm = vm[2 * q], imxm = vm[2 * q + 1];
                 const float2 cym = lds2(&sm.L[LI::cy(q)][ly - 1][lcol]), sym = lds2(&sm.L[LI::sy(q)][ly - 1][lcol]);
-                const float2 czm = make_float2(sm.L[LI::cz(q)][ly][lcol - 1], cz[q].x);
-                const float2 szm = make_float2(sm.L[LI::sz(q)][ly][lcol - 1], sz[q].x);
+                // Moore reads its own y and z link data back from shared memory
+                // rather than holding it across the barrier (four CTAs per SM
+                // leave it 128 registers)
+                float2 cyq = cy[q], syq = sy[q], czq = cz[q], szq = sz[q];
+                if constexpr (NS == 2) {
+                    cyq = lds2(&sm.L[LI::cy(q)][ly][lcol]);
+                    syq = lds2(&sm.L[LI::sy(q)][ly][lcol]);
+                    czq = lds2(&sm.L[LI::cz(q)][ly][lcol]);
+                    szq = lds2(&sm.L[LI::sz(q)][ly][lcol]);
+                }
+                const float2 czm = make_float2(sm.L[LI::cz(q)][ly][lcol - 1], czq.x);
+                const float2 szm = make_float2(sm.L[LI::sz(q)][ly][lcol - 1], szq.x);
                 const float2 m2re = mul2(p2(-2.f), re), m2im = mul2(p2(-2.f), imv);
                 // covariant Laplacian: c = +1 for the real part, -1 for the imaginary part
                 float2 lx = fma2(cx[q], rexp, fma2(sx[q], imxp, fma2(cxm[q], rexm, fma2(neg2(sxm[q]), imxm, m2re))));
-                float2 lyv = fma2(cy[q], reyp, fma2(sy[q], imyp, fma2(cym, reym, fma2(neg2(sym), imym, m2re))));
-                float2 lz = fma2(cz[q], rezp, fma2(sz[q], imzp, fma2(czm, rezm, fma2(neg2(szm), imzm, m2re))));
+                float2 lyv = fma2(cyq, reyp, fma2(syq, imyp, fma2(cym, reym, fma2(neg2(sym), imym, m2re))));
+                float2 lz = fma2(czq, rezp, fma2(szq, imzp, fma2(czm, rezm, fma2(neg2(szm), imzm, m2re))));
                 float2 a_re = fma2(lz, inv_dz2, fma2(lyv, inv_dy2, fma2(lx, inv_dx2, mul2(npot[q], re))));
                 lx = fma2(cx[q], imxp, fma2(neg2(sx[q]), rexp, fma2(cxm[q], imxm, fma2(sxm[q], rexm, m2im))));
-                lyv = fma2(cy[q], imyp, fma2(neg2(sy[q]), reyp, fma2(cym, imym, fma2(sym, reym, m2im))));
-                lz = fma2(cz[q], imzp, fma2(neg2(sz[q]), rezp, fma2(czm, imzm, fma2(szm, rezm, m2im))));
+                lyv = fma2(cyq, imyp, fma2(neg2(syq), reyp, fma2(cym, imym, fma2(sym, reym, m2im))));
+                lz = fma2(czq, imzp, fma2(neg2(szq), rezp, fma2(czm, imzm, fma2(szm, rezm, m2im))));
                 float2 a_im = fma2(lz, inv_dz2, fma2(lyv, inv_dy2, fma2(lx, inv_dx2, mul2(npot[q], imv))));
                 if (c.fric) {
                     a_re = fma2(p2(-c.fric_dt), sub2(re, qv[2 * q]), a_re);
@@ -444,8 +483,8 @@ __device__ __forceinline__ void pair_tile(PairSmem<NS>& sm, const Geom& g, const
                 // gauge current of this scalar
                 const float2 nre = neg2(re);
                 float2 jx = fma2(cx[q], fma2(imv, rexp, mul2(nre, imxp)), mul2(sx[q], fma2(re, rexp, mul2(imv, imxp))));
-                float2 jy = fma2(cy[q], fma2(imv, reyp, mul2(nre, imyp)), mul2(sy[q], fma2(re, reyp, mul2(imv, imyp))));
-                float2 jz = fma2(cz[q], fma2(imv, rezp, mul2(nre, imzp)), mul2(sz[q], fma2(re, rezp, mul2(imv, imzp))));
+                float2 jy = fma2(cyq, fma2(imv, reyp, mul2(nre, imyp)), mul2(syq, fma2(re, reyp, mul2(imv, imyp))));
+                float2 jz = fma2(czq, fma2(imv, rezp, mul2(nre, imzp)), mul2(szq, fma2(re, rezp, mul2(imv, imzp))));
                 if (ch.charge_current) {
                     jx = mul2(jx, p2(ch.q[q]));
                     jy = mul2(jy, p2(ch.q[q]));
@@ -594,7 +633,7 @@ pair_step_kernel(const Geom g, const Fields<float, 2 * NS + 3> f, const PairCoef
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PairSmem<NS>& sm = *reinterpret_cast<PairSmem<NS>*>(smem_raw);
     const int blk = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-    pair_tile<NS, DIAG>(sm, g, f, c, ch, d, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, chunk,
+    pair_tile<NS, DIAG, NS == 1>(sm, g, f, c, ch, d, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, chunk,
                         DIAG ? d.partials + 2 * blk : nullptr);
 }
 

@@ -187,6 +187,8 @@ Params::Params(Program prog)
         v["SORnx"] = "30001";
         v["SORa"] = "0.01";
         v["n"] = "1";
+        // the strings of "loop collision" (ic_func.cpp:61-72 when empty)
+        for (const char* k : {"pos1s", "pos1a", "pos2s", "pos2a", "v1s", "v1a", "v2s", "v2a"}) v[k] = "";
         v["v1x"] = "0.24";                  // ic_func.cpp:62-64
         v["v1y"] = "0.5499090833947008";
         v["v1z"] = "0";
