@@ -17,7 +17,9 @@
 //     x-planes; four CTAs share an SM, so while one waits at a barrier the
 //     others issue (8-row tiles of 8 warps, two per SM, ran 6 % slower);
 //   * each plane's now level, tile plus one-site halo, is staged in shared
-//     memory by 16-byte cp.async chunks, two planes ahead, in a 3-stage ring;
+//     memory by 16-byte cp.async chunks in a ring: Abelian-Higgs 4 stages
+//     (planes i+1 and i+2 in flight while plane i is computed), Moore 3 (its
+//     4 CTAs per SM take the shared memory a fourth stage would need);
 //   * every site's link data (e^{i q theta} per direction and scalar, sines of
 //     the plaquettes P_xy, P_xz, P_yz) is evaluated once per step: own sites by
 //     their thread, the low y and z halo by the last two warps (with 8-row
@@ -26,7 +28,8 @@
 //   * x-backward data, and the next plane's own values (read as x-forward
 //     neighbours), are carried in registers;
 //   * Abelian-Higgs loads each pair's level n-1 one plane ahead and unrolls
-//     its x-march by two (0.756 -> 0.797 of measured HBM at 512^3); Moore,
+//     its x-march by two (0.756 -> 0.797 of measured HBM at 512^3; with the
+//     4-stage ring 0.821); Moore,
 //     at the register limit, re-reads its own link data from shared memory
 //     after the barrier (0.703 -> 0.709 at 768^3);
 //   * per-plane global offsets are 32-bit (nx*ny*nz < 2^31), one multiply-add
@@ -56,11 +59,14 @@ constexpr int PT_NQ = PT_PZ / 4;       // 16-byte chunks per staged row
 constexpr int PT_LY = PT_Y + 1;        // link rows j0-1 .. j0+7 (row ly holds j0 - 1 + ly)
 constexpr int PT_LP = 68;              // link row pitch (floats): column PT_LC0 + m holds z = k0 + m
 constexpr int PT_LC0 = 2;
-constexpr int PT_STAGES = 3;
+// staging ring depth: Abelian-Higgs 4 (planes i+1 and i+2 in flight while
+// plane i is computed; 44 KB per CTA), Moore 3 (four 51 KB CTAs fill an SM)
+template <int NS>
+constexpr int pt_stages() { return NS == 1 ? 4 : 3; }
 
 template <int NS>
 struct PairSmem {
-    float st[PT_STAGES][2 * NS + 3][PT_HY][PT_PZ];  // components in field order: scalars, then theta_x,y,z
+    float st[pt_stages<NS>()][2 * NS + 3][PT_HY][PT_PZ];  // components in field order: scalars, then theta_x,y,z
     float L[4 * NS + 3][PT_LY][PT_LP];              // link data (LinkIdx<NS> order)
     double red[2][PT_Y];
 };
@@ -277,9 +283,10 @@ __device__ __forceinline__ void pair_tile(PairSmem<NS>& sm, const Geom& g, const
 #pragma unroll
         for (int cc = 0; cc < 2 * NS; ++cc) vm[cc] = *reinterpret_cast<const float2*>(f.now[cc] + s);
     }
+    constexpr int ST = pt_stages<NS>();
     int cur = 0;
-    pair_stage<NS>(sm, 0, f, g, ib0, soff, sdst);
-    pair_stage<NS>(sm, 1, f, g, wrap_idx(ib + 1, g.nx), soff, sdst);
+#pragma unroll
+    for (int b = 0; b < ST - 1; ++b) pair_stage<NS>(sm, b, f, g, wrap_idx(ib + b, g.nx), soff, sdst);
 
     double e_acc = 0.0, g_acc = 0.0;
     // level n-1 of the own pair for the next plane (PIPE)
@@ -299,11 +306,15 @@ __device__ __forceinline__ void pair_tile(PairSmem<NS>& sm, const Geom& g, const
     // second publishes the link data of plane i.
 #pragma unroll((PIPE && !DIAG) ? 2 : 1)
     for (int i = ib; i < ie; ++i) {
-        const int nxt = cur == 2 ? 0 : cur + 1;
-        const int nn = nxt == 2 ? 0 : nxt + 1;
-        __pipeline_wait_prior(0);
+        const int nxt = cur + 1 == ST ? 0 : cur + 1;
+        const int nn = cur == 0 ? ST - 1 : cur - 1;   // the slot of plane i-1
+        // planes i and i+1 (own copies; with 4 stages plane i+2 may still be in flight)
+        __pipeline_wait_prior(ST - 3);
         __syncthreads();
-        if (i + 1 < ie) pair_stage<NS>(sm, nn, f, g, wrap_idx(i + 2, g.nx), soff, sdst);
+        // plane i+ST-1 into the slot plane i-1 left; one group per plane, so
+        // that the wait above always counts planes
+        if (i + ST - 2 < ie) pair_stage<NS>(sm, nn, f, g, wrap_idx(i + ST - 1, g.nx), soff, sdst);
+        else __pipeline_commit();
         const float* S = &sm.st[cur][0][0][0];
         const float* X = &sm.st[nxt][0][0][0];
         constexpr int CS = PT_HY * PT_PZ;   // floats per staged component
