@@ -49,10 +49,10 @@ FORMS = ("f64", "f64_strict", "f32")
 BYTES = {"ah": {"f64": 120, "f64_strict": 120, "f32": 60}, "moore": {"f64": 168, "f64_strict": 168, "f32": 84}}
 KERNEL_NAME = {"f64": "ah_links_kernel + ah_update_kernel (FP64 two-pass step, fused multiply-adds)",
                "f64_strict": "ah_links_kernel + ah_update_kernel (FP64 two-pass step, reference operation order)",
-               "f32": "tiled_step_kernel<float, 1> (FP32 fused tiled step)"}
+               "f32": "pair_step_kernel<1> (FP32 step, two z-sites per thread in paired FP32 instructions)"}
 KERNEL_NAME_MOORE = {"f64": "moore_step_kernel<double> (one-pass FP64 step)",
                      "f64_strict": "moore_step_kernel<double> (one-pass FP64 step)",
-                     "f32": "tiled_step_kernel<float, 2> (FP32 fused tiled step, two scalars)"}
+                     "f32": "pair_step_kernel<2> (FP32 step, two z-sites per thread in paired FP32 instructions, two scalars)"}
 
 
 def bytes_per_site(precision: str) -> int:
