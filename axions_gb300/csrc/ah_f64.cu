@@ -13,9 +13,9 @@ cudaError_t launch_ah_step_f64(const Geom& g, const Fields<double, 5>& f, const 
 int ah_link_slots() { return L_COUNT; }
 
 cudaError_t launch_ah_twopass_strict(const Geom& g, const Fields<double, 5>& f, double* L, const StepCoef& c,
-                                     const DiagOut& d, bool diag, bool recip, cudaStream_t st, int phase)
+                                     const DiagOut& d, bool diag, bool recip, cudaStream_t st)
 {
-    return launch_ah_twopass<true>(g, f, L, c, d, diag, recip, st, phase);
+    return launch_ah_twopass<true>(g, f, L, c, d, diag, recip, st);
 }
 
 cudaError_t launch_divergence_f64(const Geom& g, const double* tx, const double* ty, const double* tz, const StepCoef& c,

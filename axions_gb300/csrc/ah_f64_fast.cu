@@ -5,9 +5,9 @@
 namespace lat {
 
 cudaError_t launch_ah_twopass_fast(const Geom& g, const Fields<double, 5>& f, double* L, const StepCoef& c,
-                                   const DiagOut& d, bool diag, bool recip, cudaStream_t st, int phase)
+                                   const DiagOut& d, bool diag, bool recip, cudaStream_t st)
 {
-    return launch_ah_twopass<false>(g, f, L, c, d, diag, recip, st, phase);
+    return launch_ah_twopass<false>(g, f, L, c, d, diag, recip, st);
 }
 
 }  // namespace lat

@@ -324,9 +324,8 @@ __global__ void __launch_bounds__(BLOCK, 2) ah_update_kernel(const Geom g, const
 }
 
 template <bool STRICT>
-// phase: 1 = the links pass, 2 = the update pass, 3 = both
 cudaError_t launch_ah_twopass(const Geom& g, const Fields<double, 5>& f, double* L, const StepCoef& c,
-                              const DiagOut& d, bool diag, bool recip, cudaStream_t st, int phase = 3)
+                              const DiagOut& d, bool diag, bool recip, cudaStream_t st)
 {
     const long long N = (long long)g.nx * g.syz;
     const LinkSlots Lw = link_slots(L, N);
@@ -337,13 +336,10 @@ cudaError_t launch_ah_twopass(const Geom& g, const Fields<double, 5>& f, double*
     all.hiy = g.ny;
     all.hiz = g.nz;
     const dim3 block(BZ, BY);
-    if (phase & 1) {
-        if (diag) ah_links_kernel<STRICT, true><<<site_grid(all), block, 0, st>>>(g, f.now[2], f.now[3], f.now[4], Lw);
-        else ah_links_kernel<STRICT, false><<<site_grid(all), block, 0, st>>>(g, f.now[2], f.now[3], f.now[4], Lw);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-    }
-    if (!(phase & 2)) return cudaSuccess;
+    if (diag) ah_links_kernel<STRICT, true><<<site_grid(all), block, 0, st>>>(g, f.now[2], f.now[3], f.now[4], Lw);
+    else ah_links_kernel<STRICT, false><<<site_grid(all), block, 0, st>>>(g, f.now[2], f.now[3], f.now[4], Lw);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
     const dim3 grid = site_grid(g);
     if (diag) {
         if (recip) ah_update_kernel<STRICT, true, true><<<grid, block, 0, st>>>(g, f, Lr, c, d);

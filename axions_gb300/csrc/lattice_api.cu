@@ -5,7 +5,6 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
-#include <functional>
 #include <vector>
 
 #include "lattice_handle.hpp"
@@ -365,12 +364,6 @@ int lat_destroy(lat_handle* h)
     if (h->snap_staged) cudaEventDestroy(h->snap_staged);
     if (h->snap_copied) cudaEventDestroy(h->snap_copied);
     if (h->snap_stream) cudaStreamDestroy(h->snap_stream);
-    if (h->run_stream) {
-        cudaStreamSynchronize(h->run_stream);
-        cudaStreamDestroy(h->run_stream);
-    }
-    if (h->run_uploaded) cudaEventDestroy(h->run_uploaded);
-    if (h->run_level) cudaEventDestroy(h->run_level);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
     return LAT_OK;
@@ -481,24 +474,10 @@ static int ensure_boundaries(lat_handle* h)
     return LAT_OK;
 }
 
-// wait_ev (lat_run's first step): an event the step waits for before it reads
-// anything but the now level's theta.  The two-pass FP64 step launches its
-// links pass first and waits before the rest; other steps wait at the start.
-static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, bool write = true,
-                   cudaEvent_t wait_ev = nullptr)
+static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, bool write = true)
 {
     const lat_params& p = h->p;
     const int tNow = (int)((h->n + 1) % 2), tPast = (int)(h->n % 2);
-    // The two-pass FP64 Abelian-Higgs step with periodic or fixed walls (where
-    // nothing but its passes touches the levels) launches the links pass, then
-    // the divergence if needed and the update pass: only the links pass runs
-    // before wait_ev.  Any other step waits at its start.
-    const bool split = p.model == LAT_MODEL_AH && h->elem == 8 && h->links && p.bc <= LAT_BC_FIXED &&
-                       bc_z_kind(p) <= LAT_BC_FIXED;
-    if (wait_ev && !split) {
-        LAT_CK(cudaStreamWaitEvent(h->stream, wait_ev, 0));
-        wait_ev = nullptr;
-    }
     int rc = ensure_boundaries(h);
     if (rc) return rc;
     const bool absorb = write && p.bc == LAT_BC_ABSORBING;
@@ -529,19 +508,15 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
     d.charge_current = p.moore_current == LAT_MOORE_CURRENT_CHARGE;
     d.write = write ? 1 : 0;
     const int th0 = h->ncomp - 3;
-    // divergence of the past level's theta for this step's Gauss term (a split
-    // step launches it between its passes, which do not touch it)
-    auto divergence = [&]() -> int {
-        if (!(diag && p.g != 0 && !h->div_valid)) return LAT_OK;
+    // divergence of the past level's theta for this step's Gauss term
+    if (diag && p.g != 0 && !h->div_valid) {
         if (h->elem == 8)
             LAT_CKL(launch_divergence_f64(h->geom, (const double*)h->slot(th0, tPast), (const double*)h->slot(th0 + 1, tPast),
                                          (const double*)h->slot(th0 + 2, tPast), cf, (double*)h->divbuf, h->stream));
         else
             LAT_CKL(launch_divergence_f32(h->geom, (const float*)h->slot(th0, tPast), (const float*)h->slot(th0 + 1, tPast),
                                          (const float*)h->slot(th0 + 2, tPast), cf, (float*)h->divbuf, h->stream));
-        return LAT_OK;
-    };
-    if (!split && (rc = divergence())) return rc;
+    }
     int tiled_used = 0;  // CTAs of the x-marching FP32 step, if it ran
     if (p.model == LAT_MODEL_AH) {
         if (h->elem == 8) {
@@ -551,19 +526,9 @@ static int do_step(lat_handle* h, bool diag, bool store_div, double* diag_dst, b
                 f.past[c] = (double*)h->slot(c, tPast);
             }
             if (h->links) {
-                auto passes = [&](int phase) {
-                    return p.precision == LAT_F64_FAST
-                               ? launch_ah_twopass_fast(h->geom, f, h->links, cf, d, diag, h->recip, h->stream, phase)
-                               : launch_ah_twopass_strict(h->geom, f, h->links, cf, d, diag, h->recip, h->stream, phase);
-                };
-                if (split) {
-                    LAT_CK(passes(1));
-                    if (wait_ev) LAT_CK(cudaStreamWaitEvent(h->stream, wait_ev, 0));
-                    if ((rc = divergence())) return rc;
-                    LAT_CK(passes(2));
-                } else {
-                    LAT_CK(passes(3));
-                }
+                LAT_CK(p.precision == LAT_F64_FAST
+                           ? launch_ah_twopass_fast(h->geom, f, h->links, cf, d, diag, h->recip, h->stream)
+                           : launch_ah_twopass_strict(h->geom, f, h->links, cf, d, diag, h->recip, h->stream));
                 h->launches += 2;
             } else {
                 LAT_CKL(launch_ah_step_f64(h->geom, f, cf, d, diag, h->stream));
@@ -659,11 +624,9 @@ int lat_step_diag(lat_handle* h, lat_diag* out)
     return LAT_OK;
 }
 
-// The loop of lat_advance.  first_wait: passed to the first step (see
-// do_step); before_last: called before the last step is enqueued.
+// The loop of lat_advance.
 static int advance_impl(lat_handle* h, int32_t nsteps, int32_t diag_every, lat_diag* out, int64_t cap,
-                        int64_t* count, cudaEvent_t first_wait = nullptr,
-                        const std::function<int()>& before_last = nullptr)
+                        int64_t* count)
 {
     int64_t ndiag = 0;
     if (diag_every > 0) {
@@ -675,15 +638,11 @@ static int advance_impl(lat_handle* h, int32_t nsteps, int32_t diag_every, lat_d
     }
     std::vector<int64_t> steps;
     for (int32_t q = 0; q < nsteps; ++q) {
-        if (q == nsteps - 1 && before_last) {
-            int rc = before_last();
-            if (rc) return rc;
-        }
         const int64_t n = h->n;
         const bool diag = diag_every > 0 && n % diag_every == 0 && ndiag < cap;
         const bool next = diag_every > 0 && (n + 1) % diag_every == 0;
         const bool store = next && h->p.g != 0;
-        int rc = do_step(h, diag, store, diag ? h->diag_dev + 2 * ndiag : nullptr, true, q == 0 ? first_wait : nullptr);
+        int rc = do_step(h, diag, store, diag ? h->diag_dev + 2 * ndiag : nullptr, true);
         if (rc) return rc;
         if (diag) {
             steps.push_back(n);
@@ -716,79 +675,20 @@ int lat_advance(lat_handle* h, int32_t nsteps, int32_t diag_every, lat_diag* out
     return advance_impl(h, nsteps, diag_every, out, cap, count);
 }
 
-// The copies of lat_run that overlap the steps go on a second stream of the
-// handle, created on first use.
-static int ensure_run_stream(lat_handle* h)
-{
-    if (h->run_stream) return LAT_OK;
-    LAT_CK(cudaStreamCreateWithFlags(&h->run_stream, cudaStreamNonBlocking));
-    LAT_CK(cudaEventCreateWithFlags(&h->run_uploaded, cudaEventDisableTiming));
-    LAT_CK(cudaEventCreateWithFlags(&h->run_level, cudaEventDisableTiming));
-    return LAT_OK;
-}
-
+// The three calls in one.  Overlapping the copies with the first and the
+// last step on a second stream (uploads during the first link pass, the final
+// past level's download during the last step) ran 5-10 % slower than the
+// calls in sequence on GB300 (Grace host link), so the calls run in sequence.
 int lat_run(lat_handle* h, const double* now, const double* past, int64_t time_step, int32_t nsteps,
             int32_t diag_every, lat_diag* out, int64_t cap, int64_t* count, double* now_out, double* past_out)
 {
     LAT_REQUIRE(h && now && past, "lat_run: null argument");
     LAT_REQUIRE(time_step >= 0 && nsteps >= 0 && diag_every >= 0, "lat_run: bad argument");
     LAT_REQUIRE(diag_every == 0 || (out && cap >= 0), "lat_run: diagnostics requested without output");
-    LAT_CK(cudaSetDevice(h->device));
-    const lat_params& p = h->p;
-    const bool overlap = nsteps >= 1 && p.model == LAT_MODEL_AH && h->elem == 8 && h->links &&
-                         p.bc <= LAT_BC_FIXED && bc_z_kind(p) <= LAT_BC_FIXED;
     int rc;
-    if (!overlap) {  // the three calls in sequence
-        if ((rc = lat_set_state(h, now, past, time_step))) return rc;
-        if ((rc = advance_impl(h, nsteps, diag_every, out, cap, count))) return rc;
-        return (now_out || past_out) ? lat_get_state(h, now_out, past_out) : LAT_OK;
-    }
-    if ((rc = ensure_run_stream(h))) return rc;
-    // the second stream's uploads are not ordered after earlier work of the
-    // handle's stream, which may still read the slots
-    LAT_CK(cudaStreamSynchronize(h->stream));
-    h->n = time_step;
-    h->bc_level = -1;
-    h->div_valid = false;
-    const int tNow = (int)((time_step + 1) % 2), tPast = (int)(time_step % 2);
-    const size_t bytes = sizeof(double) * (size_t)h->N;
-    // theta of the now level first, on the step stream: the first links pass
-    // needs nothing else; the other components follow on the second stream
-    for (int c = 2; c < 5; ++c)
-        LAT_CK(cudaMemcpyAsync(h->slot(c, tNow), now + (size_t)c * h->N, bytes, cudaMemcpyHostToDevice, h->stream));
-    for (int c = 0; c < 2; ++c)
-        LAT_CK(cudaMemcpyAsync(h->slot(c, tNow), now + (size_t)c * h->N, bytes, cudaMemcpyHostToDevice, h->run_stream));
-    for (int c = 0; c < 5; ++c)
-        LAT_CK(cudaMemcpyAsync(h->slot(c, tPast), past + (size_t)c * h->N, bytes, cudaMemcpyHostToDevice, h->run_stream));
-    LAT_CK(cudaEventRecord(h->run_uploaded, h->run_stream));
-    const int64_t nf = time_step + nsteps;  // TimeStep of the final now level
-    const int fNow = (int)((nf + 1) % 2), fPast = (int)(nf % 2);
-    // the level that becomes the final past level is read-only during the last
-    // step: its download overlaps that step
-    bool past_early = false;
-    auto before_last = [&]() -> int {
-        if (!past_out || nsteps < 2) return LAT_OK;
-        // the now level (slot fPast) becomes the final past level
-        LAT_CK(cudaEventRecord(h->run_level, h->stream));
-        LAT_CK(cudaStreamWaitEvent(h->run_stream, h->run_level, 0));
-        for (int c = 0; c < 5; ++c)
-            LAT_CK(cudaMemcpyAsync(past_out + (size_t)c * h->N, h->slot(c, fPast), bytes, cudaMemcpyDeviceToHost,
-                                   h->run_stream));
-        past_early = true;
-        return LAT_OK;
-    };
-    rc = advance_impl(h, nsteps, diag_every, out, cap, count, h->run_uploaded, before_last);
-    if (rc) {
-        cudaStreamSynchronize(h->run_stream);
-        return rc;
-    }
-    for (int c = 0; c < 5 && now_out; ++c)
-        LAT_CK(cudaMemcpyAsync(now_out + (size_t)c * h->N, h->slot(c, fNow), bytes, cudaMemcpyDeviceToHost, h->stream));
-    for (int c = 0; c < 5 && past_out && !past_early; ++c)
-        LAT_CK(cudaMemcpyAsync(past_out + (size_t)c * h->N, h->slot(c, fPast), bytes, cudaMemcpyDeviceToHost, h->stream));
-    LAT_CK(cudaStreamSynchronize(h->stream));
-    LAT_CK(cudaStreamSynchronize(h->run_stream));
-    return LAT_OK;
+    if ((rc = lat_set_state(h, now, past, time_step))) return rc;
+    if ((rc = advance_impl(h, nsteps, diag_every, out, cap, count))) return rc;
+    return (now_out || past_out) ? lat_get_state(h, now_out, past_out) : LAT_OK;
 }
 
 int lat_diagnostics(lat_handle* h, lat_diag* out)

@@ -48,10 +48,6 @@ struct lat_handle {
     cudaEvent_t snap_staged = nullptr;   // staging done (handle stream)
     cudaEvent_t snap_copied = nullptr;   // copy done (snap_stream)
     bool snap_pending = false;
-    // lat_run: copies that overlap the steps
-    cudaStream_t run_stream = nullptr;
-    cudaEvent_t run_uploaded = nullptr;  // the upload on run_stream is done
-    cudaEvent_t run_level = nullptr;     // the steps before the last are done (handle stream)
     int64_t bytes = 0;
     int64_t launches = 0;      // kernels launched by this handle
 

@@ -110,13 +110,12 @@ cudaError_t launch_moore_step_f64(const Geom&, const Fields<double, 7>&, const S
                                   cudaStream_t);
 cudaError_t launch_moore_step_f32(const Geom&, const Fields<float, 7>&, const StepCoef&, const DiagOut&, bool diag,
                                   cudaStream_t);
-// two-pass FP64 Abelian-Higgs step (link data in L, [15][N] doubles);
-// phase 1 launches the links pass, 2 the update pass, 3 both
+// two-pass FP64 Abelian-Higgs step (link data in L, [15][N] doubles)
 int ah_link_slots();
 cudaError_t launch_ah_twopass_strict(const Geom&, const Fields<double, 5>&, double* L, const StepCoef&, const DiagOut&,
-                                     bool diag, bool recip, cudaStream_t, int phase = 3);
+                                     bool diag, bool recip, cudaStream_t);
 cudaError_t launch_ah_twopass_fast(const Geom&, const Fields<double, 5>&, double* L, const StepCoef&, const DiagOut&,
-                                   bool diag, bool recip, cudaStream_t, int phase = 3);
+                                   bool diag, bool recip, cudaStream_t);
 // x-planes per CTA of the tiled FP32 step for a new handle (tuned value of the
 // shape if known in this process, else a heuristic); tune.cu
 int default_chunk(const lat_params& p);

@@ -375,8 +375,7 @@ class Lattice:
 
     def run(self, now: np.ndarray, past: np.ndarray | None, time_step: int, nsteps: int, diag_every: int = 0,
             now_out: np.ndarray | None = None, past_out: np.ndarray | None = None):
-        """set_state + advance + get_state in one call (lat_run), with the copies
-        overlapping the steps where the step allows it.  Returns (diagnostics,
+        """set_state + advance + get_state in one call (lat_run).  Returns (diagnostics,
         now_out, past_out); output arrays passed in (C-contiguous float64 of
         ncomp*N elements, e.g. pinned buffers) are filled, others allocated."""
         now = np.ascontiguousarray(now, dtype=np.float64).reshape(self.ncomp, self.N)

@@ -12,9 +12,8 @@ Reported (one JSON line on rank 0):
                library's stream around the K timed steps);
   e2e          the same metric through the C ABI with host buffers: one
                lat_run call (upload of the state from pinned memory, the K
-               steps, the diagnostics and the download of the final state,
-               its copies overlapping the steps where the step allows), all
-               inside the timed region;
+               steps, the diagnostics and the download of the final state),
+               all inside the timed region;
   roofline     dominant kernel (the step kernel): algorithmic bytes per
                site-update x sites / its average launch time, against the
                measured HBM copy bandwidth;

@@ -208,11 +208,8 @@ int lat_advance(lat_handle* h, int32_t nsteps, int32_t diag_every,
 /* A whole run from host state to host state: lat_set_state(now, past,
  * time_step), lat_advance(nsteps, diag_every, out, cap, count) and
  * lat_get_state(now_out, past_out) in one call, with the same results bit for
- * bit (now_out or past_out may be NULL).  For the two-pass FP64 Abelian-Higgs
- * step with periodic or fixed walls the copies overlap the steps on a second
- * stream of the handle: every upload but the now level's theta runs during
- * the first step's link pass, and the download of the final past level during
- * the last step.  Replaces a run of the reference program: the initial
+ * bit (now_out or past_out may be NULL).  Replaces a run of the reference
+ * program: the initial
  * conditions read or drawn at mpi_evolution.cpp:231-312, then the loop at
  * 354-985.  Synchronous: the host buffers may be reused when it returns. */
 int lat_run(lat_handle* h, const double* now, const double* past, int64_t time_step,
