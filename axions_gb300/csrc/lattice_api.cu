@@ -433,7 +433,15 @@ int lat_set_state(lat_handle* h, const double* now, const double* past, int64_t 
     h->bc_level = -1;  // new values: their Neumann layer is not set yet
     const int tNow = (int)((time_step + 1) % 2), tPast = (int)(time_step % 2);
     if ((rc = upload_level(h, now, tNow))) return rc;
-    if ((rc = upload_level(h, past, tPast))) return rc;
+    if (past == now) {
+        // one level for both (a stationary start, mpi_evolution.cpp:155-162):
+        // it crosses the host link once and is copied on the device
+        for (int c = 0; c < h->ncomp; ++c)
+            LAT_CK(cudaMemcpyAsync(h->slot(c, tPast), h->slot(c, tNow), (size_t)h->elem * h->N,
+                                   cudaMemcpyDeviceToDevice, h->stream));
+    } else if ((rc = upload_level(h, past, tPast))) {
+        return rc;
+    }
     LAT_CK(cudaStreamSynchronize(h->stream));
     h->div_valid = false;
     return LAT_OK;

@@ -29,9 +29,9 @@
 //     neighbours), are carried in registers;
 //   * Abelian-Higgs loads each pair's level n-1 one plane ahead and unrolls
 //     its x-march by two (0.756 -> 0.797 of measured HBM at 512^3; with the
-//     4-stage ring 0.821); Moore,
-//     at the register limit, re-reads its own link data from shared memory
-//     after the barrier (0.703 -> 0.709 at 768^3);
+//     4-stage ring 0.821); Moore, at the register limit, re-reads its own
+//     link data from shared memory after the barrier (0.703 -> 0.709 at
+//     768^3);
 //   * per-plane global offsets are 32-bit (nx*ny*nz < 2^31), one multiply-add
 //     per address (Moore 0.675 -> 0.703);
 //   * Moore with charges 1 and 2 (the benchmark's) runs a kernel instance with
@@ -55,11 +55,11 @@ constexpr int PT_TZ = 32;              // threads along z (each two sites)
 constexpr int PT_Z = 2 * PT_TZ;        // tile width along z
 constexpr int PT_Y = 4;                // tile height along y (warps per CTA)
 constexpr int PT_THREADS = PT_TZ * PT_Y;
-constexpr int PT_HY = PT_Y + 2;        // staged rows j0-1 .. j0+8
+constexpr int PT_HY = PT_Y + 2;        // staged rows j0-1 .. j0+PT_Y
 constexpr int PT_PZ = 72;              // staged row pitch (floats): column c holds z = k0 - 4 + c
 constexpr int PT_C0 = 4;               // column of z = k0 (16-byte aligned; own pairs 8-byte aligned)
 constexpr int PT_NQ = PT_PZ / 4;       // 16-byte chunks per staged row
-constexpr int PT_LY = PT_Y + 1;        // link rows j0-1 .. j0+7 (row ly holds j0 - 1 + ly)
+constexpr int PT_LY = PT_Y + 1;        // link rows j0-1 .. j0+PT_Y-1 (row ly holds j0 - 1 + ly)
 constexpr int PT_LP = 68;              // link row pitch (floats): column PT_LC0 + m holds z = k0 + m
 constexpr int PT_LC0 = 2;
 // staging ring depth: Abelian-Higgs 4 (planes i+1 and i+2 in flight while

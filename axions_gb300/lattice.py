@@ -374,14 +374,20 @@ class Lattice:
         return [(buf[q].time_step, buf[q].energy, buf[q].gauss_abs_sum) for q in range(cnt.value)]
 
     def run(self, now: np.ndarray, past: np.ndarray | None, time_step: int, nsteps: int, diag_every: int = 0,
-            now_out: np.ndarray | None = None, past_out: np.ndarray | None = None):
-        """set_state + advance + get_state in one call (lat_run).  Returns (diagnostics,
-        now_out, past_out); output arrays passed in (C-contiguous float64 of
-        ncomp*N elements, e.g. pinned buffers) are filled, others allocated."""
+            now_out: np.ndarray | None = None, past_out: np.ndarray | None = None, past_level: bool = True):
+        """set_state + advance + get_state in one call (lat_run).  past None:
+        a stationary start, both levels `now` (uploaded once).  Returns
+        (diagnostics, now_out, past_out); output arrays passed in (C-contiguous
+        float64 of ncomp*N elements, e.g. pinned buffers) are filled, others
+        allocated; with past_level False the past level is not downloaded and
+        past_out is None."""
         now = np.ascontiguousarray(now, dtype=np.float64).reshape(self.ncomp, self.N)
         past = now if past is None else np.ascontiguousarray(past, dtype=np.float64).reshape(self.ncomp, self.N)
         outs = []
-        for a in (now_out, past_out):
+        for a, want in ((now_out, True), (past_out, past_level)):
+            if not want:
+                outs.append(None)
+                continue
             if a is None:
                 a = np.empty((self.ncomp, self.N), dtype=np.float64)
             elif a.dtype != np.float64 or not a.flags.c_contiguous or a.size != self.ncomp * self.N:
@@ -393,9 +399,11 @@ class Lattice:
         buf = (LatDiag * max(cap, 1))()
         cnt = ctypes.c_int64(0)
         _check("lat_run", self.L.lat_run(self.h, _dp(now), _dp(past), int(time_step), int(nsteps), int(diag_every),
-                                         buf, int(cap), ctypes.byref(cnt), _dp(outs[0]), _dp(outs[1])))
+                                         buf, int(cap), ctypes.byref(cnt), _dp(outs[0]),
+                                         _dp(outs[1]) if outs[1] is not None else None))
         diags = [(buf[q].time_step, buf[q].energy, buf[q].gauss_abs_sum) for q in range(cnt.value)]
-        return diags, outs[0].reshape(self.ncomp, self.N), outs[1].reshape(self.ncomp, self.N)
+        return (diags, outs[0].reshape(self.ncomp, self.N),
+                outs[1].reshape(self.ncomp, self.N) if outs[1] is not None else None)
 
     def diagnostics(self) -> LatDiag:
         d = LatDiag()

@@ -11,9 +11,10 @@ Reported (one JSON line on rank 0):
   value        site-updates/s with the state resident in HBM (CUDA events on the
                library's stream around the K timed steps);
   e2e          the same metric through the C ABI with host buffers: one
-               lat_run call (upload of the state from pinned memory, the K
-               steps, the diagnostics and the download of the final state),
-               all inside the timed region;
+               lat_run call (upload of the initial level from pinned memory,
+               a stationary start whose two levels are one array as the
+               reference's IC; the K steps; the diagnostics; the download of
+               the final level), all inside the timed region;
   roofline     dominant kernel (the step kernel): algorithmic bytes per
                site-update x sites / its average launch time, against the
                measured HBM copy bandwidth;
@@ -330,18 +331,17 @@ def measure_gpu(n: int, precision: str, steps: int, warmup: int, ws: int, local:
     kern_ms = statistics.median(plain)
 
     # end to end through the C ABI with host buffers (pinned): one lat_run call
-    # from the IC (both levels equal, in two buffers as a caller holds them)
-    pin_past = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
-    pin_past.numpy()[:] = pin_now.numpy()
+    # from the IC, a stationary start whose two levels are one array, as the
+    # reference's IC (mpi_evolution.cpp:155-162), to the final level, what the
+    # reference's programs write at the end (finalField, ic_w_evolution.cpp:
+    # 1183-1187)
     out_now = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
-    out_past = torch.empty((nc, N), dtype=torch.float64, pin_memory=True)
     dist_barrier(ws)
     torch.cuda.synchronize(dev)
     e0 = time.perf_counter()
     e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e_start.record(stream)
-    diags, _, _ = lat.run(pin_now.numpy(), pin_past.numpy(), 0, steps, DIAG_EVERY, now_out=out_now.numpy(),
-                          past_out=out_past.numpy())
+    diags, _, _ = lat.run(pin_now.numpy(), None, 0, steps, DIAG_EVERY, now_out=out_now.numpy(), past_level=False)
     e_end.record(stream)
     torch.cuda.synchronize(dev)
     e2e_wall = time.perf_counter() - e0
@@ -349,13 +349,13 @@ def measure_gpu(n: int, precision: str, steps: int, warmup: int, ws: int, local:
     if not np.isfinite(out_now.numpy()).all():
         raise RuntimeError("non-finite field after the end-to-end run")
     lat.close()
-    del pin_now, pin_past, out_now, out_past
+    del pin_now, out_now
 
-    state_bytes = 2 * nc * N * 8
+    level_bytes = nc * N * 8
     return {
         "total_ms": total_ms, "kern_ms": kern_ms, "per_ms": per, "kinds": kinds, "launches": launches,
-        "clocks": clocks, "e2e_ms": max(e2e_ms, 1e3 * e2e_wall), "e2e_h2d": state_bytes / steps,
-        "e2e_d2h": (state_bytes + 16 * len(diags)) / steps, "sites": N,
+        "clocks": clocks, "e2e_ms": max(e2e_ms, 1e3 * e2e_wall), "e2e_h2d": level_bytes / steps,
+        "e2e_d2h": (level_bytes + 16 * len(diags)) / steps, "sites": N,
     }
 
 

@@ -181,8 +181,9 @@ int64_t lat_kernel_launches(const lat_handle* h);
 
 /* Upload the state: `now` is the level at TimeStep `time_step`, `past` the one
  * before (for a stationary start pass the same array twice, as
- * mpi_evolution.cpp:155-162 does).  Each is [ncomp][nx*ny*nz] doubles; FP32
- * handles convert on the device.  Replaces the IC load mpi_evolution.cpp:143-285. */
+ * mpi_evolution.cpp:155-162 does: it is then uploaded once and copied on the
+ * device).  Each is [ncomp][nx*ny*nz] doubles; FP32 handles convert on the
+ * device.  Replaces the IC load mpi_evolution.cpp:143-285. */
 int lat_set_state(lat_handle* h, const double* now, const double* past, int64_t time_step);
 /* Download the state; either pointer may be NULL. */
 int lat_get_state(lat_handle* h, double* now, double* past);
@@ -208,10 +209,10 @@ int lat_advance(lat_handle* h, int32_t nsteps, int32_t diag_every,
 /* A whole run from host state to host state: lat_set_state(now, past,
  * time_step), lat_advance(nsteps, diag_every, out, cap, count) and
  * lat_get_state(now_out, past_out) in one call, with the same results bit for
- * bit (now_out or past_out may be NULL).  Replaces a run of the reference
- * program: the initial
- * conditions read or drawn at mpi_evolution.cpp:231-312, then the loop at
- * 354-985.  Synchronous: the host buffers may be reused when it returns. */
+ * bit (now_out or past_out may be NULL; past == now for a stationary start).
+ * Replaces a run of the reference program: the initial conditions read or
+ * drawn at mpi_evolution.cpp:231-312, then the loop at 354-985.  Synchronous:
+ * the host buffers may be reused when it returns. */
 int lat_run(lat_handle* h, const double* now, const double* past, int64_t time_step,
             int32_t nsteps, int32_t diag_every, lat_diag* out, int64_t cap, int64_t* count,
             double* now_out, double* past_out);

@@ -1,14 +1,11 @@
 """lat_run: a whole run from host state to host state in one call.
 
 It must give, bit for bit, what lat_set_state + lat_advance + lat_get_state
-give.  For the two-pass FP64 Abelian-Higgs step with periodic or fixed walls
-its copies overlap the steps on a second stream (the uploads other than the
-now level's theta during the first links pass, the download of the final
-past level during the last step); other configurations run the three calls
-in sequence.  The cases cover both paths, a first step that is an
-energy/Gauss step (its divergence kernel runs between the two passes), one
-and two steps (the last step is also the first), a single output array and
-two runs on one handle.
+give.  The cases cover both FP64 forms, FP32 and Moore, periodic, fixed and
+Neumann walls, a first step that is an energy/Gauss step, one and two steps,
+a single output array, two runs on one handle, and a stationary start passed
+as one array for both levels (uploaded once and copied on the device) with
+only the final level downloaded.
 """
 import numpy as np
 import pytest
@@ -90,3 +87,26 @@ def test_run_twice_on_one_handle_and_one_output(lattice_mod):
     with pytest.raises(ValueError):
         with lattice_mod.Lattice(p) as lat:
             lat.run(now, past, t0, 1, 0, now_out=np.empty(3))
+
+
+@pytest.mark.parametrize("precision", [0, 1, 2])
+def test_stationary_start_as_one_array(lattice_mod, precision):
+    """The same array for both levels (mpi_evolution.cpp:155-162) gives bit for
+    bit what two equal arrays give, through lat_set_state and lat_run, and the
+    run may skip the past level's download."""
+    p = make(lattice_mod, precision)
+    ic = lattice_mod.random_phase_ic(p, 13)
+    twin = ic.copy()
+    ref_d, ref_now, ref_past = sequential(lattice_mod, p, ic, twin, 0, 6, 3)
+    with lattice_mod.Lattice(p) as lat:
+        lat.set_state(ic, twin, 0)
+        ra, rb = lat.get_state()
+    with lattice_mod.Lattice(p) as lat:
+        lat.set_state(ic, None, 0)
+        a, b = lat.get_state()
+        assert np.array_equal(a, ra) and np.array_equal(b, rb)
+        d, got_now, got_past = lat.run(ic, None, 0, 6, 3, past_level=False)
+        assert got_past is None
+        assert d == ref_d and np.array_equal(got_now, ref_now)
+        _, past_now = lat.get_state()
+        assert np.array_equal(past_now, ref_past)
