@@ -619,3 +619,33 @@ def test_fp32_pair_step_tracks_tiled_and_fp64(lattice_mod, model, sides, bc):
         np.testing.assert_allclose([x[2] for x in d], [x[2] for x in res["f64"][1]], rtol=1e-4)
     mx, l2 = normwise(res["pair"][0], res["tiled"][0])
     assert l2 < 2e-6, l2
+
+
+@pytest.mark.parametrize("charges,current", [((2.0, 1.0), 1), ((3.0, -1.0), 0), ((1.0, 0.5), 1)])
+def test_fp32_pair_moore_general_charges(lattice_mod, charges, current):
+    """The Moore pair step for charges other than (1, 2), whose link factors
+    come from the general power loop (or sincos(q theta) for a non-integer
+    charge) rather than the closed-form instance: against the tiled step and
+    the FP64 path with the bounds of the test above."""
+    from axions_gb300.params import ENERGY_EVOLUTION, F32, MODEL_MOORE, make_params
+    q1, q2 = charges
+    p = make_params(MODEL_MOORE, nx=24, ny=22, nz=64, d=0.5, dt=0.1, lam=2.0, lambda2=2.0, lambda12=0.3, eta=1.0,
+                    eta2=1.0, q1=q1, q2=q2, g=0.8, damped_nt=3, dampFac=0.5, alpha=3.0, bc_z=1,
+                    energy_form=ENERGY_EVOLUTION, moore_current=current)
+    ic = lattice_mod.random_phase_ic(p, 43, independent=True)
+    res = {}
+    for name, prec, var in (("f64", 0, 0), ("pair", F32, 0), ("tiled", F32, 3)):
+        q = p.copy()
+        q.precision = prec
+        q.kernel_variant = var
+        with lattice_mod.Lattice(q) as lat:
+            lat.set_state(ic, ic, 0)
+            d = lat.advance(12, diag_every=4)
+            res[name] = (lat.get_slots(), d)
+    s64 = res["f64"][0]
+    for name in ("pair", "tiled"):
+        st, d = res[name]
+        mx, l2 = normwise(st, s64)
+        assert l2 < 2e-6 and mx < 2e-5, (name, mx, l2)
+        np.testing.assert_allclose([x[1] for x in d], [x[1] for x in res["f64"][1]], rtol=1e-5)
+        np.testing.assert_allclose([x[2] for x in d], [x[2] for x in res["f64"][1]], rtol=1e-4)
