@@ -56,23 +56,23 @@ inline LinkSlotsC link_slots_c(const double* L, long long N)
 }
 
 // a / b where b = spacing^2 or spacing: exact reciprocal multiply when every
-// spacing is a power of two (then a*(1/b) == a/b for all a), else IEEE divide.
+// spacing is a power of two (then a*(1/b) == a/b for all a), else the IEEE
+// quotient by cdiv from the host reciprocal.
 template <bool RECIP>
 __device__ __forceinline__ double sdiv(double a, double b, double inv_b)
 {
     if constexpr (RECIP) return mul_pow2(a, inv_b);
-    else return a / b;
+    else return cdiv(a, b, inv_b);
 }
 
-// a / dt.  STRICT: IEEE divide; a zero dividend (every site of the first step
-// from an initial condition with equal levels) returns a * (1/b), the same
-// +-0, instead of entering the division's slow path.  Fast: q = a*r corrected
-// by one residual step (Markstein), which returns the correctly rounded
-// quotient except in rare cases where it is one ulp off.
+// a / dt.  STRICT: the IEEE quotient by cdiv (two residual corrections from
+// the host reciprocal; a zero dividend returns a * (1/b), the same +-0).
+// Fast: q = a*r corrected by one residual step (Markstein), which returns the
+// correctly rounded quotient except in rare cases where it is one ulp off.
 template <bool STRICT>
 __device__ __forceinline__ double tdiv(double a, double b, double inv_b)
 {
-    if constexpr (STRICT) return is_zero(a) ? a * inv_b : a / b;
+    if constexpr (STRICT) return cdiv(a, b, inv_b);
     else {
         const double q = a * inv_b;
         const double r = fma(-q, b, a);

@@ -43,12 +43,13 @@ struct Trig<float> {
     static __device__ __forceinline__ void sincos(float x, float* s, float* c) { __sincosf(reduce(x), s, c); }
 };
 
-// a / b.  FP64 divides (the reference's rounding); FP32 multiplies by the
-// reciprocal computed once on the host.
+// a / b.  FP64: the IEEE quotient (the reference's rounding) by cdiv from the
+// host reciprocal inv_b = RN(1/b), five FP64 instructions; FP32 multiplies by
+// the reciprocal.
 template <class T>
 __device__ __forceinline__ T qdiv(T a, T b, T inv_b)
 {
-    if constexpr (sizeof(T) == 8) return a / b;
+    if constexpr (sizeof(T) == 8) return cdiv(a, b, inv_b);
     else return a * inv_b;
 }
 
