@@ -68,14 +68,14 @@ int batch_chunk(const Geom& g)
 
 namespace {
 
-template <int NS, bool PAIR, bool DIAG>
+template <int NS, bool PAIR, bool DIAG, bool Q12>
 __device__ __forceinline__ void run_item(unsigned char* smem_raw, const BatchJob& J, const Fields<float, 5>& f5,
                                          int bx, int by, int bz, double* part)
 {
     if constexpr (PAIR) {
         PairSmem<NS>& ps = *reinterpret_cast<PairSmem<NS>*>(smem_raw);
         if constexpr (NS == 1) pair_tile<1, DIAG>(ps, J.g, f5, J.pc, J.ch, J.d, bx, by, bz, J.chunk, part);
-        else pair_tile<2, DIAG>(ps, J.g, J.f, J.pc, J.ch, J.d, bx, by, bz, J.chunk, part);
+        else pair_tile<2, DIAG, false, Q12>(ps, J.g, J.f, J.pc, J.ch, J.d, bx, by, bz, J.chunk, part);
         return;
     }
     TiledSmem<float, NS>& sm = *reinterpret_cast<TiledSmem<float, NS>*>(smem_raw);
@@ -90,8 +90,10 @@ __device__ __forceinline__ void run_item(unsigned char* smem_raw, const BatchJob
 // tile (PAIR) or the tiled tile: CTAs stride over the work items of all of
 // them.  One kernel per model and tile keeps each kernel's register use to
 // that tile's: four 4-warp CTAs per SM for the pair tile, as the pair step,
-// four (Abelian-Higgs) or three (Moore) 8-warp CTAs for the tiled tile.
-template <int NS, bool PAIR>
+// four (Abelian-Higgs) or three (Moore) 8-warp CTAs for the tiled tile.  Q12:
+// the Moore pair lattices with charges 1 and 2, whose link factors the tile
+// forms in closed form (pair_step.cuh).
+template <int NS, bool PAIR, bool Q12 = false>
 __global__ void __launch_bounds__(PAIR ? PT_THREADS : TT_THREADS, PAIR ? 4 : (NS == 1 ? 4 : 3))
 batch_step_kernel(const BatchStep* __restrict__ tab)
 {
@@ -135,8 +137,8 @@ batch_step_kernel(const BatchStep* __restrict__ tab)
         const int by = r % sj.tiles_y;
         const int bz = r / sj.tiles_y;
         double* part = sj.diag ? sj.d.partials + 2 * local : nullptr;
-        if (sj.diag) run_item<NS, PAIR, true>(smem_raw, sj, sf5, bx, by, bz, part);
-        else run_item<NS, PAIR, false>(smem_raw, sj, sf5, bx, by, bz, part);
+        if (sj.diag) run_item<NS, PAIR, true, Q12>(smem_raw, sj, sf5, bx, by, bz, part);
+        else run_item<NS, PAIR, false, Q12>(smem_raw, sj, sf5, bx, by, bz, part);
         __syncthreads();  // sj and the tile's shared memory are reused by the next item
     }
 }
@@ -182,8 +184,9 @@ size_t batch_smem_ns()
     return PAIR ? sizeof(PairSmem<NS>) : sizeof(TiledSmem<float, NS>);
 }
 
-// job tables per step: [tiled AH, tiled Moore, pair AH, pair Moore]
-constexpr int kTables = 4;
+// job tables per step: [tiled AH, tiled Moore, pair AH, pair Moore, pair Moore
+// with charges 1 and 2]
+constexpr int kTables = 5;
 
 }  // namespace
 
@@ -204,6 +207,7 @@ struct lat_batch {
     cudaStream_t stream = nullptr;
     int grid[kTables] = {};          // persistent CTAs of each step kernel (table order)
     int K = 0;                       // steps in the captured graph
+    unsigned mask = 0;               // tables whose kernels the graph launches
     int chunk = 0;                   // x-planes per work item; 0: the per-shape rule
     BatchStep* tab_host = nullptr;   // pinned [K][kTables]: per step, the jobs of each kernel
     BatchStep* tab_dev = nullptr;    // [K][kTables]
@@ -240,10 +244,12 @@ static void release_graph(lat_batch* b)
     b->K = 0;
 }
 
-// Build (or reuse) the graph of K steps.
-static int ensure_graph(lat_batch* b, int K)
+// Build (or reuse) the graph of K steps, launching per step the step and
+// finalize kernels of the tables in `mask` only (an empty table's launches
+// cost more than a 32^3 lattice's step).
+static int ensure_graph(lat_batch* b, int K, unsigned mask)
 {
-    if (b->K == K && b->exec) return LAT_OK;
+    if (b->K == K && b->mask == mask && b->exec) return LAT_OK;
     release_graph(b);
     BATCH_CK(cudaMallocHost((void**)&b->tab_host, sizeof(BatchStep) * kTables * (size_t)K));
     BATCH_CK(cudaMalloc((void**)&b->tab_dev, sizeof(BatchStep) * kTables * (size_t)K));
@@ -254,18 +260,50 @@ static int ensure_graph(lat_batch* b, int K)
                     b->stream);
     for (int s = 0; s < K; ++s) {
         BatchStep* t = b->tab_dev + kTables * s;
-        batch_step_kernel<1, false><<<b->grid[0], dim3(TT_Z, TT_Y), batch_smem_ns<1, false>(), b->stream>>>(t);
-        batch_step_kernel<2, false><<<b->grid[1], dim3(TT_Z, TT_Y), batch_smem_ns<2, false>(), b->stream>>>(t + 1);
-        batch_step_kernel<1, true><<<b->grid[2], dim3(PT_TZ, PT_Y), batch_smem_ns<1, true>(), b->stream>>>(t + 2);
-        batch_step_kernel<2, true><<<b->grid[3], dim3(PT_TZ, PT_Y), batch_smem_ns<2, true>(), b->stream>>>(t + 3);
-        for (int q = 0; q < kTables; ++q) batch_finalize_kernel<<<b->max_jobs, 1024, 0, b->stream>>>(t + q);
+        const dim3 tt(TT_Z, TT_Y), pt(PT_TZ, PT_Y);
+        if (mask & 1u) batch_step_kernel<1, false><<<b->grid[0], tt, batch_smem_ns<1, false>(), b->stream>>>(t);
+        if (mask & 2u) batch_step_kernel<2, false><<<b->grid[1], tt, batch_smem_ns<2, false>(), b->stream>>>(t + 1);
+        if (mask & 4u) batch_step_kernel<1, true><<<b->grid[2], pt, batch_smem_ns<1, true>(), b->stream>>>(t + 2);
+        if (mask & 8u) batch_step_kernel<2, true><<<b->grid[3], pt, batch_smem_ns<2, true>(), b->stream>>>(t + 3);
+        if (mask & 16u) batch_step_kernel<2, true, true><<<b->grid[4], pt, batch_smem_ns<2, true>(), b->stream>>>(t + 4);
+        for (int q = 0; q < kTables; ++q)
+            if (mask & (1u << q)) batch_finalize_kernel<<<b->max_jobs, 1024, 0, b->stream>>>(t + q);
     }
     cudaMemcpyAsync(b->diag_host, b->diag_dev, sizeof(double) * 2 * (size_t)K * b->max_jobs, cudaMemcpyDeviceToHost,
                     b->stream);
     BATCH_CK(cudaStreamEndCapture(b->stream, &b->graph));
     BATCH_CK(cudaGraphInstantiate(&b->exec, b->graph, 0));
     b->K = K;
+    b->mask = mask;
     return LAT_OK;
+}
+
+// The table (step kernel) of a lattice: the pair tile where its own layout
+// allows it, else the tiled tile; its model; for a Moore pair lattice whether
+// its charges are 1 and 2.  The choice depends on the lattice alone, never on
+// its company.
+static int table_of(const lat_handle* h, const Fields<float, 7>& fj)
+{
+    Fields<float, 5> f5;
+    for (int c = 0; c < 5; ++c) {
+        f5.now[c] = fj.now[c];
+        f5.past[c] = fj.past[c];
+    }
+    const bool moore = h->p.model == LAT_MODEL_MOORE;
+    const bool pair = moore ? pair_ok(h->geom, fj) : pair_ok(h->geom, f5);
+    const bool q12 = moore && pair && small_int_power(h->p.q1) == 1 && small_int_power(h->p.q2) == 2;
+    return q12 ? 4 : (pair ? 2 : 0) + (moore ? 1 : 0);
+}
+
+static Fields<float, 7> level_fields(const lat_handle* h, int64_t n)
+{
+    const int tNow = (int)((n + 1) % 2), tPast = (int)(n % 2);
+    Fields<float, 7> fj{};
+    for (int c = 0; c < h->ncomp; ++c) {
+        fj.now[c] = (const float*)h->slot(c, tNow);
+        fj.past[c] = (float*)h->slot(c, tPast);
+    }
+    return fj;
 }
 
 extern "C" {
@@ -297,6 +335,7 @@ int lat_batch_create(int32_t max_jobs, lat_batch** out)
     b->grid[1] = grid_of(batch_step_kernel<2, false>, TT_THREADS, batch_smem_ns<2, false>());
     b->grid[2] = grid_of(batch_step_kernel<1, true>, PT_THREADS, batch_smem_ns<1, true>());
     b->grid[3] = grid_of(batch_step_kernel<2, true>, PT_THREADS, batch_smem_ns<2, true>());
+    b->grid[4] = grid_of(batch_step_kernel<2, true, true>, PT_THREADS, batch_smem_ns<2, true>());
     *out = b;
     return LAT_OK;
 }
@@ -376,8 +415,6 @@ int lat_batch_advance(lat_batch* b, int32_t nsteps)
     }
     if (b->jobs.empty()) return 0;
     BATCH_CK(cudaSetDevice(b->device));
-    int rc = ensure_graph(b, nsteps);
-    if (rc) return rc;
     const int K = nsteps;
     // previous work of the handles (uploads, single steps) must be complete
     for (auto& j : b->jobs) BATCH_CK(cudaStreamSynchronize(j.h->stream));
@@ -385,12 +422,15 @@ int lat_batch_advance(lat_batch* b, int32_t nsteps)
     struct Plan {
         int steps;
         int64_t n0;
+        int table;
     };
     std::vector<Plan> plan(b->jobs.size());
+    unsigned mask = 0;
     for (size_t q = 0; q < b->jobs.size(); ++q) {
         auto& j = b->jobs[q];
         const int64_t left = j.stop_step - j.h->n;
-        plan[q] = {(int)std::max<int64_t>(0, std::min<int64_t>(K, left)), j.h->n};
+        plan[q] = {(int)std::max<int64_t>(0, std::min<int64_t>(K, left)), j.h->n, table_of(j.h, level_fields(j.h, j.h->n))};
+        if (plan[q].steps > 0) mask |= 1u << plan[q].table;
         // a diagnostic on the first step needs the divergence of the past level
         const int64_t n = j.h->n;
         if (plan[q].steps > 0 && j.diag_every > 0 && n % j.diag_every == 0 && j.h->p.g != 0 && !j.h->div_valid) {
@@ -407,6 +447,8 @@ int lat_batch_advance(lat_batch* b, int32_t nsteps)
             ++b->launches;
         }
     }
+    int rc = ensure_graph(b, K, mask);
+    if (rc) return rc;
     std::vector<std::vector<int>> diag_slots(b->jobs.size());
     for (int s = 0; s < K; ++s) {
         for (int q = 0; q < kTables; ++q) {
@@ -418,22 +460,9 @@ int lat_batch_advance(lat_batch* b, int32_t nsteps)
             auto& j = b->jobs[q];
             lat_handle* h = j.h;
             const int64_t n = plan[q].n0 + s;
-            const int tNow = (int)((n + 1) % 2), tPast = (int)(n % 2);
-            Fields<float, 7> fj{};
-            for (int c = 0; c < h->ncomp; ++c) {
-                fj.now[c] = (const float*)h->slot(c, tNow);
-                fj.past[c] = (float*)h->slot(c, tPast);
-            }
-            Fields<float, 5> f5;
-            for (int c = 0; c < 5; ++c) {
-                f5.now[c] = fj.now[c];
-                f5.past[c] = fj.past[c];
-            }
-            // the pair tile where the lattice's own layout allows it: the choice
-            // depends on the lattice alone, never on its company
-            const bool moore = h->p.model == LAT_MODEL_MOORE;
-            const bool pair = moore ? pair_ok(h->geom, fj) : pair_ok(h->geom, f5);
-            BatchStep& T = b->tab_host[kTables * s + (pair ? 2 : 0) + (moore ? 1 : 0)];
+            const Fields<float, 7> fj = level_fields(h, n);
+            const bool pair = plan[q].table >= 2;
+            BatchStep& T = b->tab_host[kTables * s + plan[q].table];
             BatchJob& J = T.jobs[T.njobs];
             std::memset(&J, 0, sizeof(J));
             J.g = h->geom;
@@ -483,7 +512,7 @@ int lat_batch_advance(lat_batch* b, int32_t nsteps)
     }
     BATCH_CK(cudaGraphLaunch(b->exec, b->stream));
     BATCH_CK(cudaStreamSynchronize(b->stream));
-    b->launches += kTables * (int64_t)K;
+    b->launches += (int64_t)__builtin_popcount(mask) * K;
     int active = 0;
     for (size_t q = 0; q < b->jobs.size(); ++q) {
         auto& j = b->jobs[q];
