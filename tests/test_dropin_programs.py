@@ -170,6 +170,14 @@ def test_icw_program_loop_collision_reproduces_reference_output(tmp_path):
         assert np.max(np.abs(final[c] - z["final"][c])) <= 1e-12 * ref, c
 
 
+def test_icw_program_default_ic_needs_the_profile_table(tmp_path):
+    """With no ic_type, bin/ic_w_evolution builds what the reference's ships
+    with, ic_func.cpp's "loop collision" (:25), from Data/SOR_Fields.txt
+    (ic_func.cpp:978); without the table it stops with that file's name."""
+    r = _run("ic_w_evolution", tmp_path, {"nx": 5, "ny": 5, "nz": 5, "nt": 1})
+    assert r.returncode != 0 and b"Data/SOR_Fields.txt" in r.stderr
+
+
 def test_icw_program_rejects_unprovided_ic(tmp_path):
     r = _run("ic_w_evolution", tmp_path, {"nx": 4, "ny": 4, "nz": 4, "nt": 1, "ic_type": "NG sine"})
     assert r.returncode == 2 and b"ic_type" in r.stderr
